@@ -1,0 +1,656 @@
+// canon_bibd.cu -- canonicity test of rank-2 incidence matrices (BIBDs, STS) on sm_103a.
+//
+// One thread owns one matrix and runs the reference's search order exactly:
+//   TestCanonicity()            Source/CanonicityChecker.h:255-586 (numParts == 1)
+//   checkColOrbit()             Source/CanonicityChecker.cpp:191-223
+//   next_permutation()          k-Factorization/Utils/Include/GroupOrder.h:136-248
+//   addAutomorphism()/UpdateOrbits()/updateGroupOrder()   GroupOrder.h:30-102
+// The permutation and its orbits are nibble-packed in two registers (v <= 16);
+// every row is one uint64 bit set (b <= 63); the column orbits of level r are a
+// bit mask of orbit-start columns (ColOrbitManager's per-row lists become one
+// word per row).  The column arrangement of the permuted matrix (permColumn)
+// lives in shared memory as bytes.  Items are taken from a global ticket
+// counter so that a thread that finishes a cheap (rejected) matrix immediately
+// takes the next one.
+#include "canon_internal.h"
+
+namespace canon {
+
+namespace {
+
+constexpr int TPB = 64;                  // threads per block (one matrix each)
+constexpr uint64_t ID16 = 0xFEDCBA9876543210ull;
+constexpr uint64_t NIB1 = 0x1111111111111111ull;
+
+__device__ __forceinline__ unsigned pg(uint64_t p, unsigned i) {
+    return (unsigned)(p >> ((i & 15u) << 2)) & 15u;
+}
+__device__ __forceinline__ uint64_t ps(uint64_t p, unsigned i, unsigned x) {
+    const unsigned sh = (i & 15u) << 2;
+    return (p & ~(15ull << sh)) | ((uint64_t)(x & 15u) << sh);
+}
+
+// revert(), GroupOrder.h:25-28: reverse positions i+1 .. j-1
+__device__ __forceinline__ uint64_t revert(uint64_t p, unsigned j, unsigned i) {
+    while (++i < --j) {
+        const unsigned a = pg(p, i), c = pg(p, j);
+        p = ps(p, i, c);
+        p = ps(p, j, a);
+    }
+    return p;
+}
+
+struct Group {
+    uint64_t perm, orb;     // nibble-packed permRow() and row orbits
+    unsigned stab;          // stabilizerLength()
+    unsigned stab_aut;      // stabilizerLengthAut()
+    uint64_t ord_lo, ord_hi;
+};
+
+__device__ __forceinline__ void mul_order(uint64_t &lo, uint64_t &hi, uint64_t m) {
+    const uint64_t nlo = lo * m;
+    hi = hi * m + __umul64hi(lo, m);
+    lo = nlo;
+}
+
+// orbit length of stabilizerLengthAut(), updateGroupOrder() GroupOrder.h:63-73
+__device__ __forceinline__ unsigned orbit_len(const Group &g, unsigned n) {
+    unsigned len = 1;
+    unsigned idx = g.stab_aut & 0xFFFFu;
+    while (++idx < n)
+        if (pg(g.orb, idx) == g.stab_aut)
+            len++;
+    return len;
+}
+
+// next_permutation(), GroupOrder.h:136-248 (the recursive call becomes a second pass)
+__device__ unsigned next_perm(Group &g, unsigned n, unsigned idx, unsigned lenStab) {
+    for (int pass = 0; pass < 2; ++pass) {
+        uint64_t perm = g.perm;
+        const uint64_t orb = g.orb;
+        unsigned temp, i, j;
+        if (idx == IMAX && pg(perm, g.stab) == n - 1)
+            idx = EMAX;
+        if (idx == IMAX) {
+            i = g.stab;
+            idx = i;
+            temp = pg(perm, i);
+            for (j = n; --j > temp;)
+                perm = ps(perm, j, j);
+            unsigned k = j++;
+            while (k-- > i)
+                perm = ps(perm, k + 1, k);
+        } else if (idx >= IMAX) {
+            j = i = n;
+            while (--i > 0 && pg(perm, i - 1) >= pg(perm, i))
+                ;
+            if (i == lenStab) {
+                g.perm = perm;
+                return EMAX;
+            }
+            temp = pg(perm, --i);
+            while (pg(perm, --j) <= temp)
+                ;
+        } else {
+            i = j = idx;
+            temp = pg(perm, i);
+            while (++j < n && pg(perm, j) <= temp)
+                ;
+            if (j >= n) {
+                g.perm = revert(perm, n, i);
+                idx = EMAX;
+                lenStab = 0;
+                continue;
+            }
+        }
+
+        if (g.stab == i) {
+            bool flag = false;
+            unsigned k = j, tmp = pg(perm, j);
+            if (idx >= IMAX) {
+                while (k > i && pg(orb, pg(perm, k)) != pg(perm, k))
+                    k--;
+                if (k != j) {
+                    if (!k) {
+                        g.perm = perm;
+                        return EMAX;
+                    }
+                    flag = (k == i);
+                    tmp = pg(perm, k--);
+                    while (++k < j)
+                        perm = ps(perm, k, pg(perm, k + 1));
+                }
+            } else {
+                while (k < n && pg(orb, pg(perm, k)) != pg(perm, k))
+                    k++;
+                if (k != j) {
+                    flag = (k == n);
+                    if (flag) {
+                        if (!i) {
+                            g.perm = perm;
+                            return EMAX;
+                        }
+                        k = (idx - 1) & 0xFFu;           // uint8 arithmetic of the reference
+                        while ((k = (k + 1) & 0xFFu) < j)
+                            perm = ps(perm, k, k);
+                    } else {
+                        tmp = pg(perm, k++);
+                        while (--k > j)
+                            perm = ps(perm, k, pg(perm, k - 1));
+                    }
+                }
+            }
+            perm = ps(perm, j, tmp);
+            if (flag) {
+                j = idx >= IMAX ? n - 1 : i;
+                temp = pg(perm, --i);
+                g.stab = i;
+            }
+        }
+
+        perm = ps(perm, i, pg(perm, j));
+        perm = ps(perm, j, temp);
+        if (idx >= IMAX) {
+            if (g.stab > i)
+                g.stab = i;
+            perm = revert(perm, n, i);
+        }
+        g.perm = perm;
+        return i;
+    }
+    return EMAX;  // not reached
+}
+
+// Update_Orbits(), GroupOrder.h:30-49, on nibble-packed orbits (SWAR replace)
+__device__ __forceinline__ uint64_t merge_orbits(uint64_t perm, uint64_t orb, unsigned n, unsigned idx,
+                                                 uint64_t nmask1) {
+    do {
+        unsigned a = pg(orb, idx);
+        unsigned c = pg(orb, pg(perm, idx));
+        if (a == c)
+            continue;
+        if (c < a) {
+            const unsigned t = a;
+            a = c;
+            c = t;
+        }
+        const uint64_t t = orb ^ (NIB1 * c);
+        uint64_t y = t | (t >> 1);
+        y |= y >> 2;
+        const uint64_t z = ~y & nmask1;          // nibble LSB set where the nibble equals c
+        const uint64_t m = z * 15u;
+        orb = (orb & ~m) | ((NIB1 * a) & m);
+    } while (++idx < n);
+    return orb;
+}
+
+struct Smem {
+    uint64_t *rows;  // rows[r * TPB]
+    uint64_t *lvl;   // lvl[r * TPB]: orbit-start masks of level r (also scratch)
+    uint8_t *pc;     // pc[j * TPB]: permColumn
+};
+
+#define R_(r) sm.rows[(r) * TPB]
+#define L_(r) sm.lvl[(r) * TPB]
+#define PC_(j) sm.pc[(j) * TPB]
+
+struct CheckOut {
+    uint8_t canonical, status, reject_row, rtc;
+    uint64_t witness;
+    uint64_t aut_lo, aut_hi;
+    uint64_t trials;
+    uint16_t n_auts;
+    uint8_t len_aut;
+};
+
+// Brings the columns into orbit normal form: sorted in decreasing order of their
+// pattern read from row 0 down.  Equal in content to GenerateBinaryColumnOrbits()
+// applied to rows 0..n-1 (MatrixCanonChecker.cpp:186-263), which swaps the first 0
+// and the last 1 inside every orbit until each row is 1s-first.
+__device__ void normalize_columns(Smem sm, unsigned n, unsigned b) {
+    // codes (16 bit) are kept four to a word in the lvl scratch area
+    for (unsigned c = 0; c < b; ++c) {
+        unsigned code = 0;
+        for (unsigned r = 0; r < n; ++r)
+            code = (code << 1) | (unsigned)((R_(r) >> c) & 1u);
+        const unsigned w = c >> 2, sh = (c & 3u) * 16u;
+        uint64_t cur = (c & 3u) ? L_(w) : 0ull;
+        cur = (cur & ~(0xFFFFull << sh)) | ((uint64_t)code << sh);
+        L_(w) = cur;
+    }
+    uint64_t acc[VMAX];
+#pragma unroll
+    for (unsigned r = 0; r < VMAX; ++r)
+        acc[r] = 0;
+    for (unsigned c = 0; c < b; ++c) {
+        const unsigned kc = (unsigned)(L_(c >> 2) >> ((c & 3u) * 16u)) & 0xFFFFu;
+        unsigned rank = 0;
+        for (unsigned c2 = 0; c2 < b; ++c2) {
+            const unsigned k2 = (unsigned)(L_(c2 >> 2) >> ((c2 & 3u) * 16u)) & 0xFFFFu;
+            rank += (k2 > kc) || (k2 == kc && c2 < c);
+        }
+#pragma unroll
+        for (unsigned r = 0; r < VMAX; ++r)
+            if (r < n)
+                acc[r] |= (uint64_t)((kc >> (n - 1 - r)) & 1u) << rank;
+    }
+#pragma unroll
+    for (unsigned r = 0; r < VMAX; ++r)
+        if (r < n)
+            R_(r) = acc[r];
+}
+
+// Orbit-start masks of every level; returns false if a row is not 1s-first
+// inside the orbits of the rows above it.
+__device__ bool build_levels(Smem sm, unsigned n, unsigned b) {
+    const uint64_t cols = (1ull << b) - 1ull;
+    uint64_t m = 1ull;
+    bool ok = true;
+    for (unsigned r = 0; r < n; ++r) {
+        L_(r) = m;
+        const uint64_t x = R_(r);
+        if (x & ~cols)
+            ok = false;
+        if (x & ~(x << 1) & ~m & cols & ~1ull)
+            ok = false;
+        m |= (x ^ (x << 1)) & cols & ~1ull;
+    }
+    L_(n) = m;
+    return ok;
+}
+
+// TestCanonicity() for one matrix whose rows are in shared memory.
+__device__ void check_one(Smem sm, unsigned n, unsigned b, unsigned flags, uint64_t max_trials,
+                          uint8_t *aut_dst, unsigned aut_cap, CheckOut &o) {
+    o.canonical = 1;
+    o.status = 0;
+    o.reject_row = 0xFF;
+    o.rtc = 0xFF;
+    o.witness = ~0ull;
+    o.aut_lo = 1;
+    o.aut_hi = 0;
+    o.trials = 0;
+    o.n_auts = 0;
+    o.len_aut = 0;
+
+    if (flags & F_RAW)
+        normalize_columns(sm, n, b);
+    if (!build_levels(sm, n, b)) {
+        o.status = ST_BADINPUT;
+        o.canonical = 0;
+        return;
+    }
+    const bool row_permut = flags & F_COMPLETE;
+    const bool full = flags & F_FULL_AUT;
+    const bool save = (flags & F_SAVE_AUTS) && aut_dst;
+    const uint64_t nmask1 = (n >= 16) ? NIB1 : (NIB1 & ((1ull << (4 * n)) - 1ull));
+    const uint64_t lastLvl = L_(n);
+    const uint64_t sentinel = 1ull << b;
+
+    for (unsigned j = 0; j < b; ++j)
+        PC_(j) = (uint8_t)j;
+
+    // init(), CanonicityChecker.cpp:35-84
+    Group g;
+    g.perm = ID16;
+    g.orb = ID16;
+    g.stab = n - 1;
+    g.stab_aut = EMAX;
+    g.ord_lo = 1;
+    g.ord_hi = 0;
+    uint64_t part_lo = 1, part_hi = 0;   // |Aut| of a partial matrix (addition)
+    unsigned n_auts = 0;
+    if (row_permut) {
+        n_auts = 1;                      // the trivial row permutation is saved by init()
+        o.len_aut = (uint8_t)n;
+        if (save && aut_cap)
+            for (unsigned i = 0; i < n; ++i)
+                aut_dst[i] = (uint8_t)i;
+    }
+    bool rejected = false;
+    bool overflow = false;
+
+    unsigned nRow = EMAX;
+    uint64_t trials = 0;
+    for (;;) {
+        nRow = next_perm(g, n, nRow, 0);
+        if (nRow == EMAX)
+            break;
+        if (++trials > max_trials) {
+            o.status |= ST_TIMEOUT;
+            break;
+        }
+        bool greater = false;
+        for (; nRow < n; ++nRow) {
+            const uint64_t x = R_(nRow);
+            const uint64_t y = R_(pg(g.perm, nRow));
+            const uint64_t m = L_(nRow) | sentinel;
+            unsigned s = 0;
+            int diff = 0;
+            while (s < b) {
+                const unsigned e = __ffsll((long long)(m & (~0ull << (s + 1)))) - 1;
+                if (e == s + 1) {
+                    diff = (int)((x >> s) & 1u) - (int)((y >> PC_(s)) & 1u);
+                } else {
+                    const uint64_t rng = ((1ull << (e - s)) - 1ull) << s;
+                    const int c1 = __popcll(x & rng);
+                    int n1 = 0;
+                    for (unsigned jj = s; jj < e; ++jj)
+                        n1 += (int)((y >> PC_(jj)) & 1u);
+                    diff = c1 - n1;
+                    if (!diff && n1 && n1 < (int)(e - s)) {
+                        // permColumn reordered inside the orbit: columns holding a 1 first
+                        unsigned lo = s, hi = e - 1;
+                        while (lo < hi) {
+                            while (lo < hi && ((y >> PC_(lo)) & 1u))
+                                ++lo;
+                            while (lo < hi && !((y >> PC_(hi)) & 1u))
+                                --hi;
+                            if (lo < hi) {
+                                const uint8_t t = PC_(lo);
+                                PC_(lo) = PC_(hi);
+                                PC_(hi) = t;
+                            }
+                        }
+                    }
+                }
+                if (diff)
+                    break;
+                s = e;
+            }
+            if (diff > 0) {
+                greater = true;
+                break;
+            }
+            if (diff < 0) {
+                if (!rejected) {
+                    rejected = true;
+                    o.canonical = 0;
+                    o.reject_row = (uint8_t)nRow;
+                    o.witness = g.perm;
+                    unsigned rtc = nRow;                 // rowToChange(), CanonicityChecker.cpp:320-330
+                    for (unsigned i = 0; i <= nRow; ++i)
+                        if (rtc < pg(g.perm, i))
+                            rtc = pg(g.perm, i);
+                    o.rtc = (uint8_t)rtc;
+                }
+                greater = true;                          // FULL_AUT: continue as after a prune
+                break;
+            }
+        }
+        if (rejected && !full)
+            break;
+        if (greater)
+            continue;
+
+        // automorphism found, CanonicityChecker.h:421-476
+        const uint64_t moved = g.perm ^ ID16;
+        const unsigned first = moved ? (unsigned)(__ffsll((long long)moved) - 1) >> 2 : n;
+        if (!row_permut) {
+            if (save) {
+                // permutation of the column orbits of the last level (:430-450)
+                const unsigned len = __popcll(lastLvl & ((1ull << b) - 1ull));
+                o.len_aut = (uint8_t)len;
+                if (n_auts == 0) {
+                    if (aut_cap)
+                        for (unsigned q = 0; q < len; ++q)
+                            aut_dst[q] = (uint8_t)q;
+                    n_auts = 1;
+                }
+                if (n_auts < aut_cap) {
+                    uint8_t *dst = aut_dst + n_auts * 64u;
+                    uint64_t starts = lastLvl & ((1ull << b) - 1ull);
+                    unsigned q = 0;
+                    while (starts) {
+                        const unsigned s0 = __ffsll((long long)starts) - 1;
+                        starts &= starts - 1;
+                        const unsigned col = PC_(s0);
+                        dst[q++] = (uint8_t)(__popcll(lastLvl & ((2ull << col) - 1ull)) - 1);
+                    }
+                } else {
+                    overflow = true;
+                }
+                ++n_auts;
+            }
+            if (g.stab_aut > first)
+                mul_order(part_lo, part_hi, orbit_len(g, n));
+        }
+        // addAutomorphism() -> udpdateStabLength() + Update_Orbits()
+        if (row_permut && g.stab_aut > first)
+            mul_order(g.ord_lo, g.ord_hi, orbit_len(g, n));
+        g.stab_aut = first;
+        g.stab = first;
+        g.orb = merge_orbits(g.perm, g.orb, n, first, nmask1);
+        if (row_permut && save) {
+            if (n_auts < aut_cap) {
+                uint8_t *dst = aut_dst + n_auts * 64u;
+                for (unsigned i = 0; i < n; ++i)
+                    dst[i] = (uint8_t)pg(g.perm, i);
+            } else {
+                overflow = true;
+            }
+            ++n_auts;
+        }
+        nRow = IMAX;
+    }
+
+    if (row_permut) {
+        mul_order(g.ord_lo, g.ord_hi, orbit_len(g, n));
+        o.aut_lo = g.ord_lo;
+        o.aut_hi = g.ord_hi;
+    } else {
+        mul_order(part_lo, part_hi, orbit_len(g, n));
+        o.aut_lo = part_lo;
+        o.aut_hi = part_hi;
+    }
+    if (rejected && !full) {
+        o.aut_lo = 0;                    // the reference leaves |Aut| undefined here
+        o.aut_hi = 0;
+    }
+    if (o.status & ST_TIMEOUT)
+        o.canonical = 0;
+    if (overflow)
+        o.status |= ST_PERM_OVF;
+    o.trials = trials;
+    o.n_auts = (uint16_t)(n_auts > 0xFFFFu ? 0xFFFFu : n_auts);
+}
+
+__device__ __forceinline__ void store_witness(uint8_t *dst16, uint64_t w, unsigned n) {
+    uint32_t wd[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const unsigned i = q * 4 + k;
+            const unsigned byte = (w == ~0ull || i >= n) ? 0xFFu : pg(w, i);
+            v |= byte << (8 * k);
+        }
+        wd[q] = v;
+    }
+    reinterpret_cast<uint4 *>(dst16)[0] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+}
+
+__global__ void __launch_bounds__(TPB) bibd_items_kernel(const Item *__restrict__ items, uint32_t n_items,
+                                                         const uint64_t *__restrict__ words, Outputs out,
+                                                         uint64_t max_trials, unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint8_t s_pc[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, s_pc + tid};
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= n_items)
+            break;
+        const Item item = items[it];
+        const unsigned n = item.nrows, b = item.ncols, o_i = item.out_idx;
+        CheckOut o;
+        if (item.kind != KIND_BIBD || n < 1 || n > VMAX || b < 1 || b > BMAX) {
+            o = CheckOut{0, ST_BADINPUT, 0xFF, 0xFF, ~0ull, 0, 0, 0, 0, 0};
+        } else {
+            for (unsigned r = 0; r < n; ++r)
+                R_(r) = words[item.data_off + r];
+            uint8_t *adst = (item.flags & F_SAVE_AUTS) && out.auts
+                                ? out.auts + (size_t)o_i * out.aut_cap * 64u
+                                : nullptr;
+            check_one(sm, n, b, item.flags, max_trials, adst, out.aut_cap, o);
+        }
+        out.canonical[o_i] = o.canonical;
+        out.status[o_i] = o.status;
+        out.reject_row[o_i] = o.reject_row;
+        out.row_to_change[o_i] = o.rtc;
+        out.player_index[o_i] = -1;
+        store_witness(out.witness + (size_t)o_i * 16u, o.witness, n);
+        out.aut[2 * (size_t)o_i] = o.aut_lo;
+        out.aut[2 * (size_t)o_i + 1] = o.aut_hi;
+        out.trials[o_i] = o.trials;
+        out.n_auts[o_i] = o.n_auts;
+        out.len_aut[o_i] = o.len_aut;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) bibd_uniform_kernel(uint32_t n_items, uint32_t v, uint32_t b,
+                                                           uint32_t flags, const uint64_t *__restrict__ rows,
+                                                           uint8_t *canonical, uint8_t *witness16, uint64_t *aut,
+                                                           uint8_t *status, uint64_t *trials_out,
+                                                           uint64_t max_trials, unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint8_t s_pc[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, s_pc + tid};
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= n_items)
+            break;
+        for (unsigned r = 0; r < v; ++r)
+            R_(r) = rows[(size_t)it * v + r];
+        CheckOut o;
+        check_one(sm, v, b, flags & ~F_SAVE_AUTS, max_trials, nullptr, 0, o);
+        canonical[it] = o.canonical;
+        if (witness16)
+            store_witness(witness16 + (size_t)it * 16u, o.witness, v);
+        if (aut) {
+            aut[2 * (size_t)it] = o.aut_lo;
+            aut[2 * (size_t)it + 1] = o.aut_hi;
+        }
+        if (status)
+            status[it] = o.status;
+        if (trials_out)
+            trials_out[it] = o.trials;
+    }
+}
+
+// CanonizeMatrix(k = 0), MatrixCanonChecker.cpp:420-496: repeat the complete check,
+// move the rows as the witness says, renormalise the columns, until canonical.
+__global__ void __launch_bounds__(TPB) bibd_canonize_kernel(uint32_t n_items, uint32_t v, uint32_t b,
+                                                            uint64_t *rows, uint64_t *aut, uint8_t *status,
+                                                            uint32_t stride_items, uint32_t first_item,
+                                                            uint64_t max_trials, unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint8_t s_pc[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, s_pc + tid};
+    for (;;) {
+        const unsigned t = atomicAdd(ticket, 1u);
+        const uint64_t it64 = (uint64_t)first_item + (uint64_t)t * stride_items;
+        if (it64 >= n_items)
+            break;
+        const size_t it = (size_t)it64;
+        for (unsigned r = 0; r < v; ++r)
+            R_(r) = rows[it * v + r];
+        CheckOut o;
+        uint8_t st = 0;
+        for (int round = 0; round < 256; ++round) {
+            check_one(sm, v, b, F_COMPLETE | F_RAW, max_trials, nullptr, 0, o);
+            if (o.status) {
+                st = o.status;
+                break;
+            }
+            if (o.canonical)
+                break;
+            uint64_t tmp[VMAX];
+#pragma unroll
+            for (unsigned r = 0; r < VMAX; ++r)
+                tmp[r] = (r < v) ? R_(r) : 0ull;
+            for (unsigned r = 0; r < v; ++r) {
+                const unsigned src = pg(o.witness, r);
+                uint64_t val = 0;
+#pragma unroll
+                for (unsigned q = 0; q < VMAX; ++q)
+                    if (q == src)
+                        val = tmp[q];
+                R_(r) = val;
+            }
+            if (round == 255)
+                st = ST_TIMEOUT;
+        }
+        for (unsigned r = 0; r < v; ++r)
+            rows[it * v + r] = R_(r);
+        if (aut) {
+            aut[2 * it] = o.aut_lo;
+            aut[2 * it + 1] = o.aut_hi;
+        }
+        if (status)
+            status[it] = st;
+    }
+}
+
+int blocks_for(const void *kernel, int num_sms) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TPB, 0);
+    if (per_sm < 1)
+        per_sm = 1;
+    return per_sm * (num_sms > 0 ? num_sms : 1);
+}
+
+}  // namespace
+
+cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint64_t *d_words, Outputs out,
+                              uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
+    if (!n_items)
+        return cudaSuccess;
+    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
+    int grid = blocks_for((const void *)bibd_items_kernel, num_sms);
+    const int need = (int)((n_items + TPB - 1) / TPB);
+    if (grid > need)
+        grid = need;
+    bibd_items_kernel<<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
+                                      const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16,
+                                      uint64_t *d_aut, uint8_t *d_status, uint64_t *d_trials,
+                                      uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
+    if (!n)
+        return cudaSuccess;
+    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
+    int grid = blocks_for((const void *)bibd_uniform_kernel, num_sms);
+    const int need = (int)((n + TPB - 1) / TPB);
+    if (grid > need)
+        grid = need;
+    bibd_uniform_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut, d_status,
+                                             d_trials, max_trials, tk);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bibd_canonize(uint32_t n, uint32_t v, uint32_t b, uint64_t *d_rows, uint64_t *d_aut,
+                                 uint8_t *d_status, uint32_t stride_items, uint32_t first_item,
+                                 uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
+    if (!n || first_item >= n || !stride_items)
+        return cudaSuccess;
+    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
+    int grid = blocks_for((const void *)bibd_canonize_kernel, num_sms);
+    const uint32_t cnt = (n - first_item + stride_items - 1) / stride_items;
+    const int need = (int)((cnt + TPB - 1) / TPB);
+    if (grid > need)
+        grid = need;
+    bibd_canonize_kernel<<<grid, TPB, 0, s>>>(n, v, b, d_rows, d_aut, d_status, stride_items, first_item,
+                                              max_trials, tk);
+    return cudaGetLastError();
+}
+
+}  // namespace canon

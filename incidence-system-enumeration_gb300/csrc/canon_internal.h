@@ -1,0 +1,67 @@
+// canon_internal.h -- shared definitions of the device kernels and the C-ABI layer.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace canon {
+
+constexpr unsigned VMAX = 16;        // rows of an incidence matrix (nibble-packed permutations)
+constexpr unsigned BMAX = 63;        // columns (one uint64 per row, bit b is the orbit sentinel)
+constexpr unsigned KS_NPMAX = 12;    // k-system players (group size 2, <= 6 groups)
+constexpr unsigned EMAX = 255;       // ELEMENT_MAX
+constexpr unsigned IMAX = 254;       // IDX_MAX
+
+// one work item: a matrix to check (16 bytes)
+struct Item {
+    uint32_t data_off;   // BIBD: offset in uint64 words; k-sys: offset in bytes
+    uint8_t  kind;       // 0 = BIBD, 1 = k-system
+    uint8_t  nrows;      // rows / rounds filled
+    uint8_t  ncols;      // b / numPlayers
+    uint8_t  flags;      // CANON_* batch flags
+    uint32_t out_idx;    // output slot
+    uint32_t pad;
+};
+
+enum : uint8_t { KIND_BIBD = 0, KIND_KSYS = 1 };
+
+// structure-of-arrays outputs, all indexed by Item::out_idx
+struct Outputs {
+    uint8_t  *canonical;
+    uint8_t  *status;
+    uint8_t  *reject_row;
+    uint8_t  *row_to_change;
+    int32_t  *player_index;
+    uint8_t  *witness;      // 16 bytes per item
+    uint64_t *aut;          // 2 per item
+    uint64_t *trials;
+    uint16_t *n_auts;
+    uint8_t  *len_aut;
+    uint8_t  *auts;         // aut_cap * 64 bytes per item
+    uint32_t  aut_cap;
+};
+
+// flags (same values as the public CANON_* flags)
+constexpr uint32_t F_COMPLETE = 0x1, F_RAW = 0x2, F_FULL_AUT = 0x4, F_SAVE_AUTS = 0x8;
+constexpr uint8_t ST_BADINPUT = 1, ST_TIMEOUT = 2, ST_PERM_OVF = 4;
+
+// launchers (stream-ordered; return cudaGetLastError())
+// d_ticket: one device word of scratch (the work-stealing counter), reset by the launcher
+cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint64_t *d_words,
+                              Outputs out, uint64_t max_trials, unsigned *d_ticket, int num_sms,
+                              cudaStream_t s);
+cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
+                                      const uint64_t *d_rows, uint8_t *d_canonical,
+                                      uint8_t *d_witness16, uint64_t *d_aut, uint8_t *d_status,
+                                      uint64_t *d_trials, uint64_t max_trials, unsigned *d_ticket,
+                                      int num_sms, cudaStream_t s);
+cudaError_t launch_bibd_canonize(uint32_t n, uint32_t v, uint32_t b, uint64_t *d_rows,
+                                 uint64_t *d_aut, uint8_t *d_status, uint32_t stride_items,
+                                 uint32_t first_item, uint64_t max_trials, unsigned *d_ticket,
+                                 int num_sms, cudaStream_t s);
+cudaError_t launch_sts_generate(uint32_t n, uint32_t v, uint64_t seed, uint64_t *d_rows,
+                                int num_sms, cudaStream_t s);
+cudaError_t launch_ksys_check(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes,
+                              Outputs out, unsigned *d_ticket, int num_sms, cudaStream_t s);
+cudaError_t ksys_upload_tables();
+
+}  // namespace canon

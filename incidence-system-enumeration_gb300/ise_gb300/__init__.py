@@ -1,0 +1,353 @@
+"""Host-side binding of the GB300 canonicity-check engine (libcanon_gb300.so).
+
+The engine is C-ABI native code (include/canon_gb300.h); this module is a thin
+ctypes layer for Python callers, tests and the benchmark.  It mirrors the
+reference's checker surface:
+
+  CanonicityChecker.TestCanonicity()   CCanonicityChecker::TestCanonicity(),
+                                       Source/CanonicityChecker.h:58,255-586
+  CanonicityChecker.CanonizeMatrix()   CMatrixCanonChecker::CanonizeMatrix(),
+                                       Source/MatrixCanonChecker.cpp:420-564
+  KSysChecker.cnvCheckNew()            alldata::cnvCheckNew(),
+                                       k-Factorization/TripleSys/Source/cnv.cpp:211
+
+There is no CPU fallback: if the native library is missing or no GPU is
+present, construction raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libcanon_gb300.so")
+
+CANON_OK = 0
+CANON_EINVAL = -1
+CANON_ENOMEM = -2
+CANON_ECUDA = -3
+CANON_ETIMEOUT = -4
+CANON_ENODEV = -5
+
+ST_OK = 0
+ST_BADINPUT = 1
+ST_TIMEOUT = 2
+ST_PERM_OVF = 4
+
+COMPLETE = 0x1
+RAW = 0x2
+FULL_AUT = 0x4
+SAVE_AUTS = 0x8
+
+# t_canonOutInfo of the reference (Source/CanonicityChecker.h:27-32)
+t_saveNothing = 0
+t_saveRowPermutations = 1
+t_saveColPermutations = 2
+t_saveRowToChange = 4
+
+HEADER_SYMBOLS = [
+    "canon_create", "canon_destroy", "canon_last_error", "canon_submit_bibd", "canon_submit_ksys",
+    "canon_sync", "canon_set_ordering", "canon_canonize_bibd", "canon_check_bibd_device",
+    "canon_generate_sts_device", "canon_device_alloc", "canon_device_free", "canon_memcpy_d2h",
+    "canon_memcpy_h2d", "canon_last_kernel_ms", "canon_kernel_launches", "canon_stream_sync",
+]
+
+
+class CanonError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("canon error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Cfg(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("max_items", ctypes.c_uint32),
+                ("max_words", ctypes.c_uint32), ("aut_cap", ctypes.c_uint32),
+                ("max_trials", ctypes.c_uint64)]
+
+
+class BibdBatch(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("v", ctypes.c_uint32), ("b", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("rows", ctypes.POINTER(ctypes.c_uint64)),
+                ("nrows", ctypes.POINTER(ctypes.c_uint8))]
+
+
+class KsysBatch(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("np", ctypes.c_uint32), ("rounds", ctypes.c_uint32),
+                ("flags", ctypes.c_uint32), ("data", ctypes.POINTER(ctypes.c_uint8)),
+                ("nrows", ctypes.POINTER(ctypes.c_uint8))]
+
+
+class Results(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32),
+                ("canonical", ctypes.POINTER(ctypes.c_uint8)),
+                ("status", ctypes.POINTER(ctypes.c_uint8)),
+                ("reject_row", ctypes.POINTER(ctypes.c_uint8)),
+                ("row_to_change", ctypes.POINTER(ctypes.c_uint8)),
+                ("player_index", ctypes.POINTER(ctypes.c_int32)),
+                ("witness", ctypes.POINTER(ctypes.c_uint8)),
+                ("aut", ctypes.POINTER(ctypes.c_uint64)),
+                ("trials", ctypes.POINTER(ctypes.c_uint64)),
+                ("n_auts", ctypes.POINTER(ctypes.c_uint16)),
+                ("len_aut", ctypes.POINTER(ctypes.c_uint8)),
+                ("auts", ctypes.POINTER(ctypes.c_uint8)),
+                ("aut_cap", ctypes.c_uint32),
+                ("kernel_ms", ctypes.c_float)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Loads libcanon_gb300.so and declares the C ABI.  Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise CanonError(CANON_ENODEV, "native library %s is not built (run build())" % path)
+    L = ctypes.CDLL(path)
+    vp, u32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    L.canon_create.argtypes = [ctypes.POINTER(Cfg)]
+    L.canon_create.restype = vp
+    L.canon_destroy.argtypes = [vp]
+    L.canon_last_error.argtypes = [vp]
+    L.canon_last_error.restype = ctypes.c_char_p
+    L.canon_submit_bibd.argtypes = [vp, ctypes.POINTER(BibdBatch)]
+    L.canon_submit_ksys.argtypes = [vp, ctypes.POINTER(KsysBatch)]
+    L.canon_sync.argtypes = [vp, ctypes.POINTER(Results)]
+    L.canon_set_ordering.argtypes = [vp, vp]
+    L.canon_canonize_bibd.argtypes = [vp, u32, u32, u32, u64p, u64p]
+    L.canon_check_bibd_device.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp, vp, vp, vp, vp]
+    L.canon_generate_sts_device.argtypes = [vp, u32, u32, u64, ctypes.c_int, vp, vp]
+    L.canon_device_alloc.argtypes = [vp, ctypes.c_size_t]
+    L.canon_device_alloc.restype = vp
+    L.canon_device_free.argtypes = [vp, vp]
+    L.canon_memcpy_d2h.argtypes = [vp, vp, vp, ctypes.c_size_t]
+    L.canon_memcpy_h2d.argtypes = [vp, vp, vp, ctypes.c_size_t]
+    L.canon_last_kernel_ms.argtypes = [vp]
+    L.canon_last_kernel_ms.restype = ctypes.c_float
+    L.canon_kernel_launches.argtypes = [vp]
+    L.canon_kernel_launches.restype = u64
+    L.canon_stream_sync.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def pack_rows(M):
+    """0/1 matrix (rows x b, b <= 63) -> one uint64 per row, bit c = column c."""
+    M = np.asarray(M, dtype=np.uint64)
+    w = np.uint64(1) << np.arange(M.shape[-1], dtype=np.uint64)
+    return (M * w).sum(axis=-1, dtype=np.uint64)
+
+
+def unpack_rows(words, b):
+    words = np.asarray(words, dtype=np.uint64)
+    return ((words[..., None] >> np.arange(b, dtype=np.uint64)) & np.uint64(1)).astype(np.uint8)
+
+
+class Context:
+    """One engine context (one CUDA stream) on one GPU."""
+
+    def __init__(self, device=0, max_items=1 << 16, max_words=0, aut_cap=64, max_trials=0):
+        self.lib = load_library()
+        cfg = Cfg(device, max_items, max_words, aut_cap, max_trials)
+        self.h = self.lib.canon_create(ctypes.byref(cfg))
+        if not self.h:
+            raise CanonError(CANON_ENODEV, "canon_create failed (no GPU?)")
+        self.aut_cap = aut_cap
+        self._kinds = []
+
+    def close(self):
+        if self.h:
+            self.lib.canon_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != CANON_OK:
+            raise CanonError(rc, self.lib.canon_last_error(self.h).decode())
+        return rc
+
+    def error(self):
+        return self.lib.canon_last_error(self.h).decode()
+
+    # ---- batched checks ----
+    def submit_bibd(self, rows, v, b, flags=0, nrows=None):
+        rows = np.ascontiguousarray(rows, dtype=np.uint64).reshape(-1)
+        n = rows.size // v
+        nr = None if nrows is None else np.ascontiguousarray(nrows, dtype=np.uint8)
+        bt = BibdBatch(n, v, b, flags, _ptr(rows, ctypes.c_uint64),
+                       _ptr(nr, ctypes.c_uint8) if nr is not None else None)
+        self._check(self.lib.canon_submit_bibd(self.h, ctypes.byref(bt)))
+        self._kinds += [("bibd", v, b)] * n
+        return n
+
+    def submit_ksys(self, data, np_, rounds, flags=0, nrows=None):
+        data = np.ascontiguousarray(data, dtype=np.uint8).reshape(-1)
+        n = data.size // (np_ * rounds)
+        nr = None if nrows is None else np.ascontiguousarray(nrows, dtype=np.uint8)
+        bt = KsysBatch(n, np_, rounds, flags, _ptr(data, ctypes.c_uint8),
+                       _ptr(nr, ctypes.c_uint8) if nr is not None else None)
+        self._check(self.lib.canon_submit_ksys(self.h, ctypes.byref(bt)))
+        self._kinds += [("ksys", np_, rounds)] * n
+        return n
+
+    def sync(self, allow_timeout=False):
+        r = Results()
+        rc = self.lib.canon_sync(self.h, ctypes.byref(r))
+        if rc != CANON_OK and not (allow_timeout and rc == CANON_ETIMEOUT):
+            raise CanonError(rc, self.error())
+        n = r.n
+        out = {"n": n, "kernel_ms": r.kernel_ms}
+        if n:
+            def arr(p, count, dt):
+                return np.ctypeslib.as_array(p, shape=(count,)).astype(dt, copy=True)
+            out["canonical"] = arr(r.canonical, n, np.uint8).astype(bool)
+            out["status"] = arr(r.status, n, np.uint8)
+            out["reject_row"] = arr(r.reject_row, n, np.uint8)
+            out["row_to_change"] = arr(r.row_to_change, n, np.uint8)
+            out["player_index"] = arr(r.player_index, n, np.int32)
+            out["witness"] = arr(r.witness, n * 16, np.uint8).reshape(n, 16)
+            a = arr(r.aut, 2 * n, np.uint64).reshape(n, 2)
+            out["aut"] = [int(lo) | (int(hi) << 64) for lo, hi in a]
+            out["trials"] = arr(r.trials, n, np.uint64)
+            out["n_auts"] = arr(r.n_auts, n, np.uint16)
+            out["len_aut"] = arr(r.len_aut, n, np.uint8)
+            out["auts_raw"] = np.ctypeslib.as_array(r.auts, shape=(n * r.aut_cap * 64,)).reshape(
+                n, r.aut_cap, 64).copy()
+        self._kinds = []
+        return out
+
+    def canonize_bibd(self, rows, v, b):
+        rows = np.array(rows, dtype=np.uint64, copy=True).reshape(-1)
+        n = rows.size // v
+        aut = np.zeros(2 * n, np.uint64)
+        self._check(self.lib.canon_canonize_bibd(self.h, n, v, b, _ptr(rows, ctypes.c_uint64),
+                                                 _ptr(aut, ctypes.c_uint64)))
+        return rows.reshape(n, v), [int(aut[2 * i]) | (int(aut[2 * i + 1]) << 64) for i in range(n)]
+
+    # ---- device-resident path ----
+    def alloc(self, nbytes):
+        p = self.lib.canon_device_alloc(self.h, nbytes)
+        if not p:
+            raise CanonError(CANON_ENOMEM, self.error())
+        return p
+
+    def free(self, p):
+        self._check(self.lib.canon_device_free(self.h, p))
+
+    def d2h(self, dst_array, src_ptr):
+        self._check(self.lib.canon_memcpy_d2h(self.h, dst_array.ctypes.data, src_ptr, dst_array.nbytes))
+        return dst_array
+
+    def h2d(self, dst_ptr, src_array):
+        src_array = np.ascontiguousarray(src_array)
+        self._check(self.lib.canon_memcpy_h2d(self.h, dst_ptr, src_array.ctypes.data, src_array.nbytes))
+
+    def generate_sts_device(self, n, v, seed, canon_odd, d_rows):
+        self._check(self.lib.canon_generate_sts_device(self.h, n, v, seed, int(canon_odd), d_rows, None))
+
+    def check_bibd_device(self, n, v, b, flags, d_rows, d_canonical, d_witness=None, d_aut=None,
+                          d_status=None, d_trials=None, stream=None):
+        self._check(self.lib.canon_check_bibd_device(self.h, n, v, b, flags, d_rows, d_canonical,
+                                                     d_witness, d_aut, d_status, d_trials, stream))
+
+    def stream_sync(self):
+        self._check(self.lib.canon_stream_sync(self.h))
+
+    def last_kernel_ms(self):
+        return float(self.lib.canon_last_kernel_ms(self.h))
+
+    def kernel_launches(self):
+        return int(self.lib.canon_kernel_launches(self.h))
+
+
+class CanonicityChecker:
+    """Mirror of CCanonicityChecker<uchar,uchar> for rank-2 incidence matrices.
+
+    TestCanonicity(nRowMax, matrix, outInfo) follows
+    Source/CanonicityChecker.h:255: it returns True for a canonical (partial)
+    matrix; afterwards permRow() is the first rejecting row permutation,
+    rowToChange() the backjump row (t_saveRowToChange), groupOrder() |Aut| and
+    permStorage() the automorphisms found (column-orbit permutations for partial
+    matrices, CPermutStorage layout with slot 0 the identity).
+    """
+
+    def __init__(self, nRow, nCol, ctx=None, save_automorphisms=False):
+        if nRow > 16 or nCol > 63:
+            raise CanonError(CANON_EINVAL, "this engine handles v <= 16 rows and b <= 63 columns")
+        self.nRow, self.nCol = nRow, nCol
+        self.ctx = ctx or Context(max_items=1024)
+        self.save = save_automorphisms
+        self._last = None
+
+    def TestCanonicity(self, nRowMax, matrix, outInfo=t_saveNothing, raw=False):
+        M = np.asarray(matrix, dtype=np.uint8)[:nRowMax, :self.nCol]
+        rows = pack_rows(M)
+        flags = (COMPLETE if outInfo & t_saveRowPermutations else 0) | (RAW if raw else 0)
+        flags |= SAVE_AUTS if self.save else 0
+        self.ctx.submit_bibd(rows, nRowMax, self.nCol, flags)
+        r = self.ctx.sync()
+        if r["status"][0] & ST_BADINPUT:
+            raise CanonError(CANON_EINVAL, "matrix is not in column-orbit normal form")
+        self._last = (nRowMax, r)
+        return bool(r["canonical"][0])
+
+    def permRow(self):
+        n, r = self._last
+        return r["witness"][0][:n].copy()
+
+    def rowToChange(self):
+        return int(self._last[1]["row_to_change"][0])
+
+    def groupOrder(self):
+        return self._last[1]["aut"][0]
+
+    def permStorage(self):
+        n, r = self._last
+        k, ln = int(r["n_auts"][0]), int(r["len_aut"][0])
+        return r["auts_raw"][0][:k, :ln].copy()
+
+    def CanonizeMatrix(self, matrix):
+        M = np.asarray(matrix, dtype=np.uint8)
+        rows, aut = self.ctx.canonize_bibd(pack_rows(M), M.shape[0], M.shape[1])
+        return unpack_rows(rows[0], M.shape[1]), aut[0]
+
+
+class KSysChecker:
+    """Mirror of alldata::cnvCheckNew(0, nrows) for group size 2 (k-Factorization)."""
+
+    def __init__(self, numPlayers, ctx=None, save_automorphisms=False):
+        self.np = numPlayers
+        self.ctx = ctx or Context(max_items=1024)
+        self.save = save_automorphisms
+        self._last = None
+
+    def cnvCheckNew(self, iMode, nrows, result):
+        R = np.asarray(result, dtype=np.uint8)[:nrows]
+        self.ctx.submit_ksys(R, self.np, nrows, SAVE_AUTS if self.save else 0)
+        r = self.ctx.sync()
+        if r["status"][0] & ST_BADINPUT:
+            raise CanonError(CANON_EINVAL, "rounds are not in the sorted result() form")
+        self._last = r
+        return bool(r["canonical"][0])
+
+    def playerIndex(self):
+        return int(self._last["player_index"][0])
+
+    def orderOfGroup(self):
+        return self._last["aut"][0]
+
+    def groupInfo(self):
+        r = self._last
+        k = int(r["n_auts"][0])
+        return r["auts_raw"][0][:k, :self.np].copy()

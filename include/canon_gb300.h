@@ -1,0 +1,181 @@
+/*
+ * canon_gb300.h -- C ABI of the GB300 canonicity-check engine.
+ *
+ * Drop-in for the canonicity test of andrei5055/Incidence-System-Enumeration:
+ *   - CCanonicityChecker<T,S>::TestCanonicity()      Source/CanonicityChecker.h:58,255-586
+ *     (callers Source/Enumerator.cpp:364 complete, :446-447 partial,
+ *      Source/MatrixCanonChecker.cpp:456 canonize)
+ *   - CMatrixCanonChecker::CanonizeMatrix()          Source/MatrixCanonChecker.cpp:420-564
+ *   - alldata::cnvCheckNew()                         k-Factorization/TripleSys/Source/cnv.cpp:211-351
+ *     (caller k-Factorization/TripleSys/Source/checkCurrentResult.cpp:91)
+ *   - the GPU seam TestCanonicityOnGPU() / CGPU_CanonChecker   Source/Enumerator.h:220-228,
+ *     Source/MatrixCanonChecker.h:204-350, Source/CanonicityChecker.cu:123-156
+ * Results are written in the reference's layouts: the witness is permRow(),
+ * the automorphisms of partial matrices are permutations of column orbits laid
+ * out as CPermutStorage (Source/PermutStorage.h:8-110: numPerm x lenPerm
+ * bytes, slot 0 the identity), k-system automorphisms as CGroupInfo entries
+ * (k-Factorization/TripleSys/Include/groupInfo.h:121-125).
+ *
+ * Ownership: input batches are caller-owned host memory, read during the
+ * submit call.  Results live in library-owned pinned buffers and stay valid
+ * until the next canon_sync() or canon_destroy() on the same context.
+ * Errors: every call returns a CANON_* status; nothing calls exit().
+ * Threading: one context per host thread; a context owns one CUDA stream.
+ */
+#ifndef CANON_GB300_H
+#define CANON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define CANON_OK        0
+#define CANON_EINVAL   -1   /* bad argument or malformed matrix */
+#define CANON_ENOMEM   -2   /* allocation failed / capacity exceeded */
+#define CANON_ECUDA    -3   /* CUDA runtime error */
+#define CANON_ETIMEOUT -4   /* a search hit its trial budget (per-item status says which) */
+#define CANON_ENODEV   -5   /* no usable GPU */
+
+/* ---- per-item status bits (canon_results.status[i]) ---- */
+#define CANON_ST_OK        0u
+#define CANON_ST_BADINPUT  1u   /* matrix not in the required form */
+#define CANON_ST_TIMEOUT   2u   /* trial budget exhausted: verdict invalid */
+#define CANON_ST_PERM_OVF  4u   /* automorphism arena too small: list truncated */
+
+/* ---- batch flags ---- */
+/* Complete matrix: TestCanonicity(v, .., t_saveRowPermutations | t_saveRowToChange)
+ * (Enumerator.cpp:696): witness permRow(), rowToChange() and |Aut| are reported.
+ * Without it the check is the partial one, t_saveNothing (Enumerator.cpp:446-447);
+ * |Aut| of the partial matrix is still reported (an addition). */
+#define CANON_COMPLETE    0x1u
+/* Input rows are an arbitrary 0/1 matrix: bring the columns into the orbit
+ * normal form first (GenerateBinaryColumnOrbits, MatrixCanonChecker.cpp:186-263).
+ * Without it the matrix must already be in normal form (as the enumerator
+ * builds it, MatrixCanonChecker.cpp:14-93). */
+#define CANON_RAW         0x2u
+/* Keep searching after the first rejection (treated like a "greater" prune) so
+ * that |Aut| is also reported for non-canonical matrices.  No counterpart in the
+ * reference's BIBD checker; the k-system analogue is m_doNotExitEarlyIfNotCanonical
+ * (cnv.cpp:159-160). */
+#define CANON_FULL_AUT    0x4u
+/* Store automorphisms: column-orbit permutations for partial BIBD checks
+ * (CanonicityChecker.h:427-451), every row automorphism for complete ones
+ * (t_outRowPermute), relabelings for k-systems (updateGroup, cnv.cpp:127-133). */
+#define CANON_SAVE_AUTS   0x8u
+
+/* ---- context ---- */
+typedef struct canon_ctx canon_ctx;
+
+typedef struct {
+    int      device;          /* CUDA device ordinal */
+    uint32_t max_items;       /* capacity: matrices per sync (0 = 1<<21) */
+    uint32_t max_words;       /* capacity: 64-bit input words per sync (0 = 16*max_items) */
+    uint32_t aut_cap;         /* automorphisms kept per matrix when CANON_SAVE_AUTS (0 = 64) */
+    uint64_t max_trials;      /* per-matrix trial budget (0 = 1<<28) */
+} canon_cfg;
+
+/* BIBD / incidence-system batch: n matrices of b columns (b <= 63), v rows each
+ * (v <= 16), row j of matrix i at rows[i*v + j] with bit c = column c.
+ * nrows[i] (optional, NULL = all v) is the number of filled rows of matrix i. */
+typedef struct {
+    uint32_t        n;
+    uint32_t        v;
+    uint32_t        b;
+    uint32_t        flags;
+    const uint64_t *rows;
+    const uint8_t  *nrows;
+} canon_bibd_batch;
+
+/* k-system batch (group size 2): n matrices of np players (np <= 12, even),
+ * `rounds` rounds each, round j of matrix i at data[(i*rounds + j)*np ..]
+ * as the reference's result() rows (pairs ascending, ordered by first player,
+ * round 0 = 0 1 2 .. np-1).  nrows[i] (optional) = rounds filled. */
+typedef struct {
+    uint32_t       n;
+    uint32_t       np;
+    uint32_t       rounds;
+    uint32_t       flags;
+    const uint8_t *data;
+    const uint8_t *nrows;
+} canon_ksys_batch;
+
+/* Results of every batch submitted since the previous sync, in submission
+ * order (BIBD and k-system items share one index space). */
+typedef struct {
+    uint32_t        n;              /* items */
+    const uint8_t  *canonical;      /* [n] 1 = canonical */
+    const uint8_t  *status;         /* [n] CANON_ST_* bits */
+    const uint8_t  *reject_row;     /* [n] BIBD: nRow of the first diff<0 (255 if canonical) */
+    const uint8_t  *row_to_change;  /* [n] BIBD: rowToChange(); k-sys: 255 */
+    const int32_t  *player_index;   /* [n] k-sys: m_playerIndex; BIBD: -1 */
+    const uint8_t  *witness;        /* [n*16] permRow() at rejection (BIBD), 0xFF-filled if canonical */
+    const uint64_t *aut;            /* [2n] |Aut| as (lo, hi) pairs */
+    const uint64_t *trials;         /* [n] permutations / relabelings tried */
+    const uint16_t *n_auts;         /* [n] automorphisms stored (CANON_SAVE_AUTS) incl. slot 0 */
+    const uint8_t  *len_aut;        /* [n] bytes per stored automorphism */
+    const uint8_t  *auts;           /* [n*aut_cap*64] arena, item i at i*aut_cap*64 */
+    uint32_t        aut_cap;
+    float           kernel_ms;      /* device time of the check kernels (CUDA events) */
+} canon_results;
+
+/* Learned search order: BF16 MLP 64 -> H -> H -> 1.  NULL weights = plain order. */
+typedef struct {
+    uint32_t        in_dim;         /* 64 */
+    uint32_t        hidden;         /* 128 */
+    const uint16_t *w1, *w2, *w3;   /* bf16, row-major [out][in] */
+    const float    *b1, *b2, *b3;
+} canon_mlp_weights;
+
+/* Creates a context on cfg->device.  Replaces the per-thread CGPU_CanonChecker
+ * set-up (MatrixCanonChecker.h:204-247, CanonicityChecker.cu:17-67). */
+canon_ctx *canon_create(const canon_cfg *cfg);
+void       canon_destroy(canon_ctx *ctx);
+const char *canon_last_error(const canon_ctx *ctx);
+
+/* Queue a batch of incidence matrices: one TestCanonicity() per matrix. */
+int canon_submit_bibd(canon_ctx *ctx, const canon_bibd_batch *batch);
+/* Queue a batch of k-system matrices: one cnvCheckNew(0, nrows) per matrix. */
+int canon_submit_ksys(canon_ctx *ctx, const canon_ksys_batch *batch);
+/* Copy the queued input to the GPU, run the checks, wait, expose the results. */
+int canon_sync(canon_ctx *ctx, canon_results *out);
+/* Install (or with NULL remove) the learned ordering network. */
+int canon_set_ordering(canon_ctx *ctx, const canon_mlp_weights *w);
+
+/* CanonizeMatrix(k = 0) for a batch of complete incidence matrices, in place on
+ * host memory (rows as in canon_bibd_batch, all v rows filled).  aut_out[2n]
+ * (optional) receives |Aut|.  MatrixCanonChecker.cpp:420-564. */
+int canon_canonize_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint64_t *rows,
+                        uint64_t *aut_out);
+
+/* ---- device-resident entry points (inputs already in HBM) ---- */
+/* Same check as canon_submit_bibd + canon_sync for device pointers, all items
+ * with v rows; launched on `stream` (a cudaStream_t, NULL = the context's).
+ * Output arrays are device pointers (any may be NULL except canonical). */
+int canon_check_bibd_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
+                            const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16,
+                            uint64_t *d_aut, uint8_t *d_status, uint64_t *d_trials, void *stream);
+/* Seeded STS(v) batch on the device (Stinson hill-climbing + uniform row and
+ * column permutations); if canon_odd, odd items are replaced by their
+ * canonical form.  rows: device pointer [n*v]. */
+int canon_generate_sts_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint64_t seed, int canon_odd,
+                              uint64_t *d_rows, void *stream);
+/* Device memory helpers so callers without a CUDA toolchain can hold batches in HBM. */
+void *canon_device_alloc(canon_ctx *ctx, size_t bytes);
+int   canon_device_free(canon_ctx *ctx, void *p);
+int   canon_memcpy_d2h(canon_ctx *ctx, void *dst, const void *src, size_t bytes);
+int   canon_memcpy_h2d(canon_ctx *ctx, void *dst, const void *src, size_t bytes);
+/* Device time (ms, CUDA events on the launching stream) of the last kernel issued by
+ * canon_check_bibd_device / canon_sync. */
+float canon_last_kernel_ms(const canon_ctx *ctx);
+/* Number of kernels this context launched since creation. */
+uint64_t canon_kernel_launches(const canon_ctx *ctx);
+int canon_stream_sync(canon_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CANON_GB300_H */
