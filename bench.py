@@ -1,0 +1,317 @@
+"""Benchmark of the canonicity-check hot path on one GB300.
+
+Workload (one "step"): the exact canonicity check of 1,048,576 STS(15)
+incidence matrices (15 x 35, one uint64 per row): item i is a random STS(15)
+(Stinson hill-climbing, seed 20241203 + splitmix stream i) under a uniform row
+and column permutation; odd items are replaced by their canonical form
+(CanonizeMatrix).  Per matrix the check reports the canonical flag, the first
+rejecting row permutation (witness) and |Aut| (the search continues past a
+rejection to count the group).  The batch is generated on the GPU once, before
+timing.
+
+  value : checks/s with the batch resident in HBM (canon_check_bibd_device),
+          CUDA events on the launching stream, L2 flushed between steps.
+  e2e   : checks/s through the public batch API with host buffers
+          (canon_submit_bibd + canon_sync: pinned staging, H2D, kernel, D2H of
+          every result array), host wall clock.
+
+`--impl reference` times the CPU restatement of the reference checker (the
+oracle) on all host cores over a bounded sample of the same workload.
+"""
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "incidence-system-enumeration_gb300"))
+
+N_ITEMS = 1 << 20
+V, B = 15, 35
+SEED = 20241203
+FLAGS_NAME = "COMPLETE|RAW|FULL_AUT"
+METRIC = "exact canonicity checks/sec (STS(15) 15x35, plain order)"
+WORKLOAD = ("1,048,576 STS(15) 15x35 bit-packed matrices, seed %d, odd items canonical; "
+            "outputs canonical flag + first rejecting permutation + |Aut|" % SEED)
+IN_BYTES = V * 8          # packed rows read per check
+OUT_BYTES = 1 + 16 + 16   # flag + witness + |Aut| written per check
+MEASURED_PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out", "clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        os.makedirs(os.path.dirname(self.path), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        try:
+            rows = [l.split(",") for l in open(self.path).read().splitlines() if l.strip()]
+        except Exception:
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                    reasons.add(name)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample_rows(n):
+    """The first n items of the workload, built on the CPU by the oracle's
+    restatement of the generator and canonizer (same streams as the device)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    rows = np.stack([oracle.sts_random_rows(V, SEED, i) for i in range(n)])
+
+    def canon(i):
+        M = oracle.rows_to_matrix(rows[i], B)
+        C, _, _ = oracle.bibd_canonize(M)
+        return i, (C.astype(np.uint64) << np.arange(B, dtype=np.uint64)).sum(axis=1, dtype=np.uint64)
+
+    with cf.ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        for i, r in ex.map(canon, range(1, n, 2)):
+            rows[i] = r
+    return rows
+
+
+def cpu_check_rate(rows, threads, budget_s):
+    """Oracle checks/s over `rows` on `threads` host threads (ctypes releases the GIL)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    flags = oracle.SAVE_ROW_PERM | oracle.SAVE_ROW_TO_CHANGE | oracle.FULL_AUT
+
+    def one(i):
+        M = oracle.bibd_normalize(oracle.rows_to_matrix(rows[i], B))
+        return oracle.bibd_test(M, flags)["canonical"]
+
+    done = 0
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        idx = 0
+        while idx < len(rows):
+            chunk = list(range(idx, min(len(rows), idx + 4 * threads)))
+            list(ex.map(one, chunk))
+            done += len(chunk)
+            idx += len(chunk)
+            if time.perf_counter() - t0 > budget_s:
+                break
+    dt = time.perf_counter() - t0
+    return done / dt, done, dt
+
+
+def run_reference(args, rank, world, dist):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = 32 * threads
+    rows = cpu_sample_rows(sample)
+    for _ in range(args.warmup):
+        cpu_check_rate(rows[: 2 * threads], threads, 60)
+    rates = []
+    t_all = 0.0
+    n_all = 0
+    for _ in range(args.steps):
+        rate, done, dt = cpu_check_rate(rows, threads, 120)
+        rates.append(rate)
+        t_all += dt
+        n_all += done
+    value = n_all / t_all
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "checks/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_all / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/u64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "ordering": "plain", "l2": "n/a (host CPU)"},
+        "cpu_baseline": {"value": value, "unit": "checks/s", "cores": threads, "kind": "port",
+                         "sample": "first %d items of the workload per step (%d checks/step)"
+                                   % (len(rows), len(rows))},
+        "e2e": {"value": value, "unit": "checks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, local, dist):
+    import ise_gb300 as G
+    ctx = G.Context(device=local, max_items=N_ITEMS, max_words=N_ITEMS * V, aut_cap=1)
+    flags = G.COMPLETE | G.RAW | G.FULL_AUT
+    n = N_ITEMS
+    d_rows = ctx.alloc(n * V * 8)
+    d_can = ctx.alloc(n)
+    d_wit = ctx.alloc(n * 16)
+    d_aut = ctx.alloc(n * 16)
+    d_st = ctx.alloc(n)
+    ctx.generate_sts_device(n, V, SEED, True, d_rows)
+    ctx.stream_sync()
+    l2_flush = ctx.alloc(512 << 20)
+    zeros = np.zeros(512 << 20, np.uint8)
+
+    def flush_l2():
+        ctx.h2d(l2_flush, zeros)
+
+    for _ in range(args.warmup):
+        ctx.check_bibd_device(n, V, B, flags, d_rows, d_can, d_wit, d_aut, d_st)
+        ctx.stream_sync()
+    launches0 = ctx.kernel_launches()
+    times = []
+    barrier(dist)
+    ctx.stream_sync()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush_l2()
+            ctx.check_bibd_device(n, V, B, flags, d_rows, d_can, d_wit, d_aut, d_st)
+            ctx.stream_sync()
+            times.append(ctx.last_kernel_ms())
+    barrier(dist)
+    launches = ctx.kernel_launches() - launches0
+    t_total = max_over_ranks(dist, sum(times) / 1e3)
+    st = ctx.d2h(np.zeros(n, np.uint8), d_st)
+    can = ctx.d2h(np.zeros(n, np.uint8), d_can)
+    if st.any():
+        raise SystemExit("bench: %d items reported a bad status" % int((st != 0).sum()))
+    value = world * n * args.steps / t_total
+    ms_step = 1e3 * t_total / args.steps
+    hbm, src = peaks()
+    achieved = (IN_BYTES + OUT_BYTES) * n / (min(times) / 1e3) / 1e9
+
+    # end to end through the batch API with host buffers
+    host_rows = ctx.d2h(np.zeros(n * V, np.uint64), d_rows)
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.submit_bibd(host_rows, V, B, flags)
+        res = ctx.sync()
+    e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    assert res["n"] == n and np.array_equal(res["canonical"].astype(np.uint8), can)
+    h2d = n * V * 8 + n * 16
+    d2h = n * (1 + 1 + 1 + 1 + 4 + 16 + 16 + 8 + 2 + 1)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        sample = min(n, 64 * threads)
+        rows_s = host_rows.reshape(n, V)[:sample]
+        rate, done, dt = cpu_check_rate(rows_s, threads, 30)
+        cpu = {"value": rate, "unit": "checks/s", "cores": threads, "kind": "port",
+               "sample": "first %d items of the same batch (%d checked in %.1f s)" % (sample, done, dt)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "checks/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64 bit rows / u8", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "ordering": "plain", "flags": FLAGS_NAME,
+                       "items_per_step": n, "canonical_fraction": float(can.mean()),
+                       "l2": "flushed between steps (512 MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": world * n / e2e_dt, "unit": "checks/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None,
+                         "note": "peak %s; the check is an integer search (ALU/issue bound), HBM "
+                                 "traffic is %d B per check" % (src, IN_BYTES + OUT_BYTES)},
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    for p in (d_rows, d_can, d_wit, d_aut, d_st, l2_flush):
+        ctx.free(p)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    rank, world, local, dist = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, rank, world, dist)
+    else:
+        run_gpu(args, rank, world, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -40,7 +40,7 @@ struct Cand {
 
 __device__ __forceinline__ void eval_candidate(unsigned c, unsigned np, unsigned ng, unsigned nr,
                                                const uint64_t *seq, const uint64_t *part,
-                                               const uint64_t *pair, Cand &o) {
+                                               const uint64_t *pair, bool consecutive, Cand &o) {
     const unsigned d = c % nr;
     const unsigned qd = c / nr;
     const unsigned t = qd & ((1u << ng) - 1u);
@@ -66,16 +66,29 @@ __device__ __forceinline__ void eval_candidate(unsigned c, unsigned np, unsigned
     for (unsigned x = 0; x < np; ++x)
         inv = nib_set(inv, nib_get(ttr, x), x);
     o.inv = inv;
-    unsigned daymax = d;
     const unsigned u = nib_get(inv, 0);
-    for (unsigned i = 1; i < nr; ++i) {
-        const unsigned w = nib_get(inv, i + 1u);
-        const unsigned rr = nib_get(pair[u], w);
-        if (!rr) {            // no round gives second entry i+1: the sorted result is greater
-            o.res = 2;
-            return;
+    // second entries (partner of label 0) of the relabelled rounds; the sorted
+    // form lists the rounds in increasing order of it (kmSortRowsBy2ndValue)
+    unsigned second = 0;
+    if (!consecutive)
+        for (unsigned r = 0; r < nr; ++r)
+            second |= 1u << nib_get(ttr, nib_get(part[r], u));
+    unsigned daymax = d;
+    for (unsigned i = consecutive ? 1u : 0u; i < nr; ++i) {
+        unsigned w;
+        if (consecutive) {
+            // rounds 0..i-1 matched second entries 1..i; equality needs i+1 next
+            w = nib_get(inv, i + 1u);
+            if (!nib_get(pair[u], w)) {
+                o.res = 2;
+                return;
+            }
+        } else {
+            const unsigned tv = __ffs(second) - 1u;
+            second &= second - 1u;
+            w = nib_get(inv, tv);
         }
-        const unsigned r = rr - 1u;
+        const unsigned r = nib_get(pair[u], w) - 1u;
         const uint64_t pr = part[r];
         uint64_t q = 0;
         for (unsigned x = 0; x < np; ++x)
@@ -86,6 +99,8 @@ __device__ __forceinline__ void eval_candidate(unsigned c, unsigned np, unsigned
                 daymax = r;
             continue;
         }
+        // rounds in canonical pair order compare like their partner tables: the
+        // first player whose partner differs decides
         const unsigned x0 = (unsigned)(__ffsll((long long)(q ^ orig)) - 1) >> 2;
         if (nib_get(q, x0) < nib_get(orig, x0)) {
             o.res = -1;
@@ -171,9 +186,7 @@ __global__ void __launch_bounds__(KTPB) ksys_kernel(const Item *__restrict__ ite
                 pt = nib_set(pt, x, y);
                 pt = nib_set(pt, y, x);
             }
-            // rounds sorted by their second entry, round 0 = 0 1 2 .. np-1
-            if (nib_get(pt, 0) != lane + 1u)
-                ok = false;
+            // round 0 = 0 1 2 .. np-1 (the first round is fixed)
             if (lane == 0)
                 for (unsigned p = 0; p < np; ++p)
                     if (row[p] != p)
@@ -182,6 +195,9 @@ __global__ void __launch_bounds__(KTPB) ksys_kernel(const Item *__restrict__ ite
             part[lane] = pt;
         }
         ok = __all_sync(0xFFFFFFFFu, ok);
+        // fast path when round i pairs player 0 with i+1 (every canonical matrix does)
+        const bool consecutive =
+            __all_sync(0xFFFFFFFFu, !(ok && lane < nr) || nib_get(part[lane], 0) == lane + 1u);
         __syncwarp();
         if (ok && lane < np) {
             uint64_t pr = 0;
@@ -209,7 +225,7 @@ __global__ void __launch_bounds__(KTPB) ksys_kernel(const Item *__restrict__ ite
                 Cand o;
                 o.res = 1;
                 if (c < total)
-                    eval_candidate(c, np, ng, nr, seq, part, pair, o);
+                    eval_candidate(c, np, ng, nr, seq, part, pair, consecutive, o);
                 const unsigned rej = __ballot_sync(0xFFFFFFFFu, c < total && o.res < 0);
                 unsigned aut = __ballot_sync(0xFFFFFFFFu, c < total && o.res == 0);
                 unsigned upto = (total - base < 32u) ? (total - base) : 32u;
