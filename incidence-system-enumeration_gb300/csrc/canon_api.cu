@@ -196,7 +196,7 @@ int canon_submit_bibd(canon_ctx *c, const canon_bibd_batch *bt) {
         return CANON_OK;
     if (!bt->rows || bt->v < 1 || bt->v > canon::VMAX || bt->b < 1 || bt->b > canon::BMAX)
         return fail(c, CANON_EINVAL, "bibd batch: need rows, 1 <= v <= 16, 1 <= b <= 63");
-    if (bt->flags & ~0xFu)
+    if (bt->flags & ~0x1Fu)
         return fail(c, CANON_EINVAL, "bibd batch: unknown flags");
     const uint32_t total = c->n_bitems + c->n_kitems;
     if ((uint64_t)total + bt->n > c->cfg.max_items)
@@ -411,8 +411,9 @@ int canon_check_bibd_device(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, ui
                             uint8_t *d_status, uint64_t *d_trials, void *stream) {
     if (!c || !d_rows || !d_canonical)
         return fail(c, CANON_EINVAL, "null argument");
-    if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x7u))
-        return fail(c, CANON_EINVAL, "check: need 1 <= v <= 16, 1 <= b <= 63, flags in COMPLETE|RAW|FULL_AUT");
+    if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x17u))
+        return fail(c, CANON_EINVAL,
+                    "check: need 1 <= v <= 16, 1 <= b <= 63, flags in COMPLETE|RAW|FULL_AUT|AUT_CANON");
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
     cudaEventRecord(c->ev0, s);

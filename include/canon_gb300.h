@@ -66,6 +66,12 @@ extern "C" {
  * (CanonicityChecker.h:427-451), every row automorphism for complete ones
  * (t_outRowPermute), relabelings for k-systems (updateGroup, cnv.cpp:127-133). */
 #define CANON_SAVE_AUTS   0x8u
+/* Complete matrices only: |Aut| of a rejected matrix is taken from its canonical
+ * form, reached the way CanonizeMatrix() does (MatrixCanonChecker.cpp:420-496:
+ * move the rows as the witness says, renormalise the columns, check again until
+ * canonical).  The flag, witness and row_to_change stay those of the first check.
+ * Much cheaper than CANON_FULL_AUT on non-canonical matrices. */
+#define CANON_AUT_CANON   0x10u
 
 /* ---- context ---- */
 typedef struct canon_ctx canon_ctx;
@@ -154,7 +160,8 @@ int canon_canonize_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint
 /* ---- device-resident entry points (inputs already in HBM) ---- */
 /* Same check as canon_submit_bibd + canon_sync for device pointers, all items
  * with v rows; launched on `stream` (a cudaStream_t, NULL = the context's).
- * Output arrays are device pointers (any may be NULL except canonical). */
+ * Output arrays are device pointers (any may be NULL except canonical).
+ * flags: CANON_COMPLETE, CANON_RAW, CANON_FULL_AUT, CANON_AUT_CANON. */
 int canon_check_bibd_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                             const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16,
                             uint64_t *d_aut, uint8_t *d_status, uint64_t *d_trials, void *stream);

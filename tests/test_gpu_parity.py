@@ -18,7 +18,10 @@ def oracle_bibd(M, gflags):
     if gflags & G.SAVE_AUTS and gflags & G.COMPLETE:
         f |= oracle.SAVE_AUT_ROWS
     X = oracle.bibd_normalize(M) if gflags & G.RAW else M
-    return oracle.bibd_test(X, f, perm_cap=64 if gflags & G.SAVE_AUTS else 0)
+    o = oracle.bibd_test(X, f, perm_cap=64 if gflags & G.SAVE_AUTS else 0)
+    if gflags & G.AUT_CANON and not o["canonical"]:
+        _, o["aut"], _ = oracle.bibd_canonize(X)
+    return o
 
 
 def compare_bibd(ctx, mats, gflags, v, b):
@@ -41,7 +44,7 @@ def compare_bibd(ctx, mats, gflags, v, b):
             assert bytes(r["witness"][i][:n]) == o["witness"], i
             if gflags & G.COMPLETE:
                 assert int(r["row_to_change"][i]) == o["row_to_change"], i
-        if o["canonical"] or gflags & G.FULL_AUT:
+        if o["canonical"] or gflags & (G.FULL_AUT | G.AUT_CANON):
             assert r["aut"][i] == o["aut"], (i, r["aut"][i], o["aut"])
         if gflags & G.SAVE_AUTS:
             k = int(r["n_auts"][i])
@@ -53,10 +56,19 @@ def compare_bibd(ctx, mats, gflags, v, b):
 
 
 def test_sts15_complete_raw_full_aut(ctx):
-    mats = [oracle.rows_to_matrix(oracle.sts_random_rows(15, 2024, i), 35) for i in range(96)]
+    mats = [oracle.rows_to_matrix(oracle.sts_random_rows(15, 2024, i), 35) for i in range(12)]
     sts = cases.load_sts15()
-    mats += [M for M, _ in sts[::3]]
+    mats += [M for M, _ in sts[::5]]
     compare_bibd(ctx, mats, G.COMPLETE | G.RAW | G.FULL_AUT, 15, 35)
+
+
+def test_sts15_complete_aut_by_canonization(ctx):
+    mats = [oracle.rows_to_matrix(oracle.sts_random_rows(15, 4048, i), 35) for i in range(128)]
+    sts = cases.load_sts15()
+    mats += [M for M, _ in sts[1::3]]
+    r = compare_bibd(ctx, mats, G.COMPLETE | G.RAW | G.AUT_CANON, 15, 35)
+    fixture = {a for _, a in sts}
+    assert all(a in fixture for a in r["aut"])
 
 
 def test_sts15_complete_reference_semantics(ctx):
@@ -130,7 +142,7 @@ def test_device_entry_point_matches_batched_path(ctx):
     d_st = ctx.alloc(n)
     try:
         ctx.generate_sts_device(n, 15, 5, True, d_rows)
-        ctx.check_bibd_device(n, 15, 35, G.COMPLETE | G.RAW | G.FULL_AUT, d_rows, d_can, d_wit, d_aut, d_st)
+        ctx.check_bibd_device(n, 15, 35, G.COMPLETE | G.RAW | G.AUT_CANON, d_rows, d_can, d_wit, d_aut, d_st)
         ctx.stream_sync()
         rows = ctx.d2h(np.zeros(n * 15, np.uint64), d_rows).reshape(n, 15)
         can = ctx.d2h(np.zeros(n, np.uint8), d_can)
@@ -144,7 +156,7 @@ def test_device_entry_point_matches_batched_path(ctx):
     sts = {M.tobytes(): a for M, a in cases.load_sts15()}
     for i in range(n):
         M = oracle.rows_to_matrix(rows[i], 35)
-        o = oracle_bibd(M, G.COMPLETE | G.RAW | G.FULL_AUT)
+        o = oracle_bibd(M, G.COMPLETE | G.RAW | G.AUT_CANON)
         assert bool(can[i]) == o["canonical"]
         assert int(aut[i][0]) == o["aut"]
         if not o["canonical"]:
