@@ -1,0 +1,609 @@
+// canon_bibd_core.cuh -- device search of the rank-2 incidence-matrix checker.
+//
+// Included by canon_bibd.cu; written in plain CUDA C++ so that the same
+// functions can also be compiled for the host.
+#pragma once
+#include "canon_internal.h"
+#include "canon_nibble.cuh"
+
+namespace canon {
+namespace bibd {
+
+constexpr int TPB = 64;                  // threads per block (one matrix each)
+constexpr uint64_t ID16 = 0xFEDCBA9876543210ull;
+constexpr uint64_t NIB1 = 0x1111111111111111ull;
+
+__device__ __forceinline__ unsigned pg(uint64_t p, unsigned i) {
+    return (unsigned)(p >> ((i & 15u) << 2)) & 15u;
+}
+__device__ __forceinline__ uint64_t ps(uint64_t p, unsigned i, unsigned x) {
+    const unsigned sh = (i & 15u) << 2;
+    return (p & ~(15ull << sh)) | ((uint64_t)(x & 15u) << sh);
+}
+
+// revert(), GroupOrder.h:25-28: reverse positions i+1 .. j-1
+__device__ __forceinline__ uint64_t revert(uint64_t p, unsigned j, unsigned i) {
+    while (++i < --j) {
+        const unsigned a = pg(p, i), c = pg(p, j);
+        p = ps(p, i, c);
+        p = ps(p, j, a);
+    }
+    return p;
+}
+
+struct Group {
+    uint64_t perm, orb;     // nibble-packed permRow() and row orbits
+    unsigned stab;          // stabilizerLength()
+    unsigned stab_aut;      // stabilizerLengthAut()
+    uint64_t ord_lo, ord_hi;
+};
+
+__device__ __forceinline__ void mul_order(uint64_t &lo, uint64_t &hi, uint64_t m) {
+    const uint64_t nlo = lo * m;
+    hi = hi * m + __umul64hi(lo, m);
+    lo = nlo;
+}
+
+// orbit length of stabilizerLengthAut(), updateGroupOrder() GroupOrder.h:63-73
+__device__ __forceinline__ unsigned orbit_len(const Group &g, unsigned n) {
+    unsigned len = 1;
+    unsigned idx = g.stab_aut & 0xFFFFu;
+    while (++idx < n)
+        if (pg(g.orb, idx) == g.stab_aut)
+            len++;
+    return len;
+}
+
+// next_permutation(), GroupOrder.h:136-248 (the recursive call becomes a second pass)
+__device__ unsigned next_perm(Group &g, unsigned n, unsigned idx, unsigned lenStab) {
+    for (int pass = 0; pass < 2; ++pass) {
+        uint64_t perm = g.perm;
+        const uint64_t orb = g.orb;
+        unsigned temp, i, j;
+        if (idx == IMAX && pg(perm, g.stab) == n - 1)
+            idx = EMAX;
+        if (idx == IMAX) {
+            i = g.stab;
+            idx = i;
+            temp = pg(perm, i);
+            for (j = n; --j > temp;)
+                perm = ps(perm, j, j);
+            unsigned k = j++;
+            while (k-- > i)
+                perm = ps(perm, k + 1, k);
+        } else if (idx >= IMAX) {
+            j = i = n;
+            while (--i > 0 && pg(perm, i - 1) >= pg(perm, i))
+                ;
+            if (i == lenStab) {
+                g.perm = perm;
+                return EMAX;
+            }
+            temp = pg(perm, --i);
+            while (pg(perm, --j) <= temp)
+                ;
+        } else {
+            i = j = idx;
+            temp = pg(perm, i);
+            while (++j < n && pg(perm, j) <= temp)
+                ;
+            if (j >= n) {
+                g.perm = revert(perm, n, i);
+                idx = EMAX;
+                lenStab = 0;
+                continue;
+            }
+        }
+
+        if (g.stab == i) {
+            bool flag = false;
+            unsigned k = j, tmp = pg(perm, j);
+            if (idx >= IMAX) {
+                while (k > i && pg(orb, pg(perm, k)) != pg(perm, k))
+                    k--;
+                if (k != j) {
+                    if (!k) {
+                        g.perm = perm;
+                        return EMAX;
+                    }
+                    flag = (k == i);
+                    tmp = pg(perm, k--);
+                    while (++k < j)
+                        perm = ps(perm, k, pg(perm, k + 1));
+                }
+            } else {
+                while (k < n && pg(orb, pg(perm, k)) != pg(perm, k))
+                    k++;
+                if (k != j) {
+                    flag = (k == n);
+                    if (flag) {
+                        if (!i) {
+                            g.perm = perm;
+                            return EMAX;
+                        }
+                        k = (idx - 1) & 0xFFu;           // uint8 arithmetic of the reference
+                        while ((k = (k + 1) & 0xFFu) < j)
+                            perm = ps(perm, k, k);
+                    } else {
+                        tmp = pg(perm, k++);
+                        while (--k > j)
+                            perm = ps(perm, k, pg(perm, k - 1));
+                    }
+                }
+            }
+            perm = ps(perm, j, tmp);
+            if (flag) {
+                j = idx >= IMAX ? n - 1 : i;
+                temp = pg(perm, --i);
+                g.stab = i;
+            }
+        }
+
+        perm = ps(perm, i, pg(perm, j));
+        perm = ps(perm, j, temp);
+        if (idx >= IMAX) {
+            if (g.stab > i)
+                g.stab = i;
+            perm = revert(perm, n, i);
+        }
+        g.perm = perm;
+        return i;
+    }
+    return EMAX;  // not reached
+}
+
+// Update_Orbits(), GroupOrder.h:30-49, on nibble-packed orbits (SWAR replace)
+__device__ __forceinline__ uint64_t merge_orbits(uint64_t perm, uint64_t orb, unsigned n, unsigned idx,
+                                                 uint64_t nmask1) {
+    do {
+        unsigned a = pg(orb, idx);
+        unsigned c = pg(orb, pg(perm, idx));
+        if (a == c)
+            continue;
+        if (c < a) {
+            const unsigned t = a;
+            a = c;
+            c = t;
+        }
+        const uint64_t t = orb ^ (NIB1 * c);
+        uint64_t y = t | (t >> 1);
+        y |= y >> 2;
+        const uint64_t z = ~y & nmask1;          // nibble LSB set where the nibble equals c
+        const uint64_t m = z * 15u;
+        orb = (orb & ~m) | ((NIB1 * a) & m);
+    } while (++idx < n);
+    return orb;
+}
+
+struct Smem {
+    uint64_t *rows;  // rows[r * TPB]: row r as a bit set of columns
+    uint64_t *lvl;   // lvl[r * TPB]: orbit-start masks of level r (also scratch)
+    uint8_t *pc;     // pc[j * TPB]: permColumn
+    uint16_t *cm;    // cm[c * TPB]: column c as a bit set of rows
+    uint32_t *vd;    // vd[r * TPB]: verdicts at level r, bits 0-15 "greater" (reject), 16-31 "equal"
+};
+
+#define R_(r) sm.rows[(r) * TPB]
+#define L_(r) sm.lvl[(r) * TPB]
+#define PC_(j) sm.pc[(j) * TPB]
+#define CM_(c) sm.cm[(c) * TPB]
+#define VD_(r) sm.vd[(r) * TPB]
+
+struct CheckOut {
+    uint8_t canonical, status, reject_row, rtc;
+    uint64_t witness;
+    uint64_t aut_lo, aut_hi;
+    uint64_t trials;
+    uint16_t n_auts;
+    uint8_t len_aut;
+};
+
+// Brings the columns into orbit normal form: sorted in decreasing order of their
+// pattern read from row 0 down.  Equal in content to GenerateBinaryColumnOrbits()
+// applied to rows 0..n-1 (MatrixCanonChecker.cpp:186-263), which swaps the first 0
+// and the last 1 inside every orbit until each row is 1s-first.
+__device__ void normalize_columns(Smem sm, unsigned n, unsigned b) {
+    // codes (16 bit) are kept four to a word in the lvl scratch area
+    for (unsigned c = 0; c < b; ++c) {
+        unsigned code = 0;
+        for (unsigned r = 0; r < n; ++r)
+            code = (code << 1) | (unsigned)((R_(r) >> c) & 1u);
+        const unsigned w = c >> 2, sh = (c & 3u) * 16u;
+        uint64_t cur = (c & 3u) ? L_(w) : 0ull;
+        cur = (cur & ~(0xFFFFull << sh)) | ((uint64_t)code << sh);
+        L_(w) = cur;
+    }
+    uint64_t acc[VMAX];
+#pragma unroll
+    for (unsigned r = 0; r < VMAX; ++r)
+        acc[r] = 0;
+    for (unsigned c = 0; c < b; ++c) {
+        const unsigned kc = (unsigned)(L_(c >> 2) >> ((c & 3u) * 16u)) & 0xFFFFu;
+        unsigned rank = 0;
+        for (unsigned c2 = 0; c2 < b; ++c2) {
+            const unsigned k2 = (unsigned)(L_(c2 >> 2) >> ((c2 & 3u) * 16u)) & 0xFFFFu;
+            rank += (k2 > kc) || (k2 == kc && c2 < c);
+        }
+#pragma unroll
+        for (unsigned r = 0; r < VMAX; ++r)
+            if (r < n)
+                acc[r] |= (uint64_t)((kc >> (n - 1 - r)) & 1u) << rank;
+    }
+#pragma unroll
+    for (unsigned r = 0; r < VMAX; ++r)
+        if (r < n)
+            R_(r) = acc[r];
+}
+
+// Orbit-start masks of every level and the column-major copy of the matrix;
+// returns false if a row is not 1s-first inside the orbits of the rows above it.
+__device__ bool build_levels(Smem sm, unsigned n, unsigned b) {
+    const uint64_t cols = (1ull << b) - 1ull;
+    uint64_t m = 1ull;
+    bool ok = true;
+    for (unsigned r = 0; r < n; ++r) {
+        L_(r) = m;
+        const uint64_t x = R_(r);
+        if (x & ~cols)
+            ok = false;
+        if (x & ~(x << 1) & ~m & cols & ~1ull)
+            ok = false;
+        m |= (x ^ (x << 1)) & cols & ~1ull;
+    }
+    L_(n) = m;
+    for (unsigned c = 0; c < b; ++c) {
+        unsigned col = 0;
+        for (unsigned r = 0; r < n; ++r)
+            col |= (unsigned)((R_(r) >> c) & 1u) << r;
+        CM_(c) = (uint16_t)col;
+    }
+    return ok;
+}
+
+// Verdicts of every row as the candidate for position `lv` (the comparison of
+// row lv of the matrix with the candidate row under the current column
+// arrangement, checkColOrbit() CanonicityChecker.cpp:191-223 and :349-365),
+// evaluated for all rows at once: each orbit of level lv is one bit-parallel
+// step over the row masks of its image columns.
+__device__ void level_verdicts(Smem sm, unsigned lv, unsigned b, unsigned allrows) {
+    const uint64_t x = R_(lv);
+    const uint64_t m = L_(lv) | (1ull << b);
+    unsigned undec = allrows, rej = 0;
+    unsigned s = 0;
+    while (s < b && undec) {
+        const unsigned e = __ffsll((long long)(m & (~0ull << (s + 1)))) - 1;
+        if (e == s + 1) {
+            const unsigned ones = CM_(PC_(s));
+            if ((x >> s) & 1u) {
+                undec &= ones;                 // a 0 against the matrix's 1: smaller, pruned
+            } else {
+                rej |= undec & ones;           // a 1 against 0: the permuted matrix is greater
+                undec &= ~ones;
+            }
+        } else {
+            const unsigned len = e - s;
+            const unsigned c = __popcll(x & (((1ull << len) - 1ull) << s));
+            // bit-sliced per-row counts of 1s among the image columns of the orbit
+            unsigned p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
+            for (unsigned j = s; j < e; ++j) {
+                unsigned carry = CM_(PC_(j)), t;
+                t = p0 & carry; p0 ^= carry; carry = t;
+                t = p1 & carry; p1 ^= carry; carry = t;
+                t = p2 & carry; p2 ^= carry; carry = t;
+                t = p3 & carry; p3 ^= carry; carry = t;
+                t = p4 & carry; p4 ^= carry; carry = t;
+                p5 ^= carry;
+            }
+            const unsigned pl[6] = {p0, p1, p2, p3, p4, p5};
+            unsigned gt = 0, eq = 0xFFFFFFFFu;
+#pragma unroll
+            for (int k = 5; k >= 0; --k) {
+                if ((c >> k) & 1u) {
+                    eq &= pl[k];
+                } else {
+                    gt |= eq & pl[k];
+                    eq &= ~pl[k];
+                }
+            }
+            rej |= undec & gt;
+            undec &= eq;
+        }
+        s = e;
+    }
+    VD_(lv) = (rej & 0xFFFFu) | ((undec & 0xFFFFu) << 16);
+}
+
+// The column arrangement for level lv+1 after row `cand` compared equal at level
+// lv: inside every orbit of level lv that row lv splits, the image columns holding
+// a 1 in row `cand` move to the front (the reordering of checkColOrbit()).
+__device__ void refine(Smem sm, unsigned lv, unsigned cand, unsigned b) {
+    const uint64_t x = R_(lv);
+    const uint64_t m = L_(lv) | (1ull << b);
+    uint64_t split = L_(lv + 1) & ~L_(lv);   // starts of the second parts
+    while (split) {
+        const unsigned t = __ffsll((long long)split) - 1;
+        split &= split - 1;
+        // the orbit [s, e) of level lv containing t
+        const uint64_t below = L_(lv) & ((1ull << t) - 1ull);
+        const unsigned s = 63 - __clzll((long long)below);
+        const unsigned e = __ffsll((long long)(m & (~0ull << (s + 1)))) - 1;
+        (void)x;
+        unsigned lo = s, hi = e - 1;
+        while (lo < hi) {
+            while (lo < hi && ((CM_(PC_(lo)) >> cand) & 1u))
+                ++lo;
+            while (lo < hi && !((CM_(PC_(hi)) >> cand) & 1u))
+                --hi;
+            if (lo < hi) {
+                const uint8_t tmp = PC_(lo);
+                PC_(lo) = PC_(hi);
+                PC_(hi) = tmp;
+            }
+        }
+    }
+}
+
+// the set of entries at positions 0..i of a nibble-packed permutation
+__device__ __forceinline__ unsigned prefix_set(uint64_t perm, unsigned i) {
+    unsigned m = 0;
+    for (unsigned p = 0; p <= i; ++p)
+        m |= 1u << nib_get(perm, p);
+    return m;
+}
+
+// positions i+1.. of perm := the elements of `set` in increasing order
+__device__ __forceinline__ uint64_t write_suffix(uint64_t perm, unsigned i, unsigned set) {
+    unsigned p = i + 1;
+    while (set) {
+        const unsigned t = __ffs(set) - 1;
+        set &= set - 1;
+        perm = ps(perm, p++, t);
+    }
+    return perm;
+}
+
+// TestCanonicity() for one matrix whose rows are in shared memory: the
+// reference's search order (next_permutation() over row permutations with the
+// orbit pruning of the automorphisms found so far), with every comparison of
+// a candidate row taken from the verdict masks of its level.  A run of
+// candidates that compare "smaller" at one position (each of which the
+// reference tries and prunes in turn) is passed over in one step; the trial
+// count still counts each of them.
+__device__ void search(Smem sm, unsigned n, unsigned b, unsigned flags, uint64_t max_trials, uint8_t *aut_dst,
+                       unsigned aut_cap, CheckOut &o) {
+    const bool row_permut = flags & F_COMPLETE;
+    const bool full = flags & F_FULL_AUT;
+    const bool save = (flags & F_SAVE_AUTS) && aut_dst;
+    const uint64_t nmask1 = (n >= 16) ? NIB1 : (NIB1 & ((1ull << (4 * n)) - 1ull));
+    const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
+    const uint64_t lastLvl = L_(n);
+    const uint64_t colsMask = (1ull << b) - 1ull;
+
+    for (unsigned j = 0; j < b; ++j)
+        PC_(j) = (uint8_t)j;
+    // verdicts along the trivial permutation (every prefix of it compares equal)
+    for (unsigned lv = 0; lv < n; ++lv) {
+        level_verdicts(sm, lv, b, allrows);
+        if (lv + 1 < n)
+            refine(sm, lv, lv, b);
+    }
+
+    // init(), CanonicityChecker.cpp:35-84
+    Group g;
+    g.perm = ID16;
+    g.orb = ID16;
+    g.stab = n - 1;
+    g.stab_aut = EMAX;
+    g.ord_lo = 1;
+    g.ord_hi = 0;
+    uint64_t part_lo = 1, part_hi = 0;   // |Aut| of a partial matrix (addition)
+    unsigned n_auts = 0;
+    o.n_auts = 0;
+    o.len_aut = 0;
+    if (row_permut) {
+        n_auts = 1;                      // the trivial row permutation is saved by init()
+        o.len_aut = (uint8_t)n;
+        if (save && aut_cap)
+            for (unsigned i = 0; i < n; ++i)
+                aut_dst[i] = (uint8_t)i;
+    }
+    bool rejected = false, overflow = false;
+    uint64_t trials = 0;
+
+    unsigned i = next_perm(g, n, EMAX, 0);
+    while (i != EMAX) {
+        if (++trials > max_trials) {
+            o.status |= ST_TIMEOUT;
+            break;
+        }
+        bool descended_to_end = false;
+        for (;;) {
+            const unsigned x = pg(g.perm, i);
+            const unsigned vd = VD_(i);
+            const bool is_rej = (vd >> x) & 1u;
+            const bool is_eq = (vd >> (16 + x)) & 1u;
+            if (is_rej && !rejected) {
+                rejected = true;
+                o.canonical = 0;
+                o.reject_row = (uint8_t)i;
+                o.witness = g.perm;
+                unsigned rtc = i;                        // rowToChange(), CanonicityChecker.cpp:320-330
+                for (unsigned q = 0; q <= i; ++q)
+                    if (rtc < pg(g.perm, q))
+                        rtc = pg(g.perm, q);
+                o.rtc = (uint8_t)rtc;
+                if (!full)
+                    break;
+            }
+            if (is_eq) {
+                refine(sm, i, x, b);
+                if (i + 1 == n) {
+                    descended_to_end = true;
+                    break;
+                }
+                ++i;
+                level_verdicts(sm, i, b, allrows);
+                continue;
+            }
+            // pruned at position i ("smaller", or "greater" once counting |Aut| only)
+            if (g.stab != i) {
+                const unsigned used = prefix_set(g.perm, i);
+                const unsigned rest = allrows & ~used;
+                const unsigned larger = rest & ~((2u << x) - 1u);
+                const unsigned good = larger & ((vd >> 16) | (full ? 0u : vd));
+                if (good) {
+                    const unsigned y = __ffs(good) - 1;
+                    const unsigned skipped = __popc(larger & ((1u << y) - 1u));
+                    trials += skipped + 1;
+                    if (trials > max_trials) {
+                        o.status |= ST_TIMEOUT;
+                        i = EMAX;
+                        break;
+                    }
+                    g.perm = ps(g.perm, i, y);
+                    g.perm = write_suffix(g.perm, i, (rest & ~(1u << y)) | (1u << x));
+                    continue;
+                }
+                trials += __popc(larger);
+                if (larger) {
+                    const unsigned mx = 31 - __clz(larger);
+                    g.perm = ps(g.perm, i, mx);
+                    g.perm = write_suffix(g.perm, i, (rest & ~(1u << mx)) | (1u << x));
+                }
+            }
+            i = next_perm(g, n, i, 0);
+            break;
+        }
+        if (rejected && !full)
+            break;
+        if (!descended_to_end)
+            continue;
+
+        // automorphism found, CanonicityChecker.h:421-476
+        const uint64_t moved = g.perm ^ ID16;
+        const unsigned first = moved ? (unsigned)(__ffsll((long long)moved) - 1) >> 2 : n;
+        if (!row_permut) {
+            if (save) {
+                // permutation of the column orbits of the last level (:430-450)
+                const unsigned len = __popcll(lastLvl & colsMask);
+                o.len_aut = (uint8_t)len;
+                if (n_auts == 0) {
+                    if (aut_cap)
+                        for (unsigned q = 0; q < len; ++q)
+                            aut_dst[q] = (uint8_t)q;
+                    n_auts = 1;
+                }
+                if (n_auts < aut_cap) {
+                    uint8_t *dst = aut_dst + n_auts * 64u;
+                    uint64_t starts = lastLvl & colsMask;
+                    unsigned q = 0;
+                    while (starts) {
+                        const unsigned s0 = __ffsll((long long)starts) - 1;
+                        starts &= starts - 1;
+                        const unsigned col = PC_(s0);
+                        dst[q++] = (uint8_t)(__popcll(lastLvl & ((2ull << col) - 1ull)) - 1);
+                    }
+                } else {
+                    overflow = true;
+                }
+                ++n_auts;
+            }
+            if (g.stab_aut > first)
+                mul_order(part_lo, part_hi, orbit_len(g, n));
+        }
+        // addAutomorphism() -> udpdateStabLength() + Update_Orbits()
+        if (row_permut && g.stab_aut > first)
+            mul_order(g.ord_lo, g.ord_hi, orbit_len(g, n));
+        g.stab_aut = first;
+        g.stab = first;
+        g.orb = merge_orbits(g.perm, g.orb, n, first, nmask1);
+        if (row_permut && save) {
+            if (n_auts < aut_cap) {
+                uint8_t *dst = aut_dst + n_auts * 64u;
+                for (unsigned q = 0; q < n; ++q)
+                    dst[q] = (uint8_t)pg(g.perm, q);
+            } else {
+                overflow = true;
+            }
+            ++n_auts;
+        }
+        i = next_perm(g, n, IMAX, 0);
+    }
+
+    if (row_permut) {
+        mul_order(g.ord_lo, g.ord_hi, orbit_len(g, n));
+        o.aut_lo = g.ord_lo;
+        o.aut_hi = g.ord_hi;
+    } else {
+        mul_order(part_lo, part_hi, orbit_len(g, n));
+        o.aut_lo = part_lo;
+        o.aut_hi = part_hi;
+    }
+    if (rejected && !full) {
+        o.aut_lo = 0;                    // the reference leaves |Aut| undefined here
+        o.aut_hi = 0;
+    }
+    if (overflow)
+        o.status |= ST_PERM_OVF;
+    o.trials = trials;
+    o.n_auts = (uint16_t)(n_auts > 0xFFFFu ? 0xFFFFu : n_auts);
+}
+
+// TestCanonicity() with the batch flags; with F_AUT_CANON a rejected complete
+// matrix is then canonised (CanonizeMatrix(), MatrixCanonChecker.cpp:420-496: move
+// the rows as the witness says, renormalise, check again) and |Aut| is taken from
+// its canonical form.  Outputs other than |Aut| are those of the first check.
+__device__ void check_one(Smem sm, unsigned n, unsigned b, unsigned flags, uint64_t max_trials,
+                          uint8_t *aut_dst, unsigned aut_cap, CheckOut &o) {
+    o.canonical = 1;
+    o.status = 0;
+    o.reject_row = 0xFF;
+    o.rtc = 0xFF;
+    o.witness = ~0ull;
+    o.aut_lo = 1;
+    o.aut_hi = 0;
+    o.trials = 0;
+    o.n_auts = 0;
+    o.len_aut = 0;
+
+    if (flags & F_RAW)
+        normalize_columns(sm, n, b);
+    if (!build_levels(sm, n, b)) {
+        o.status = ST_BADINPUT;
+        o.canonical = 0;
+        return;
+    }
+    search(sm, n, b, flags, max_trials, aut_dst, aut_cap, o);
+    if ((flags & F_AUT_CANON) && (flags & F_COMPLETE) && !o.canonical && !o.status) {
+        CheckOut c = o;
+        for (int round = 0; round < 4096 && !c.canonical && !c.status; ++round) {
+            uint64_t tmp[VMAX];
+#pragma unroll
+            for (unsigned r = 0; r < VMAX; ++r)
+                tmp[r] = (r < n) ? R_(r) : 0ull;
+            for (unsigned r = 0; r < n; ++r) {
+                const unsigned src = pg(c.witness, r);
+                uint64_t val = 0;
+#pragma unroll
+                for (unsigned q = 0; q < VMAX; ++q)
+                    if (q == src)
+                        val = tmp[q];
+                R_(r) = val;
+            }
+            normalize_columns(sm, n, b);
+            build_levels(sm, n, b);
+            c.canonical = 1;
+            c.witness = ~0ull;
+            search(sm, n, b, F_COMPLETE, max_trials, nullptr, 0, c);
+        }
+        o.aut_lo = c.canonical ? c.aut_lo : 0;
+        o.aut_hi = c.canonical ? c.aut_hi : 0;
+        o.status |= c.canonical ? c.status : (uint8_t)(c.status | ST_TIMEOUT);
+    }
+    if (o.status & ST_TIMEOUT)
+        o.canonical = 0;
+}
+
+
+}  // namespace bibd
+}  // namespace canon

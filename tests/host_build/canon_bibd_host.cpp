@@ -1,0 +1,34 @@
+// canon_bibd_host.cpp -- the device search of canon_bibd_core.cuh compiled for the
+// host (test only): CUDA qualifiers are defined away and the intrinsics the search
+// uses are given host definitions, so the CPU suite can check the kernel logic
+// against the oracle without a GPU.
+#include <cstdint>
+#include <cstring>
+#define __device__
+#define __host__
+#define __forceinline__ inline
+#define __global__
+static inline int __ffsll(long long x) { return __builtin_ffsll(x); }
+static inline int __ffs(unsigned x) { return __builtin_ffs((int)x); }
+static inline int __popcll(unsigned long long x) { return __builtin_popcountll(x); }
+static inline int __popc(unsigned x) { return __builtin_popcount(x); }
+static inline int __clzll(long long x) { return x ? __builtin_clzll((unsigned long long)x) : 64; }
+static inline int __clz(unsigned x) { return x ? __builtin_clz(x) : 32; }
+static inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) { return (unsigned long long)(((unsigned __int128)a * b) >> 64); }
+#include "../../incidence-system-enumeration_gb300/csrc/canon_bibd_core.cuh"
+using namespace canon;
+using namespace canon::bibd;
+extern "C" int emu_check(const uint64_t *rows, unsigned n, unsigned b, unsigned flags, uint64_t max_trials,
+                         uint8_t *canonical, uint8_t *status, uint8_t *reject_row, uint64_t *witness, uint64_t *aut, uint64_t *trials) {
+    static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
+    static uint32_t s_vd[VMAX * TPB];
+    static uint16_t s_cm[64 * TPB];
+    static uint8_t s_pc[64 * TPB];
+    Smem sm{s_rows, s_lvl, s_pc, s_cm, s_vd};
+    for (unsigned r = 0; r < n; ++r) R_(r) = rows[r];
+    CheckOut o;
+    check_one(sm, n, b, flags, max_trials, nullptr, 0, o);
+    *canonical = o.canonical; *status = o.status; *reject_row = o.reject_row; *witness = o.witness;
+    aut[0] = o.aut_lo; aut[1] = o.aut_hi; *trials = o.trials;
+    return 0;
+}
