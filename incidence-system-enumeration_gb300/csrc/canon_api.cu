@@ -508,4 +508,37 @@ int canon_stream_sync(canon_ctx *c) {
     return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "stream sync");
 }
 
+int canon_check_bibd_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                             const uint8_t *d_nrows, const canon_device_outputs *out, uint64_t max_trials,
+                             void *stream) {
+    if (n > CANON_NOALLOC_MAX_ITEMS)
+        return CANON_ESIZE;
+    if (!out || !d_rows || v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x1Fu))
+        return CANON_EINVAL;
+    if (!out->canonical || !out->status || !out->reject_row || !out->row_to_change || !out->player_index ||
+        !out->witness || !out->aut || !out->trials || !out->n_auts || !out->len_aut)
+        return CANON_EINVAL;
+    if ((flags & canon::F_SAVE_AUTS) && (!out->auts || !out->aut_cap))
+        return CANON_EINVAL;
+    if (!n)
+        return CANON_OK;
+    Outputs o{};
+    o.canonical = out->canonical;
+    o.status = out->status;
+    o.reject_row = out->reject_row;
+    o.row_to_change = out->row_to_change;
+    o.player_index = out->player_index;
+    o.witness = out->witness;
+    o.aut = out->aut;
+    o.trials = out->trials;
+    o.n_auts = out->n_auts;
+    o.len_aut = out->len_aut;
+    o.auts = (flags & canon::F_SAVE_AUTS) ? out->auts : nullptr;
+    o.aut_cap = (flags & canon::F_SAVE_AUTS) ? out->aut_cap : 0;
+    const cudaError_t e = canon::launch_bibd_check_noalloc(n, v, b, flags, d_rows, d_nrows, o,
+                                                           max_trials ? max_trials : (1ull << 28),
+                                                           (cudaStream_t)stream);
+    return e == cudaSuccess ? CANON_OK : CANON_ECUDA;
+}
+
 }  // extern "C"

@@ -12,6 +12,8 @@
 // lives in shared memory as bytes.  Items are taken from a global ticket
 // counter so that a thread that finishes a cheap (rejected) matrix immediately
 // takes the next one.
+#include <mutex>
+
 #include "canon_bibd_core.cuh"
 
 namespace canon {
@@ -222,6 +224,93 @@ cudaError_t launch_bibd_canonize(uint32_t n, uint32_t v, uint32_t b, uint64_t *d
     bibd_canonize_kernel<<<grid, TPB, 0, s>>>(n, v, b, d_rows, d_aut, d_status, stride_items, first_item,
                                               max_trials, tk);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// canon_check_bibd_noalloc(): the batched check for callers that cannot
+// allocate device memory.  Its scratch -- one work descriptor per matrix and the
+// work-stealing counter -- lives in this file-scope array instead of in a
+// context; every GPU that loads the library holds it until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_ITEMS = 65536;                       // CANON_NOALLOC_MAX_ITEMS
+constexpr size_t NOALLOC_COUNTER_OFF = (size_t)NOALLOC_MAX_ITEMS * sizeof(Item);
+constexpr size_t NOALLOC_SCRATCH_BYTES = NOALLOC_COUNTER_OFF + 256;   // 1 MiB + 256 B
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+int g_noalloc_sms[NOALLOC_MAX_DEVICES] = {};
+
+// one work descriptor per matrix, read from the caller's device arrays
+__global__ void noalloc_fill_items(Item *items, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
+                                   const uint8_t *__restrict__ nrows) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t nr = nrows ? nrows[i] : v;
+        Item it{};
+        it.data_off = i * v;
+        it.kind = (nr >= 1 && nr <= v) ? KIND_BIBD : 0xFFu;   // out-of-range rows: flagged bad input
+        it.nrows = (uint8_t)nr;
+        it.ncols = (uint8_t)b;
+        it.flags = (uint8_t)flags;
+        it.out_idx = i;
+        items[i] = it;
+    }
+}
+
+// Device address of the scratch on the current device, found once per device.
+cudaError_t noalloc_scratch(unsigned char **ptr, int *sms) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return e;
+        int count = 0;
+        e = cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess)
+            return e;
+        g_noalloc_sms[dev] = count;
+        g_noalloc_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    *ptr = g_noalloc_ptr[dev];
+    *sms = g_noalloc_sms[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t launch_bibd_check_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                                      const uint8_t *d_nrows, Outputs out, uint64_t max_trials, cudaStream_t s) {
+    if (n > NOALLOC_MAX_ITEMS)
+        return cudaErrorInvalidValue;
+    if (!n)
+        return cudaSuccess;
+    unsigned char *scratch = nullptr;
+    int sms = 0;
+    cudaError_t e = noalloc_scratch(&scratch, &sms);
+    if (e != cudaSuccess)
+        return e;
+    Item *items = reinterpret_cast<Item *>(scratch);
+    unsigned *counter = reinterpret_cast<unsigned *>(scratch + NOALLOC_COUNTER_OFF);
+    int grid = (int)((n + 255) / 256);
+    if (grid > 4 * sms)
+        grid = 4 * sms;
+    noalloc_fill_items<<<grid, 256, 0, s>>>(items, n, v, b, flags, d_nrows);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    // the work counter is cleared by the launcher before the check runs
+    return launch_bibd_check(items, n, d_rows, out, max_trials, counter, sms, s);
 }
 
 }  // namespace canon

@@ -58,6 +58,10 @@ cudaError_t launch_bibd_canonize(uint32_t n, uint32_t v, uint32_t b, uint64_t *d
                                  uint64_t *d_aut, uint8_t *d_status, uint32_t stride_items,
                                  uint32_t first_item, uint64_t max_trials, unsigned *d_ticket,
                                  int num_sms, cudaStream_t s);
+// check of a device-resident batch with the scratch in static device memory (no allocation)
+cudaError_t launch_bibd_check_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
+                                      const uint64_t *d_rows, const uint8_t *d_nrows, Outputs out,
+                                      uint64_t max_trials, cudaStream_t s);
 cudaError_t launch_sts_generate(uint32_t n, uint32_t v, uint64_t seed, uint64_t *d_rows,
                                 int num_sms, cudaStream_t s);
 cudaError_t launch_ksys_check(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes,

@@ -28,6 +28,8 @@ CANON_ENOMEM = -2
 CANON_ECUDA = -3
 CANON_ETIMEOUT = -4
 CANON_ENODEV = -5
+CANON_ESIZE = -6
+NOALLOC_MAX_ITEMS = 65536
 
 ST_OK = 0
 ST_BADINPUT = 1
@@ -51,6 +53,7 @@ HEADER_SYMBOLS = [
     "canon_sync", "canon_set_ordering", "canon_canonize_bibd", "canon_check_bibd_device",
     "canon_generate_sts_device", "canon_device_alloc", "canon_device_free", "canon_memcpy_d2h",
     "canon_memcpy_h2d", "canon_last_kernel_ms", "canon_kernel_launches", "canon_stream_sync",
+    "canon_check_bibd_noalloc",
 ]
 
 
@@ -76,6 +79,15 @@ class KsysBatch(ctypes.Structure):
     _fields_ = [("n", ctypes.c_uint32), ("np", ctypes.c_uint32), ("rounds", ctypes.c_uint32),
                 ("flags", ctypes.c_uint32), ("data", ctypes.POINTER(ctypes.c_uint8)),
                 ("nrows", ctypes.POINTER(ctypes.c_uint8))]
+
+
+class DeviceOutputs(ctypes.Structure):
+    """canon_device_outputs: device pointers of canon_check_bibd_noalloc's outputs."""
+    _fields_ = [("canonical", ctypes.c_void_p), ("status", ctypes.c_void_p),
+                ("reject_row", ctypes.c_void_p), ("row_to_change", ctypes.c_void_p),
+                ("player_index", ctypes.c_void_p), ("witness", ctypes.c_void_p),
+                ("aut", ctypes.c_void_p), ("trials", ctypes.c_void_p), ("n_auts", ctypes.c_void_p),
+                ("len_aut", ctypes.c_void_p), ("auts", ctypes.c_void_p), ("aut_cap", ctypes.c_uint32)]
 
 
 class Results(ctypes.Structure):
@@ -130,6 +142,7 @@ def load_library(path=LIB_PATH):
     L.canon_kernel_launches.argtypes = [vp]
     L.canon_kernel_launches.restype = u64
     L.canon_stream_sync.argtypes = [vp]
+    L.canon_check_bibd_noalloc.argtypes = [u32, u32, u32, u32, vp, vp, ctypes.POINTER(DeviceOutputs), u64, vp]
     _lib = L
     return L
 

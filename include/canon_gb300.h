@@ -39,6 +39,7 @@ extern "C" {
 #define CANON_ECUDA    -3   /* CUDA runtime error */
 #define CANON_ETIMEOUT -4   /* a search hit its trial budget (per-item status says which) */
 #define CANON_ENODEV   -5   /* no usable GPU */
+#define CANON_ESIZE    -6   /* batch larger than CANON_NOALLOC_MAX_ITEMS (canon_check_bibd_noalloc) */
 
 /* ---- per-item status bits (canon_results.status[i]) ---- */
 #define CANON_ST_OK        0u
@@ -181,6 +182,50 @@ float canon_last_kernel_ms(const canon_ctx *ctx);
 /* Number of kernels this context launched since creation. */
 uint64_t canon_kernel_launches(const canon_ctx *ctx);
 int canon_stream_sync(canon_ctx *ctx);
+
+/* ---- checking without allocating ---- */
+/* Device output arrays of canon_check_bibd_noalloc (one entry per matrix, same
+ * meaning as the canon_results fields).  auts may be NULL unless CANON_SAVE_AUTS
+ * is set, in which case it holds aut_cap*64 bytes per matrix. */
+typedef struct {
+    uint8_t  *canonical;
+    uint8_t  *status;
+    uint8_t  *reject_row;
+    uint8_t  *row_to_change;
+    int32_t  *player_index;
+    uint8_t  *witness;      /* 16 bytes per matrix */
+    uint64_t *aut;          /* (lo, hi) per matrix */
+    uint64_t *trials;
+    uint16_t *n_auts;
+    uint8_t  *len_aut;
+    uint8_t  *auts;
+    uint32_t  aut_cap;
+} canon_device_outputs;
+
+#define CANON_NOALLOC_MAX_ITEMS 65536u
+
+/* The batched TestCanonicity() check of canon_submit_bibd + canon_sync for
+ * device-resident matrices, for callers that cannot call cudaMalloc: code that
+ * runs while a CUDA graph is being captured, inside a host application whose
+ * device memory belongs to another allocator or pool, or on a latency path
+ * where the implicit synchronisation of cudaMalloc/cudaFree is not acceptable.
+ * It needs no context and allocates nothing: its scratch (one 16-byte work
+ * descriptor per matrix and a work counter) is a static device array of
+ * 1 MiB + 256 bytes that every GPU loading this library holds until the
+ * process exits.  Hence at most CANON_NOALLOC_MAX_ITEMS matrices per call;
+ * larger batches are refused with CANON_ESIZE.  Rows and per-matrix filled-row
+ * counts (d_nrows, NULL = all v) are device pointers laid out as in
+ * canon_bibd_batch; `out` holds device pointers.  Launched on `stream`
+ * (a cudaStream_t, NULL = the default stream) and not waited for.
+ * The first call on a device looks up the scratch's device address (once per
+ * device, with that device current), so make that first call before any stream
+ * capture.  All calls share the one scratch array: calls whose work overlaps on
+ * the GPU race, so issue them on one stream or wait in between.  The work
+ * counter is cleared by every call.  max_trials 0 = 1<<28.
+ * No counterpart in the reference. */
+int canon_check_bibd_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                             const uint8_t *d_nrows, const canon_device_outputs *out, uint64_t max_trials,
+                             void *stream);
 
 #ifdef __cplusplus
 }
