@@ -196,7 +196,7 @@ int canon_submit_bibd(canon_ctx *c, const canon_bibd_batch *bt) {
         return CANON_OK;
     if (!bt->rows || bt->v < 1 || bt->v > canon::VMAX || bt->b < 1 || bt->b > canon::BMAX)
         return fail(c, CANON_EINVAL, "bibd batch: need rows, 1 <= v <= 16, 1 <= b <= 63");
-    if (bt->flags & ~0x1Fu)
+    if (bt->flags & ~0x3Fu)
         return fail(c, CANON_EINVAL, "bibd batch: unknown flags");
     const uint32_t total = c->n_bitems + c->n_kitems;
     if ((uint64_t)total + bt->n > c->cfg.max_items)
@@ -411,9 +411,10 @@ int canon_check_bibd_device(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, ui
                             uint8_t *d_status, uint64_t *d_trials, void *stream) {
     if (!c || !d_rows || !d_canonical)
         return fail(c, CANON_EINVAL, "null argument");
-    if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x17u))
+    if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x37u))
         return fail(c, CANON_EINVAL,
-                    "check: need 1 <= v <= 16, 1 <= b <= 63, flags in COMPLETE|RAW|FULL_AUT|AUT_CANON");
+                    "check: need 1 <= v <= 16, 1 <= b <= 63, flags in COMPLETE|RAW|FULL_AUT|AUT_CANON|"
+                    "REFERENCE_ORDER");
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
     cudaEventRecord(c->ev0, s);
@@ -513,7 +514,7 @@ int canon_check_bibd_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                              void *stream) {
     if (n > CANON_NOALLOC_MAX_ITEMS)
         return CANON_ESIZE;
-    if (!out || !d_rows || v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x1Fu))
+    if (!out || !d_rows || v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x3Fu))
         return CANON_EINVAL;
     if (!out->canonical || !out->status || !out->reject_row || !out->row_to_change || !out->player_index ||
         !out->witness || !out->aut || !out->trials || !out->n_auts || !out->len_aut)

@@ -58,12 +58,10 @@ __global__ void __launch_bounds__(TPB) bibd_items_kernel(const Item *__restrict_
         if (item.kind != KIND_BIBD || n < 1 || n > VMAX || b < 1 || b > BMAX) {
             o = CheckOut{0, ST_BADINPUT, 0xFF, 0xFF, ~0ull, 0, 0, 0, 0, 0};
         } else {
-            for (unsigned r = 0; r < n; ++r)
-                R_(r) = words[item.data_off + r];
             uint8_t *adst = (item.flags & F_SAVE_AUTS) && out.auts
                                 ? out.auts + (size_t)o_i * out.aut_cap * 64u
                                 : nullptr;
-            check_one(sm, n, b, item.flags, max_trials, adst, out.aut_cap, o);
+            check_one(sm, words + item.data_off, n, b, item.flags, max_trials, adst, out.aut_cap, o);
         }
         out.canonical[o_i] = o.canonical;
         out.status[o_i] = o.status;
@@ -95,10 +93,8 @@ __global__ void __launch_bounds__(TPB) bibd_uniform_kernel(uint32_t n_items, uin
         const unsigned it = atomicAdd(ticket, 1u);
         if (it >= n_items)
             break;
-        for (unsigned r = 0; r < v; ++r)
-            R_(r) = rows[(size_t)it * v + r];
         CheckOut o;
-        check_one(sm, v, b, flags & ~F_SAVE_AUTS, max_trials, nullptr, 0, o);
+        check_one(sm, rows + (size_t)it * v, v, b, flags & ~F_SAVE_AUTS, max_trials, nullptr, 0, o);
         canonical[it] = o.canonical;
         if (witness16)
             store_witness(witness16 + (size_t)it * 16u, o.witness, v);
@@ -113,8 +109,9 @@ __global__ void __launch_bounds__(TPB) bibd_uniform_kernel(uint32_t n_items, uin
     }
 }
 
-// CanonizeMatrix(k = 0), MatrixCanonChecker.cpp:420-496: repeat the complete check,
-// move the rows as the witness says, renormalise the columns, until canonical.
+// CanonizeMatrix(k = 0), MatrixCanonChecker.cpp:420-564: the matrix is replaced by
+// its canonical form, the lex-max matrix that the reference reaches by repeated
+// checks; the lex-max search finds it directly, together with |Aut|.
 __global__ void __launch_bounds__(TPB) bibd_canonize_kernel(uint32_t n_items, uint32_t v, uint32_t b,
                                                             uint64_t *rows, uint64_t *aut, uint8_t *status,
                                                             uint32_t stride_items, uint32_t first_item,
@@ -132,39 +129,21 @@ __global__ void __launch_bounds__(TPB) bibd_canonize_kernel(uint32_t n_items, ui
         if (it64 >= n_items)
             break;
         const size_t it = (size_t)it64;
-        for (unsigned r = 0; r < v; ++r)
-            R_(r) = rows[it * v + r];
-        CheckOut o;
         uint8_t st = 0;
-        for (int round = 0; round < 4096; ++round) {
-            check_one(sm, v, b, F_COMPLETE | F_RAW, max_trials, nullptr, 0, o);
-            if (o.status) {
-                st = o.status;
-                break;
-            }
-            if (o.canonical)
-                break;
-            uint64_t tmp[VMAX];
-#pragma unroll
-            for (unsigned r = 0; r < VMAX; ++r)
-                tmp[r] = (r < v) ? R_(r) : 0ull;
-            for (unsigned r = 0; r < v; ++r) {
-                const unsigned src = pg(o.witness, r);
-                uint64_t val = 0;
-#pragma unroll
-                for (unsigned q = 0; q < VMAX; ++q)
-                    if (q == src)
-                        val = tmp[q];
-                R_(r) = val;
-            }
-            if (round == 4095)
+        MaxOut mo{false, false, 0, 0};
+        if (!load_rows(sm, rows + it * v, v, b, F_RAW)) {
+            st = ST_BADINPUT;
+        } else {
+            max_search(sm, v, b, max_trials, mo);
+            if (mo.timeout)
                 st = ST_TIMEOUT;
+            else
+                for (unsigned r = 0; r < v; ++r)
+                    rows[it * v + r] = R_(r);
         }
-        for (unsigned r = 0; r < v; ++r)
-            rows[it * v + r] = R_(r);
         if (aut) {
-            aut[2 * it] = o.aut_lo;
-            aut[2 * it + 1] = o.aut_hi;
+            aut[2 * it] = st ? 0 : mo.leaves;
+            aut[2 * it + 1] = 0;
         }
         if (status)
             status[it] = st;

@@ -549,12 +549,139 @@ __device__ void search(Smem sm, unsigned n, unsigned b, unsigned flags, uint64_t
     o.n_auts = (uint16_t)(n_auts > 0xFFFFu ? 0xFFFFu : n_auts);
 }
 
-// TestCanonicity() with the batch flags; with F_AUT_CANON a rejected complete
-// matrix is then canonised (CanonizeMatrix(), MatrixCanonChecker.cpp:420-496: move
-// the rows as the witness says, renormalise, check again) and |Aut| is taken from
-// its canonical form.  Outputs other than |Aut| are those of the first check.
-__device__ void check_one(Smem sm, unsigned n, unsigned b, unsigned flags, uint64_t max_trials,
-                          uint8_t *aut_dst, unsigned aut_cap, CheckOut &o) {
+// Lex-max search: the greatest matrix reachable from M by row and column
+// permutations (the canonical form that CanonizeMatrix() converges to,
+// MatrixCanonChecker.cpp:420-496) and the number of row permutations that reach
+// it (|Aut|, the order updateGroupOrder() accumulates, GroupOrder.h:63-73).
+// Depth-first over row prefixes; at each level the candidate rows whose best
+// column arrangement gives the greatest row are found bit-parallel, orbit by
+// orbit (the same comparison as checkColOrbit()), and only they are branched on.
+// The rows of M serve as the first bound; a greater row replaces the bound from
+// that level down (the subtrees already searched are all smaller than it), so M
+// is canonical iff the bound never rises.  On return R_() holds the canonical
+// form.  No automorphism pruning: every leaf is a distinct row permutation.
+struct MaxOut {
+    bool improved;      // M is not canonical
+    bool timeout;
+    uint64_t leaves;    // |Aut|
+    uint64_t nodes;
+};
+
+__device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o) {
+    const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
+    const uint64_t cols = (1ull << b) - 1ull;
+    const uint64_t sentinel = 1ull << b;
+    for (unsigned j = 0; j < b; ++j)
+        PC_(j) = (uint8_t)j;
+    o.improved = false;
+    o.timeout = false;
+    o.leaves = 0;
+    o.nodes = 0;
+    unsigned valid = n;        // rows 0..valid-1 of the bound (and levels 0..valid) are set
+    unsigned used = 0;
+    uint64_t perm = 0;
+    unsigned i = 0;
+    bool enter = true;         // entering the node at level i (else: next child of level i)
+    for (;;) {
+        if (enter) {
+            if (i == n) {
+                ++o.leaves;
+                enter = false;
+                --i;
+                used &= ~(1u << pg(perm, i));
+                continue;
+            }
+            if (++o.nodes > max_nodes) {
+                o.timeout = true;
+                return;
+            }
+            // the greatest arranged row over the unused rows, and the rows reaching it
+            const uint64_t m = L_(i) | sentinel;
+            unsigned tied = allrows & ~used;
+            uint64_t arr = 0;
+            unsigned s = 0;
+            while (s < b) {
+                const unsigned e = __ffsll((long long)(m & (~0ull << (s + 1)))) - 1;
+                if (e == s + 1) {
+                    const unsigned ones = CM_(PC_(s)) & tied;
+                    if (ones) {
+                        tied = ones;
+                        arr |= 1ull << s;
+                    }
+                } else {
+                    unsigned p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
+                    for (unsigned j = s; j < e; ++j) {
+                        unsigned carry = CM_(PC_(j)) & tied, t;
+                        t = p0 & carry; p0 ^= carry; carry = t;
+                        t = p1 & carry; p1 ^= carry; carry = t;
+                        t = p2 & carry; p2 ^= carry; carry = t;
+                        t = p3 & carry; p3 ^= carry; carry = t;
+                        t = p4 & carry; p4 ^= carry; carry = t;
+                        p5 ^= carry;
+                    }
+                    const unsigned pl[6] = {p0, p1, p2, p3, p4, p5};
+                    unsigned cstar = 0;
+#pragma unroll
+                    for (int k = 5; k >= 0; --k) {
+                        const unsigned t = tied & pl[k];
+                        if (t) {
+                            tied = t;
+                            cstar |= 1u << k;
+                        }
+                    }
+                    arr |= ((1ull << cstar) - 1ull) << s;
+                }
+                s = e;
+            }
+            bool set_bound = i >= valid;
+            if (!set_bound) {
+                const uint64_t d = arr ^ R_(i);
+                if (d) {
+                    if (!((arr >> (__ffsll((long long)d) - 1)) & 1u)) {
+                        // smaller than the bound: every extension is smaller too
+                        enter = false;
+                        if (i == 0)
+                            return;
+                        --i;
+                        used &= ~(1u << pg(perm, i));
+                        continue;
+                    }
+                    o.improved = true;
+                    o.leaves = 0;
+                    set_bound = true;
+                }
+            }
+            if (set_bound) {
+                R_(i) = arr;
+                L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
+                valid = i + 1;
+            }
+            VD_(i) = tied;            // children still to visit
+        }
+        // next child of the node at level i
+        const unsigned rem = VD_(i);
+        if (!rem) {
+            if (i == 0)
+                return;
+            enter = false;
+            --i;
+            used &= ~(1u << pg(perm, i));
+            continue;
+        }
+        const unsigned x = __ffs(rem) - 1;
+        VD_(i) = rem & (rem - 1);
+        refine(sm, i, x, b);
+        perm = ps(perm, i, x);
+        used |= 1u << x;
+        ++i;
+        enter = true;
+    }
+}
+
+// Trials the reference-order search may spend before the lex-max search decides.
+constexpr uint64_t QUICK_TRIALS = 256;
+
+__device__ __forceinline__ void reset_out(CheckOut &o) {
     o.canonical = 1;
     o.status = 0;
     o.reject_row = 0xFF;
@@ -565,14 +692,23 @@ __device__ void check_one(Smem sm, unsigned n, unsigned b, unsigned flags, uint6
     o.trials = 0;
     o.n_auts = 0;
     o.len_aut = 0;
+}
 
+__device__ __forceinline__ bool load_rows(Smem sm, const uint64_t *src, unsigned n, unsigned b, unsigned flags) {
+    for (unsigned r = 0; r < n; ++r)
+        R_(r) = src[r];
     if (flags & F_RAW)
         normalize_columns(sm, n, b);
-    if (!build_levels(sm, n, b)) {
-        o.status = ST_BADINPUT;
-        o.canonical = 0;
-        return;
-    }
+    return build_levels(sm, n, b);
+}
+
+// The reference path: TestCanonicity() in its own search order (exact trial
+// counts and automorphism lists); with F_AUT_CANON a rejected complete matrix is
+// then canonised as CanonizeMatrix() does (MatrixCanonChecker.cpp:420-496: move
+// the rows as the witness says, renormalise, check again) and |Aut| is that of
+// its canonical form.  Outputs other than |Aut| are those of the first check.
+__device__ void check_reference(Smem sm, unsigned n, unsigned b, unsigned flags, uint64_t max_trials,
+                                uint8_t *aut_dst, unsigned aut_cap, CheckOut &o) {
     search(sm, n, b, flags, max_trials, aut_dst, aut_cap, o);
     if ((flags & F_AUT_CANON) && (flags & F_COMPLETE) && !o.canonical && !o.status) {
         CheckOut c = o;
@@ -600,10 +736,63 @@ __device__ void check_one(Smem sm, unsigned n, unsigned b, unsigned flags, uint6
         o.aut_hi = c.canonical ? c.aut_hi : 0;
         o.status |= c.canonical ? c.status : (uint8_t)(c.status | ST_TIMEOUT);
     }
+}
+
+// TestCanonicity() of one matrix (rows at `src`, n words).  Unless the reference
+// order is required (F_SAVE_AUTS: automorphism lists in the reference's order;
+// F_REFERENCE_ORDER: its trial counts), the verdict and |Aut| come from the
+// lex-max search, and the witness from a reference-order search: a short one
+// first (a random non-canonical matrix is rejected within a few trials), a full
+// one only if the lex-max search shows a matrix to be non-canonical that the
+// short search did not reject.  Verdict, witness, rowToChange and |Aut| are
+// identical either way; `trials` counts the reference-order trials spent.
+__device__ void check_one(Smem sm, const uint64_t *src, unsigned n, unsigned b, unsigned flags,
+                          uint64_t max_trials, uint8_t *aut_dst, unsigned aut_cap, CheckOut &o) {
+    reset_out(o);
+    if (!load_rows(sm, src, n, b, flags)) {
+        o.status = ST_BADINPUT;
+        o.canonical = 0;
+        return;
+    }
+    const bool want_aut = (flags & (F_AUT_CANON | F_FULL_AUT)) || o.canonical;
+    if (flags & (F_SAVE_AUTS | F_REFERENCE_ORDER)) {
+        check_reference(sm, n, b, flags, max_trials, aut_dst, aut_cap, o);
+    } else {
+        const unsigned sflags = flags & ~(F_FULL_AUT | F_AUT_CANON);
+        search(sm, n, b, sflags, QUICK_TRIALS < max_trials ? QUICK_TRIALS : max_trials, nullptr, 0, o);
+        const bool decided = !o.canonical && !(o.status & ST_TIMEOUT);
+        if (decided && !(flags & (F_AUT_CANON | F_FULL_AUT))) {
+            o.aut_lo = 0;                // rejected: the reference leaves |Aut| undefined
+            o.aut_hi = 0;
+        } else {
+            const uint64_t quick = o.trials;
+            o.status = 0;
+            MaxOut mo;
+            max_search(sm, n, b, max_trials, mo);
+            if (mo.timeout) {
+                o.status = ST_TIMEOUT;
+            } else if (!decided) {
+                if (mo.improved) {
+                    // non-canonical, rejected late in the reference order: find its witness
+                    load_rows(sm, src, n, b, flags);
+                    reset_out(o);
+                    search(sm, n, b, sflags, max_trials, nullptr, 0, o);
+                    o.trials += quick;
+                } else {
+                    o.canonical = 1;
+                }
+            }
+            if (!o.status) {
+                const bool has = !mo.improved || (flags & (F_AUT_CANON | F_FULL_AUT));
+                o.aut_lo = has ? mo.leaves : 0;
+                o.aut_hi = 0;
+            }
+        }
+        (void)want_aut;
+    }
     if (o.status & ST_TIMEOUT)
         o.canonical = 0;
 }
-
 
 }  // namespace bibd
 }  // namespace canon

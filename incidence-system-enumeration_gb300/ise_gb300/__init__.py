@@ -41,6 +41,7 @@ RAW = 0x2
 FULL_AUT = 0x4
 SAVE_AUTS = 0x8
 AUT_CANON = 0x10
+REFERENCE_ORDER = 0x20
 
 # t_canonOutInfo of the reference (Source/CanonicityChecker.h:27-32)
 t_saveNothing = 0

@@ -73,6 +73,13 @@ extern "C" {
  * canonical).  The flag, witness and row_to_change stay those of the first check.
  * Much cheaper than CANON_FULL_AUT on non-canonical matrices. */
 #define CANON_AUT_CANON   0x10u
+/* Run the check in the reference's own search order throughout (next_permutation()
+ * with its orbit pruning), so that canon_results.trials equals the number of
+ * permutations the reference tries.  Without it (and without CANON_SAVE_AUTS, which
+ * implies it) the verdict and |Aut| come from a lex-max search over the same tree
+ * and only the witness is taken from the reference order: every output except
+ * `trials` is identical, and the check is several times faster. */
+#define CANON_REFERENCE_ORDER 0x20u
 
 /* ---- context ---- */
 typedef struct canon_ctx canon_ctx;
@@ -162,7 +169,7 @@ int canon_canonize_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint
 /* Same check as canon_submit_bibd + canon_sync for device pointers, all items
  * with v rows; launched on `stream` (a cudaStream_t, NULL = the context's).
  * Output arrays are device pointers (any may be NULL except canonical).
- * flags: CANON_COMPLETE, CANON_RAW, CANON_FULL_AUT, CANON_AUT_CANON. */
+ * flags: CANON_COMPLETE, CANON_RAW, CANON_FULL_AUT, CANON_AUT_CANON, CANON_REFERENCE_ORDER. */
 int canon_check_bibd_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                             const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16,
                             uint64_t *d_aut, uint8_t *d_status, uint64_t *d_trials, void *stream);

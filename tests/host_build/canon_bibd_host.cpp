@@ -25,10 +25,25 @@ extern "C" int emu_check(const uint64_t *rows, unsigned n, unsigned b, unsigned 
     static uint16_t s_cm[64 * TPB];
     static uint8_t s_pc[64 * TPB];
     Smem sm{s_rows, s_lvl, s_pc, s_cm, s_vd};
-    for (unsigned r = 0; r < n; ++r) R_(r) = rows[r];
     CheckOut o;
-    check_one(sm, n, b, flags, max_trials, nullptr, 0, o);
+    check_one(sm, rows, n, b, flags, max_trials, nullptr, 0, o);
     *canonical = o.canonical; *status = o.status; *reject_row = o.reject_row; *witness = o.witness;
     aut[0] = o.aut_lo; aut[1] = o.aut_hi; *trials = o.trials;
     return 0;
+}
+// the lex-max search alone: canonical form into rows_out, |Aut| and node count
+extern "C" int emu_maxsearch(const uint64_t *rows, unsigned n, unsigned b, uint64_t *rows_out, uint64_t *leaves,
+                             uint64_t *nodes, uint8_t *improved) {
+    static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
+    static uint32_t s_vd[VMAX * TPB];
+    static uint16_t s_cm[64 * TPB];
+    static uint8_t s_pc[64 * TPB];
+    Smem sm{s_rows, s_lvl, s_pc, s_cm, s_vd};
+    if (!load_rows(sm, rows, n, b, F_RAW))
+        return -1;
+    MaxOut mo;
+    max_search(sm, n, b, 1ull << 30, mo);
+    for (unsigned r = 0; r < n; ++r) rows_out[r] = R_(r);
+    *leaves = mo.leaves; *nodes = mo.nodes; *improved = mo.improved;
+    return mo.timeout ? -2 : 0;
 }

@@ -15,7 +15,7 @@ SRC = os.path.join(conftest.REPO, "tests", "host_build", "canon_bibd_host.cpp")
 OUT = os.path.join(conftest.REPO, "tests", "host_build", "_build", "libcanon_bibd_host.so")
 CUDA_INC = "/usr/local/cuda/include"
 
-COMPLETE, RAW, FULL_AUT, AUT_CANON = 0x1, 0x2, 0x4, 0x10
+COMPLETE, RAW, FULL_AUT, AUT_CANON, REFERENCE_ORDER = 0x1, 0x2, 0x4, 0x10, 0x20
 
 
 @pytest.fixture(scope="module")
@@ -56,17 +56,45 @@ def compare(L, M, flags):
     o = expected(M, flags)
     assert e["status"] == 0
     assert e["canonical"] == o["canonical"]
-    assert e["trials"] == o["trials"]
+    if flags & REFERENCE_ORDER:
+        assert e["trials"] == o["trials"]
     if not o["canonical"]:
         assert e["witness"] == o["witness"] and e["reject_row"] == o["reject_row"]
     if o["canonical"] or flags & (FULL_AUT | AUT_CANON):
         assert e["aut"] == o["aut"]
 
 
-@pytest.mark.parametrize("flags", [COMPLETE | RAW, COMPLETE | RAW | FULL_AUT, COMPLETE | RAW | AUT_CANON])
+FLAGS = [COMPLETE | RAW, COMPLETE | RAW | FULL_AUT, COMPLETE | RAW | AUT_CANON]
+
+
+@pytest.mark.parametrize("flags", FLAGS + [f | REFERENCE_ORDER for f in FLAGS])
 def test_sts15_random(host, flags):
-    for i in range(12 if flags & FULL_AUT else 30):
+    for i in range(8 if flags & FULL_AUT and flags & REFERENCE_ORDER else 30):
         compare(host, oracle.rows_to_matrix(oracle.sts_random_rows(15, 808, i), 35), flags)
+
+
+def test_sts15_canonical_fixture_aut(host):
+    for M, aut in cases.load_sts15():
+        import ise_gb300 as G
+        e = run(host, G.pack_rows(M), 15, 35, COMPLETE)
+        assert e["canonical"] and e["aut"] == aut
+
+
+def test_lex_max_search_gives_canonical_form(host):
+    import ise_gb300 as G
+    canon = {M.tobytes(): a for M, a in cases.load_sts15()}
+    u64 = ctypes.c_uint64
+    for i in range(25):
+        rows = oracle.sts_random_rows(15, 4242, i)
+        out = np.zeros(15, np.uint64)
+        leaves, nodes, imp = u64(), u64(), ctypes.c_uint8()
+        rc = host.emu_maxsearch(rows.ctypes.data_as(ctypes.POINTER(u64)), 15, 35,
+                                out.ctypes.data_as(ctypes.POINTER(u64)), ctypes.byref(leaves),
+                                ctypes.byref(nodes), ctypes.byref(imp))
+        assert rc == 0
+        C = G.unpack_rows(out, 35)
+        Co, ao, _ = oracle.bibd_canonize(oracle.rows_to_matrix(rows, 35))
+        assert np.array_equal(C, Co) and leaves.value == ao == canon[C.tobytes()]
 
 
 def test_partial_prefixes(host):
@@ -77,9 +105,12 @@ def test_partial_prefixes(host):
         for k in (3, 6, 9, 12):
             compare(host, oracle.bibd_normalize(P[:k]), 0)
             compare(host, oracle.bibd_normalize(P[:k]), FULL_AUT)
+            compare(host, oracle.bibd_normalize(P[:k]), REFERENCE_ORDER)
     for params in [(8, 14, 7, 4, 3), (11, 11, 5, 5, 2), (7, 14, 6, 3, 2)]:
         for M, _ in cases.bibd_designs(*params):
             for _ in range(3):
                 P = cases.permute_normalize(M, rng)
                 for k in range(2, P.shape[0] + 1):
-                    compare(host, oracle.bibd_normalize(P[:k]), COMPLETE if k == P.shape[0] else 0)
+                    f = COMPLETE if k == P.shape[0] else 0
+                    compare(host, oracle.bibd_normalize(P[:k]), f)
+                    compare(host, oracle.bibd_normalize(P[:k]), f | FULL_AUT)
