@@ -182,7 +182,7 @@ def run_reference(args, rank, world, dist):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample = 32 * threads
+    sample = 256 * threads
     rows = cpu_sample_rows(sample)
     for _ in range(args.warmup):
         cpu_check_rate(rows[: 2 * threads], threads, 60)
@@ -190,7 +190,7 @@ def run_reference(args, rank, world, dist):
     t_all = 0.0
     n_all = 0
     for _ in range(args.steps):
-        rate, done, dt = cpu_check_rate(rows, threads, 120)
+        rate, done, dt = cpu_check_rate(rows, threads, 30)
         rates.append(rate)
         t_all += dt
         n_all += done
@@ -269,9 +269,9 @@ def run_gpu(args, rank, world, local, dist):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        sample = min(n, 64 * threads)
+        sample = min(n, 4096 * threads)
         rows_s = host_rows.reshape(n, V)[:sample]
-        rate, done, dt = cpu_check_rate(rows_s, threads, 30)
+        rate, done, dt = cpu_check_rate(rows_s, threads, 20)
         cpu = {"value": rate, "unit": "checks/s", "cores": threads, "kind": "port",
                "sample": "first %d items of the same batch (%d checked in %.1f s)" % (sample, done, dt)}
 
