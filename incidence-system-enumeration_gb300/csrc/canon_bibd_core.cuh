@@ -567,12 +567,38 @@ struct MaxOut {
     uint64_t nodes;
 };
 
+// The arranged column masks for level lv+1 after row `cand` was taken at level
+// lv: inside every orbit of level lv that the bound's row lv splits, the columns
+// holding a 1 in row `cand` move to the front.  CM_() holds the row masks of the
+// columns in arranged order (the column masks permuted by permColumn).
+__device__ __forceinline__ void refine_arranged(Smem sm, unsigned lv, unsigned cand, unsigned b) {
+    const uint64_t m = L_(lv) | (1ull << b);
+    uint64_t split = L_(lv + 1) & ~L_(lv);
+    while (split) {
+        const unsigned t = __ffsll((long long)split) - 1;
+        split &= split - 1;
+        const uint64_t below = L_(lv) & ((1ull << t) - 1ull);
+        const unsigned s = 63 - __clzll((long long)below);
+        const unsigned e = __ffsll((long long)(m & (~0ull << (s + 1)))) - 1;
+        unsigned lo = s, hi = e - 1;
+        while (lo < hi) {
+            while (lo < hi && ((CM_(lo) >> cand) & 1u))
+                ++lo;
+            while (lo < hi && !((CM_(hi) >> cand) & 1u))
+                --hi;
+            if (lo < hi) {
+                const uint16_t tmp = CM_(lo);
+                CM_(lo) = CM_(hi);
+                CM_(hi) = tmp;
+            }
+        }
+    }
+}
+
 __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o) {
     const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     const uint64_t cols = (1ull << b) - 1ull;
     const uint64_t sentinel = 1ull << b;
-    for (unsigned j = 0; j < b; ++j)
-        PC_(j) = (uint8_t)j;
     o.improved = false;
     o.timeout = false;
     o.leaves = 0;
@@ -595,23 +621,32 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                 o.timeout = true;
                 return;
             }
-            // the greatest arranged row over the unused rows, and the rows reaching it
-            const uint64_t m = L_(i) | sentinel;
+            // the greatest arranged row over the unused rows, orbit by orbit, compared
+            // with the bound as it is built: 0 equal so far, 1 greater, 2 smaller
+            const bool have_bound = i < valid;
+            const uint64_t bound = have_bound ? R_(i) : 0ull;
             unsigned tied = allrows & ~used;
             uint64_t arr = 0;
+            int state = 0;
+            uint64_t st = (L_(i) | sentinel) & ~1ull;
             unsigned s = 0;
-            while (s < b) {
-                const unsigned e = __ffsll((long long)(m & (~0ull << (s + 1)))) - 1;
+            for (;;) {
+                const unsigned e = __ffsll((long long)st) - 1;
                 if (e == s + 1) {
-                    const unsigned ones = CM_(PC_(s)) & tied;
+                    const unsigned ones = CM_(s) & tied;
+                    const unsigned mx = ones ? 1u : 0u;
                     if (ones) {
                         tied = ones;
                         arr |= 1ull << s;
                     }
+                    if (state == 0 && have_bound) {
+                        const unsigned bb = (unsigned)(bound >> s) & 1u;
+                        state = mx > bb ? 1 : (mx < bb ? 2 : 0);
+                    }
                 } else {
                     unsigned p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
                     for (unsigned j = s; j < e; ++j) {
-                        unsigned carry = CM_(PC_(j)) & tied, t;
+                        unsigned carry = CM_(j) & tied, t;
                         t = p0 & carry; p0 ^= carry; carry = t;
                         t = p1 & carry; p1 ^= carry; carry = t;
                         t = p2 & carry; p2 ^= carry; carry = t;
@@ -629,29 +664,32 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                             cstar |= 1u << k;
                         }
                     }
+                    const uint64_t rng = ((1ull << (e - s)) - 1ull) << s;
                     arr |= ((1ull << cstar) - 1ull) << s;
-                }
-                s = e;
-            }
-            bool set_bound = i >= valid;
-            if (!set_bound) {
-                const uint64_t d = arr ^ R_(i);
-                if (d) {
-                    if (!((arr >> (__ffsll((long long)d) - 1)) & 1u)) {
-                        // smaller than the bound: every extension is smaller too
-                        enter = false;
-                        if (i == 0)
-                            return;
-                        --i;
-                        used &= ~(1u << pg(perm, i));
-                        continue;
+                    if (state == 0 && have_bound) {
+                        const unsigned cb = __popcll(bound & rng);
+                        state = cstar > cb ? 1 : (cstar < cb ? 2 : 0);
                     }
+                }
+                if (state == 2 || e >= b)
+                    break;
+                s = e;
+                st &= st - 1;
+            }
+            if (state == 2) {
+                // smaller than the bound: every extension is smaller too
+                enter = false;
+                if (i == 0)
+                    return;
+                --i;
+                used &= ~(1u << pg(perm, i));
+                continue;
+            }
+            if (state == 1 || !have_bound) {
+                if (state == 1) {
                     o.improved = true;
                     o.leaves = 0;
-                    set_bound = true;
                 }
-            }
-            if (set_bound) {
                 R_(i) = arr;
                 L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
                 valid = i + 1;
@@ -670,7 +708,7 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
         }
         const unsigned x = __ffs(rem) - 1;
         VD_(i) = rem & (rem - 1);
-        refine(sm, i, x, b);
+        refine_arranged(sm, i, x, b);
         perm = ps(perm, i, x);
         used |= 1u << x;
         ++i;
