@@ -54,7 +54,7 @@ HEADER_SYMBOLS = [
     "canon_sync", "canon_set_ordering", "canon_canonize_bibd", "canon_check_bibd_device",
     "canon_generate_sts_device", "canon_device_alloc", "canon_device_free", "canon_memcpy_d2h",
     "canon_memcpy_h2d", "canon_last_kernel_ms", "canon_kernel_launches", "canon_stream_sync",
-    "canon_check_bibd_noalloc",
+    "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys",
 ]
 
 
@@ -89,6 +89,15 @@ class DeviceOutputs(ctypes.Structure):
                 ("player_index", ctypes.c_void_p), ("witness", ctypes.c_void_p),
                 ("aut", ctypes.c_void_p), ("trials", ctypes.c_void_p), ("n_auts", ctypes.c_void_p),
                 ("len_aut", ctypes.c_void_p), ("auts", ctypes.c_void_p), ("aut_cap", ctypes.c_uint32)]
+
+
+class EnumStats(ctypes.Structure):
+    _fields_ = [("checks", ctypes.c_uint64), ("designs", ctypes.c_uint64), ("levels", ctypes.c_uint32),
+                ("batches", ctypes.c_uint32), ("seconds", ctypes.c_double), ("kernel_ms", ctypes.c_double)]
+
+
+DESIGN_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint32,
+                             ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64)
 
 
 class Results(ctypes.Structure):
@@ -144,6 +153,8 @@ def load_library(path=LIB_PATH):
     L.canon_kernel_launches.restype = u64
     L.canon_stream_sync.argtypes = [vp]
     L.canon_check_bibd_noalloc.argtypes = [u32, u32, u32, u32, vp, vp, ctypes.POINTER(DeviceOutputs), u64, vp]
+    L.canon_enumerate_bibd.argtypes = [vp, u32, u32, u32, u32, u32, DESIGN_CB, vp, ctypes.POINTER(EnumStats)]
+    L.canon_enumerate_ksys.argtypes = [vp, u32, DESIGN_CB, vp, ctypes.POINTER(EnumStats)]
     _lib = L
     return L
 
@@ -275,6 +286,33 @@ class Context:
                           d_status=None, d_trials=None, stream=None):
         self._check(self.lib.canon_check_bibd_device(self.h, n, v, b, flags, d_rows, d_canonical,
                                                      d_witness, d_aut, d_status, d_trials, stream))
+
+    # ---- frontier-batched enumeration ----
+    def enumerate_bibd(self, v, b, r, k, lam):
+        """All BIBD(v,b,r,k,lambda) up to isomorphism: [(matrix v x b uint8, |Aut|)], stats."""
+        found = []
+
+        def cb(user, M, rows, cols, lo, hi):
+            words = np.ctypeslib.as_array(ctypes.cast(M, ctypes.POINTER(ctypes.c_uint64)),
+                                          shape=(rows,)).copy()
+            found.append((unpack_rows(words, cols), int(lo) | (int(hi) << 64)))
+
+        c = DESIGN_CB(cb)
+        st = EnumStats()
+        self._check(self.lib.canon_enumerate_bibd(self.h, v, b, r, k, lam, c, None, ctypes.byref(st)))
+        return found, st
+
+    def enumerate_ksys(self, np_):
+        """All 1-factorizations of K_np up to isomorphism: [(rounds x np uint8, |Aut|)], stats."""
+        found = []
+
+        def cb(user, M, rows, cols, lo, hi):
+            found.append((np.ctypeslib.as_array(M, shape=(rows * cols,)).reshape(rows, cols).copy(), int(lo)))
+
+        c = DESIGN_CB(cb)
+        st = EnumStats()
+        self._check(self.lib.canon_enumerate_ksys(self.h, np_, c, None, ctypes.byref(st)))
+        return found, st
 
     def stream_sync(self):
         self._check(self.lib.canon_stream_sync(self.h))

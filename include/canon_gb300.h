@@ -190,6 +190,33 @@ float canon_last_kernel_ms(const canon_ctx *ctx);
 uint64_t canon_kernel_launches(const canon_ctx *ctx);
 int canon_stream_sync(canon_ctx *ctx);
 
+/* ---- frontier-batched orderly enumeration (the callers of the check) ---- */
+typedef struct {
+    uint64_t checks;      /* matrices checked on the GPU */
+    uint64_t designs;     /* canonical complete matrices */
+    uint32_t levels;      /* rows / rounds added */
+    uint32_t batches;     /* canon_sync calls */
+    double   seconds;     /* wall time */
+    double   kernel_ms;   /* device time of the checks */
+} canon_enum_stats;
+
+/* Called for every canonical complete matrix: BIBD rows as rows x uint64 (cast to
+ * bytes), k-systems as rows x cols bytes in result() form; |Aut| as (lo, hi). */
+typedef void (*canon_design_cb)(void *user, const uint8_t *matrix, uint32_t rows, uint32_t cols,
+                                uint64_t aut_lo, uint64_t aut_hi);
+
+/* All BIBD(v, b, r, k, lambda) up to isomorphism by orderly generation, level by
+ * level, every level's partial matrices checked in batches on the GPU: the work of
+ * CEnumerator::Enumerate() with C_InSysEnumerator/CBIBD_Enumerator
+ * (Source/Enumerator.cpp:540-1024; checks at :446-447 and :364).  v <= 16, b <= 63. */
+int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uint32_t k, uint32_t lambda,
+                         canon_design_cb cb, void *user, canon_enum_stats *stats);
+/* All 1-factorizations of K_np up to isomorphism, round by round, every round's
+ * partial matrices checked in batches on the GPU: the work of alldata::Run() for
+ * group size 2 with the check at every level (k-Factorization/TripleSys/Source/
+ * TripleSys.cpp:80-775, check at checkCurrentResult.cpp:91).  np even, <= 12. */
+int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *user, canon_enum_stats *stats);
+
 /* ---- checking without allocating ---- */
 /* Device output arrays of canon_check_bibd_noalloc (one entry per matrix, same
  * meaning as the canon_results fields).  auts may be NULL unless CANON_SAVE_AUTS

@@ -114,3 +114,16 @@ def test_partial_prefixes(host):
                     f = COMPLETE if k == P.shape[0] else 0
                     compare(host, oracle.bibd_normalize(P[:k]), f)
                     compare(host, oracle.bibd_normalize(P[:k]), f | FULL_AUT)
+
+
+def test_trial_budget_ends_the_search_with_a_timeout_status(host):
+    import ise_gb300 as G
+    M = cases.load_sts15()[0][0]
+    rows = np.ascontiguousarray(G.pack_rows(M), np.uint64)
+    u8, u64 = ctypes.c_uint8, ctypes.c_uint64
+    for flags in (COMPLETE, COMPLETE | REFERENCE_ORDER):
+        can, st, rr, w, tr = u8(), u8(), u8(), u64(), u64()
+        aut = (u64 * 2)()
+        host.emu_check(rows.ctypes.data_as(ctypes.POINTER(u64)), 15, 35, flags, u64(4), ctypes.byref(can),
+                       ctypes.byref(st), ctypes.byref(rr), ctypes.byref(w), aut, ctypes.byref(tr))
+        assert st.value & 2 and not can.value

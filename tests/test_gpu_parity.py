@@ -239,3 +239,18 @@ def test_edge_cases(ctx):
     ctx.submit_ksys(R, 10, 9, 0)
     r = ctx.sync()
     assert r["status"][0] & G.ST_BADINPUT
+
+
+def test_trial_budget_reports_timeout_not_a_hang():
+    ctx = G.Context(max_items=64, aut_cap=1, max_trials=4)
+    try:
+        M = cases.load_sts15()[0][0]
+        ctx.submit_bibd(G.pack_rows(M), 15, 35, G.COMPLETE)
+        with pytest.raises(G.CanonError) as e:
+            ctx.sync()
+        assert e.value.code == G.CANON_ETIMEOUT
+        ctx.submit_bibd(G.pack_rows(M), 15, 35, G.COMPLETE)
+        r = ctx.sync(allow_timeout=True)
+        assert r["status"][0] & G.ST_TIMEOUT and not r["canonical"][0]
+    finally:
+        ctx.close()
