@@ -302,6 +302,54 @@ def run_gpu(args, rank, world, local, dist):
     ctx.close()
 
 
+ENUM_WORKLOADS = {
+    "enum-sts13": ("bibd", (13, 26, 6, 3, 1), "config 1: all BIBD(13,26,6,3,1) (STS(13)) by orderly generation"),
+    "enum-sts15": ("bibd", (15, 35, 7, 3, 1), "all BIBD(15,35,7,3,1) (STS(15)) by orderly generation"),
+    "enum-k10": ("ksys", (10,), "config 5: all 1-factorizations of K10, every round checked"),
+}
+
+
+def run_enum(args):
+    """Whole enumerations with every level checked on the GPU (configs 1 and 5)."""
+    import ise_gb300 as G
+    kind, params, desc = ENUM_WORKLOADS[args.workload]
+    ctx = G.Context(max_items=1 << 16)
+    runs = []
+    for _ in range(args.warmup + args.steps):
+        if kind == "bibd":
+            found, st = ctx.enumerate_bibd(*params)
+        else:
+            found, st = ctx.enumerate_ksys(*params)
+        runs.append((len(found), st.checks, st.seconds, st.kernel_ms, st.batches))
+    timed = runs[args.warmup:]
+    secs = sum(r[2] for r in timed)
+    checks = sum(r[1] for r in timed)
+    designs = sum(r[0] for r in timed)
+    cpu = None
+    if not args.no_cpu:
+        import time as _t
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import oracle
+        t0 = _t.perf_counter()
+        if kind == "bibd":
+            ref, nchk = oracle.bibd_enumerate(*params)
+        else:
+            ref, nchk = oracle.ksys_enumerate(*params)
+        dt = _t.perf_counter() - t0
+        assert len(ref) == timed[0][0]
+        cpu = {"value": len(ref) / dt, "unit": "designs/s", "cores": 1, "kind": "port",
+               "sample": "one whole enumeration (%d checks, %.1f s)" % (nchk, dt)}
+    line = {"metric": "designs/sec (%s)" % args.workload, "value": designs / secs, "unit": "designs/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 bit rows / u8",
+            "data": "exhaustive", "config": {"workload": desc, "designs": timed[0][0],
+                                             "checks_per_step": timed[0][1], "batches_per_step": timed[0][4]},
+            "checks_per_s": checks / secs, "kernel_ms_per_step": sum(r[3] for r in timed) / args.steps,
+            "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -312,12 +360,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--items", type=int, default=N_ITEMS,
                     help="matrices per step (default: the full 1,048,576; smaller only for profiling)")
+    ap.add_argument("--workload", default="check-sts15", choices=["check-sts15"] + sorted(ENUM_WORKLOADS),
+                    help="check-sts15 (default, the metric's configuration) or a whole enumeration")
     ap.add_argument("--mode", default="autcanon", choices=["autcanon", "plain"],
                     help="autcanon: |Aut| of rejected matrices via canonization (the workload); "
                          "plain: the reference's TestCanonicity outputs only")
     args = ap.parse_args()
     rank, world, local, dist = dist_setup(args.gpus)
-    if args.impl == "reference":
+    if args.workload != "check-sts15":
+        if rank == 0:
+            run_enum(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world, dist)
     else:
         run_gpu(args, rank, world, local, dist)
