@@ -350,6 +350,120 @@ def run_enum(args):
     ctx.close()
 
 
+MIX_SHAPES = [  # (share, kind, (v, b, r, k, lambda) or np, min filled rows, max filled rows)
+    (0.40, "bibd", (15, 35, 7, 3, 1), 5, 15),
+    (0.30, "bibd", (8, 14, 7, 4, 3), 4, 8),
+    (0.20, "bibd", (11, 11, 5, 5, 2), 4, 11),
+    (0.10, "ksys", 10, 3, 9),
+]
+
+
+def _permute_bits(words, perm):
+    """Column permutation of packed rows: new column c = old column perm[c]."""
+    bits = (words[..., None] >> perm.astype(np.uint64)) & np.uint64(1)
+    return (bits << np.arange(len(perm), dtype=np.uint64)).sum(axis=-1, dtype=np.uint64)
+
+
+def build_mix(ctx, n_total, seed):
+    """Seeded stand-in for the uneven batch of config 3: partial matrices that are
+    prefixes of randomly relabelled designs (so every one is a valid partial design)."""
+    import ise_gb300 as G
+    rng = np.random.default_rng(seed)
+    batches = []
+    for share, kind, params, lo, hi in MIX_SHAPES:
+        cnt = int(round(share * n_total))
+        nr = rng.integers(lo, hi + 1, size=cnt).astype(np.uint8)
+        if kind == "bibd" and params[0] == 15:
+            d = ctx.alloc(cnt * 15 * 8)
+            ctx.generate_sts_device(cnt, 15, seed + 1, False, d)
+            rows = ctx.d2h(np.zeros(cnt * 15, np.uint64), d).reshape(cnt, 15)
+            ctx.free(d)
+            batches.append(("bibd", 15, 35, rows, nr))
+        elif kind == "bibd":
+            v, b = params[0], params[1]
+            designs, _ = ctx.enumerate_bibd(*params)
+            base = np.stack([G.pack_rows(M) for M, _ in designs])
+            pick = rng.integers(len(base), size=cnt)
+            rp = np.argsort(rng.random((cnt, v)), axis=1)
+            rows = np.take_along_axis(base[pick], rp, axis=1)
+            cp = np.argsort(rng.random((cnt, b)), axis=1)
+            rows = _permute_bits(rows, cp[:, None, :].repeat(v, axis=1))
+            batches.append(("bibd", v, b, rows, nr))
+        else:
+            found, _ = ctx.enumerate_ksys(params)
+            base = np.stack([R for R, _ in found])                       # 396 x 9 x 10
+            pick = rng.integers(len(base), size=cnt)
+            R = base[pick].astype(np.int64)
+            # relabel so that a random round becomes round 0 = (0 1)(2 3)...
+            d = rng.integers(9, size=cnt)
+            src = R[np.arange(cnt), d]                                   # cnt x 10 players in pair order
+            gperm = np.argsort(rng.random((cnt, 5)), axis=1)
+            flip = rng.integers(2, size=(cnt, 5))
+            lab = np.zeros((cnt, 10), np.int64)
+            for g in range(5):
+                a_ = src[np.arange(cnt), 2 * gperm[:, g]]
+                b_ = src[np.arange(cnt), 2 * gperm[:, g] + 1]
+                x_ = np.where(flip[:, g] == 1, b_, a_)
+                y_ = np.where(flip[:, g] == 1, a_, b_)
+                lab[np.arange(cnt), x_] = 2 * g
+                lab[np.arange(cnt), y_] = 2 * g + 1
+            X = np.take_along_axis(lab[:, None, :].repeat(9, axis=1), R, axis=2)   # relabelled rounds
+            pa, pb = X[..., 0::2], X[..., 1::2]
+            lo_, hi_ = np.minimum(pa, pb), np.maximum(pa, pb)
+            order = np.argsort(lo_, axis=2)
+            lo_ = np.take_along_axis(lo_, order, axis=2)
+            hi_ = np.take_along_axis(hi_, order, axis=2)
+            rounds = np.stack([lo_, hi_], axis=3).reshape(cnt, 9, 10)
+            rorder = np.argsort(rounds[:, :, 1], axis=1)
+            rounds = np.take_along_axis(rounds, rorder[:, :, None], axis=1).astype(np.uint8)
+            batches.append(("ksys", 10, 9, rounds, nr))
+    return batches
+
+
+def run_mix(args):
+    """Config 3: one persistent launch over the uneven 2M mix."""
+    import ise_gb300 as G
+    n_total = args.items if args.items != N_ITEMS else 2_097_152
+    ctx = G.Context(max_items=n_total + 16, max_words=16 * n_total, aut_cap=1)
+    batches = build_mix(ctx, n_total, SEED + 3)
+    n = sum(len(b[4]) for b in batches)
+
+    def submit():
+        for kind, v, b, rows, nr in batches:
+            if kind == "bibd":
+                ctx.submit_bibd(rows, v, b, G.RAW, nr)
+            else:
+                ctx.submit_ksys(rows, v, b, 0, nr)
+
+    for _ in range(args.warmup):
+        submit()
+        ctx.sync()
+    l0 = ctx.kernel_launches()
+    kms, walls = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            submit()
+            r = ctx.sync()
+            walls.append(time.perf_counter() - t0)
+            kms.append(r["kernel_ms"])
+    assert r["n"] == n and not r["status"].any()
+    line = {"metric": "exact canonicity checks/sec (config 3 uneven mix, one persistent launch)",
+            "value": n * args.steps / (sum(kms) / 1e3), "unit": "checks/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sum(kms) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64 bit rows / u8", "data": "synthetic",
+            "config": {"workload": "%d partial matrices: 40%% STS(15) 5-15 rows, 30%% BIBD(8,14,7,4,3) 4-8, "
+                                   "20%% BIBD(11,11,5,5,2) 4-11, 10%% K10 3-9 rounds; prefixes of randomly "
+                                   "relabelled designs, seed %d" % (n, SEED + 3),
+                       "canonical_fraction": float(r["canonical"].mean())},
+            "e2e": {"value": n * args.steps / sum(walls), "unit": "checks/s",
+                    "h2d_bytes_per_step": int(sum(b[3].nbytes for b in batches) + 16 * n),
+                    "d2h_bytes_per_step": 51 * n},
+            "gpu_launches": ctx.kernel_launches() - l0, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -360,14 +474,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--items", type=int, default=N_ITEMS,
                     help="matrices per step (default: the full 1,048,576; smaller only for profiling)")
-    ap.add_argument("--workload", default="check-sts15", choices=["check-sts15"] + sorted(ENUM_WORKLOADS),
+    ap.add_argument("--workload", default="check-sts15", choices=["check-sts15", "mix"] + sorted(ENUM_WORKLOADS),
                     help="check-sts15 (default, the metric's configuration) or a whole enumeration")
     ap.add_argument("--mode", default="autcanon", choices=["autcanon", "plain"],
                     help="autcanon: |Aut| of rejected matrices via canonization (the workload); "
                          "plain: the reference's TestCanonicity outputs only")
     args = ap.parse_args()
     rank, world, local, dist = dist_setup(args.gpus)
-    if args.workload != "check-sts15":
+    if args.workload == "mix":
+        if rank == 0:
+            run_mix(args)
+    elif args.workload != "check-sts15":
         if rank == 0:
             run_enum(args)
     elif args.impl == "reference":

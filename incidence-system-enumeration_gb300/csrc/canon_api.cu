@@ -282,14 +282,20 @@ int canon_sync(canon_ctx *c, canon_results *r) {
         if (c->n_bytes)
             cudaMemcpyAsync(c->d_bytes, c->h_bytes, c->n_bytes, cudaMemcpyHostToDevice, s);
         cudaEventRecord(c->ev0, s);
-        if (c->n_bitems) {
+        if (c->n_bitems && c->n_kitems) {
+            // uneven batch: one persistent launch for both kinds
+            e = canon::launch_mixed_check(c->d_bitems, c->n_bitems, c->d_kitems, c->n_kitems, c->d_words,
+                                          c->d_bytes, c->d_out, c->cfg.max_trials, c->d_ticket, c->num_sms, s);
+            if (e != cudaSuccess)
+                return cuda_fail(c, e, "mixed check launch");
+            ++c->launches;
+        } else if (c->n_bitems) {
             e = canon::launch_bibd_check(c->d_bitems, c->n_bitems, c->d_words, c->d_out, c->cfg.max_trials,
                                          c->d_ticket, c->num_sms, s);
             if (e != cudaSuccess)
                 return cuda_fail(c, e, "bibd check launch");
             ++c->launches;
-        }
-        if (c->n_kitems) {
+        } else if (c->n_kitems) {
             e = canon::launch_ksys_check(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, c->d_ticket + 1,
                                          c->num_sms, s);
             if (e != cudaSuccess)

@@ -8,6 +8,8 @@
 
 namespace canon {
 namespace bibd {
+// internal linkage: the header is compiled into more than one translation unit
+namespace {
 
 constexpr int TPB = 64;                  // threads per block (one matrix each)
 constexpr uint64_t ID16 = 0xFEDCBA9876543210ull;
@@ -832,5 +834,47 @@ __device__ void check_one(Smem sm, const uint64_t *src, unsigned n, unsigned b, 
         o.canonical = 0;
 }
 
+__device__ __forceinline__ void store_witness(uint8_t *dst16, uint64_t w, unsigned n) {
+    uint32_t wd[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const unsigned i = q * 4 + k;
+            const unsigned byte = (w == ~0ull || i >= n) ? 0xFFu : pg(w, i);
+            v |= byte << (8 * k);
+        }
+        wd[q] = v;
+    }
+    reinterpret_cast<uint4 *>(dst16)[0] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+}
+
+// One work item of a batch: the check and the writes of every output array.
+__device__ void check_item(Smem sm, const Item &item, const uint64_t *__restrict__ words, Outputs out,
+                           uint64_t max_trials) {
+    const unsigned n = item.nrows, b = item.ncols, o_i = item.out_idx;
+    CheckOut o;
+    if (item.kind != KIND_BIBD || n < 1 || n > VMAX || b < 1 || b > BMAX) {
+        o = CheckOut{0, ST_BADINPUT, 0xFF, 0xFF, ~0ull, 0, 0, 0, 0, 0};
+    } else {
+        uint8_t *adst =
+            (item.flags & F_SAVE_AUTS) && out.auts ? out.auts + (size_t)o_i * out.aut_cap * 64u : nullptr;
+        check_one(sm, words + item.data_off, n, b, item.flags, max_trials, adst, out.aut_cap, o);
+    }
+    out.canonical[o_i] = o.canonical;
+    out.status[o_i] = o.status;
+    out.reject_row[o_i] = o.reject_row;
+    out.row_to_change[o_i] = o.rtc;
+    out.player_index[o_i] = -1;
+    store_witness(out.witness + (size_t)o_i * 16u, o.witness, n);
+    out.aut[2 * (size_t)o_i] = o.aut_lo;
+    out.aut[2 * (size_t)o_i + 1] = o.aut_hi;
+    out.trials[o_i] = o.trials;
+    out.n_auts[o_i] = o.n_auts;
+    out.len_aut[o_i] = o.len_aut;
+}
+
+}  // namespace
 }  // namespace bibd
 }  // namespace canon

@@ -67,6 +67,11 @@ cudaError_t launch_sts_generate(uint32_t n, uint32_t v, uint64_t seed, uint64_t 
                                 int num_sms, cudaStream_t s);
 cudaError_t launch_ksys_check(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes,
                               Outputs out, unsigned *d_ticket, int num_sms, cudaStream_t s);
+// one persistent launch over a mixed batch: k-system items (warp each) then incidence items (thread each);
+// d_ticket: two device words
+cudaError_t launch_mixed_check(const Item *d_bitems, uint32_t nb, const Item *d_kitems, uint32_t nk,
+                               const uint64_t *d_words, const uint8_t *d_bytes, Outputs out,
+                               uint64_t max_trials, unsigned *d_ticket, int num_sms, cudaStream_t s);
 cudaError_t ksys_upload_tables();
 
 }  // namespace canon

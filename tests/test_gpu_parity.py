@@ -254,3 +254,52 @@ def test_trial_budget_reports_timeout_not_a_hang():
         assert r["status"][0] & G.ST_TIMEOUT and not r["canonical"][0]
     finally:
         ctx.close()
+
+
+def test_mixed_batch_one_persistent_launch(ctx):
+    """Incidence matrices of three shapes and k-systems in one sync (the fused kernel)."""
+    rng = np.random.default_rng(17)
+    sts = cases.load_sts15()
+    groups = []
+    for params, cnt in [((15, 35, 7, 3, 1), 24), ((8, 14, 7, 4, 3), 16), ((11, 11, 5, 5, 2), 12)]:
+        designs = [M for M, _ in sts] if params[0] == 15 else [M for M, _ in cases.bibd_designs(*params)]
+        v, b = params[0], params[1]
+        mats = []
+        for _ in range(cnt):
+            M = designs[int(rng.integers(len(designs)))]
+            P = M[rng.permutation(v)][:, rng.permutation(b)]
+            k = int(rng.integers(3, v + 1))
+            mats.append(P[:k])
+        groups.append((v, b, mats))
+    k10 = cases.load_k10()
+    kmats, knr = [], []
+    for _ in range(20):
+        R = cases.ksys_relabel_random(k10[int(rng.integers(396))][0], rng)
+        k = int(rng.integers(3, 10))
+        pad = np.zeros((9, 10), np.uint8)
+        pad[:k] = R[:k]
+        kmats.append(pad)
+        knr.append(k)
+    for v, b, mats in groups:
+        rows = np.zeros((len(mats), v), np.uint64)
+        nr = np.zeros(len(mats), np.uint8)
+        for i, M in enumerate(mats):
+            rows[i, :M.shape[0]] = G.pack_rows(M)
+            nr[i] = M.shape[0]
+        ctx.submit_bibd(rows, v, b, G.RAW | G.FULL_AUT, nr)
+    ctx.submit_ksys(np.stack(kmats), 10, 9, 0, np.array(knr, np.uint8))
+    r = ctx.sync()
+    i = 0
+    for v, b, mats in groups:
+        for M in mats:
+            o = oracle_bibd(M, G.RAW | G.FULL_AUT)
+            assert r["status"][i] == 0
+            assert bool(r["canonical"][i]) == o["canonical"], i
+            assert r["aut"][i] == o["aut"], i
+            if not o["canonical"]:
+                assert bytes(r["witness"][i][:M.shape[0]]) == o["witness"], i
+            i += 1
+    for M, k in zip(kmats, knr):
+        o = oracle.ksys_test(M[:k])
+        assert bool(r["canonical"][i]) == o["canonical"] and int(r["player_index"][i]) == o["player_index"], i
+        i += 1
