@@ -361,7 +361,7 @@ MIX_SHAPES = [  # (share, kind, (v, b, r, k, lambda) or np, min filled rows, max
 def _permute_bits(words, perm):
     """Column permutation of packed rows: new column c = old column perm[c]."""
     bits = (words[..., None] >> perm.astype(np.uint64)) & np.uint64(1)
-    return (bits << np.arange(len(perm), dtype=np.uint64)).sum(axis=-1, dtype=np.uint64)
+    return (bits << np.arange(perm.shape[-1], dtype=np.uint64)).sum(axis=-1, dtype=np.uint64)
 
 
 def build_mix(ctx, n_total, seed):
