@@ -41,6 +41,10 @@ WORKLOAD = ("1,048,576 STS(15) 15x35 bit-packed matrices, seed %d, odd items can
             "outputs canonical flag + first rejecting permutation + |Aut|" % SEED)
 IN_BYTES = V * 8          # packed rows read per check
 OUT_BYTES = 1 + 16 + 16   # flag + witness + |Aut| written per check
+# DRAM bytes per check of the check kernel: dram__bytes_read.sum + dram__bytes_write.sum of one ncu
+# capture of 131,072 checks (15,918,592 B + 0 B; profiles/bibd_uniform_kernel_sts15_131k.md),
+# scaled by the checks of a launch (traffic grows with the number of matrices read).
+TRAFFIC_PER_CHECK = 15918592.0 / 131072
 MEASURED_PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
 
 
@@ -289,7 +293,7 @@ def run_gpu(args, rank, world, local, dist):
             "e2e": None if e2e_dt is None else {"value": world * n / e2e_dt, "unit": "checks/s",
                                                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
+                         "frac": achieved / hbm, "traffic": TRAFFIC_PER_CHECK * n,
                          "note": "peak %s; the check is an integer search (ALU/issue bound), HBM "
                                  "traffic is %d B per check" % (src, IN_BYTES + OUT_BYTES)},
             "cpu_baseline": cpu,

@@ -38,6 +38,15 @@ struct canon_ctx {
     unsigned *d_ticket = nullptr;      // work-stealing counters (2 words)
     Outputs d_out{}, h_out{};
     std::vector<uint8_t> item_kind;   // per out_idx
+    // learned order: installed weights (device) and lazily grown scratch
+    bool order_on = false;
+    float *d_mlp = nullptr;            // flat FP32 parameters (canon::mlp::N_PARAMS)
+    uint16_t *d_w1 = nullptr, *d_w2 = nullptr, *d_w2t = nullptr, *d_w3 = nullptr;   // BF16 copies
+    float *d_adam_m = nullptr, *d_adam_v = nullptr, *d_grad = nullptr, *d_loss = nullptr;
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint64_t *d_orders = nullptr;
+    size_t d_orders_bytes = 0;
     std::string err;
     float last_ms = 0.f;
     uint64_t launches = 0;
@@ -93,6 +102,107 @@ void free_outputs(Outputs &o, bool device) {
         if (p)
             device ? cudaFree(p) : cudaFreeHost(p);
     o = Outputs{};
+}
+
+uint16_t to_bf16(float f) {
+    // round to nearest even (NaN kept quiet)
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7F800000u) == 0x7F800000u && (u & 0x7FFFFFu))
+        return (uint16_t)((u >> 16) | 0x40u);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+constexpr int P_W1 = 0, P_B1 = 128 * 64, P_W2 = P_B1 + 128, P_B2 = P_W2 + 128 * 128, P_W3 = P_B2 + 128,
+              P_B3 = P_W3 + 128;
+
+cudaError_t ensure_mlp(canon_ctx *c) {
+    if (c->d_mlp)
+        return cudaSuccess;
+    cudaError_t e = dev_alloc(&c->d_mlp, canon::mlp::N_PARAMS);
+    if (e == cudaSuccess)
+        e = dev_alloc(&c->d_w1, 128 * 64);
+    if (e == cudaSuccess)
+        e = dev_alloc(&c->d_w2, 128 * 128);
+    if (e == cudaSuccess)
+        e = dev_alloc(&c->d_w2t, 128 * 128);
+    if (e == cudaSuccess)
+        e = dev_alloc(&c->d_w3, 128);
+    if (e == cudaSuccess)
+        e = dev_alloc(&c->d_adam_m, canon::mlp::N_PARAMS);
+    if (e == cudaSuccess)
+        e = dev_alloc(&c->d_adam_v, canon::mlp::N_PARAMS);
+    if (e == cudaSuccess)
+        e = dev_alloc(&c->d_grad, canon::mlp::N_PARAMS);
+    if (e == cudaSuccess)
+        e = dev_alloc(&c->d_loss, 1);
+    return e;
+}
+
+// upload flat FP32 parameters and their BF16 copies (W2 also transposed)
+cudaError_t upload_params(canon_ctx *c, const float *p) {
+    cudaError_t e = ensure_mlp(c);
+    if (e != cudaSuccess)
+        return e;
+    std::vector<uint16_t> w1(128 * 64), w2(128 * 128), w2t(128 * 128), w3(128);
+    for (int i = 0; i < 128 * 64; ++i)
+        w1[i] = to_bf16(p[P_W1 + i]);
+    for (int o = 0; o < 128; ++o)
+        for (int i = 0; i < 128; ++i) {
+            w2[o * 128 + i] = to_bf16(p[P_W2 + o * 128 + i]);
+            w2t[i * 128 + o] = w2[o * 128 + i];
+        }
+    for (int i = 0; i < 128; ++i)
+        w3[i] = to_bf16(p[P_W3 + i]);
+    cudaStream_t s = c->stream;
+    cudaMemcpyAsync(c->d_mlp, p, canon::mlp::N_PARAMS * 4, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->d_w1, w1.data(), w1.size() * 2, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->d_w2, w2.data(), w2.size() * 2, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->d_w2t, w2t.data(), w2t.size() * 2, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->d_w3, w3.data(), w3.size() * 2, cudaMemcpyHostToDevice, s);
+    return cudaStreamSynchronize(s);
+}
+
+cudaError_t ensure_scratch(canon_ctx *c, size_t bytes) {
+    if (c->scratch_bytes >= bytes)
+        return cudaSuccess;
+    if (c->d_scratch)
+        cudaFree(c->d_scratch);
+    c->d_scratch = nullptr;
+    c->scratch_bytes = 0;
+    cudaError_t e = cudaMalloc(&c->d_scratch, bytes);
+    if (e == cudaSuccess)
+        c->scratch_bytes = bytes;
+    return e;
+}
+
+cudaError_t mlp_forward_installed(canon_ctx *c, long n, const void *x, float *y, void *h1, void *h2, cudaStream_t s) {
+    return canon::mlp::forward(n, x, c->d_w1, c->d_mlp + P_B1, c->d_w2, c->d_mlp + P_B2, c->d_w3, c->d_mlp + P_B3, y,
+                               h1, h2, c->num_sms, s);
+}
+
+// orders of the first-row candidates for n matrices (chunked: features, scores, sort)
+cudaError_t compute_orders(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, const uint64_t *d_rows,
+                           uint64_t *d_orders, cudaStream_t s) {
+    const uint32_t chunk = 1u << 16;
+    const size_t feat_bytes = (size_t)chunk * v * 64 * 2, score_bytes = (size_t)chunk * v * 4;
+    cudaError_t e = ensure_scratch(c, feat_bytes + score_bytes + 256);
+    if (e != cudaSuccess)
+        return e;
+    void *feat = c->d_scratch;
+    float *scores = reinterpret_cast<float *>(static_cast<char *>(c->d_scratch) + feat_bytes);
+    for (uint32_t off = 0; off < n; off += chunk) {
+        const uint32_t cnt = (n - off < chunk) ? n - off : chunk;
+        e = canon::mlp::features(cnt, v, b, 0, d_rows + (size_t)off * v, feat, s);
+        if (e == cudaSuccess)
+            e = mlp_forward_installed(c, (long)cnt * v, feat, scores, nullptr, nullptr, s);
+        if (e == cudaSuccess)
+            e = canon::launch_order_by_score(cnt, v, scores, d_orders + off, s);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -170,7 +280,9 @@ void canon_destroy(canon_ctx *c) {
         cudaStreamSynchronize(c->stream);
     free_outputs(c->d_out, true);
     free_outputs(c->h_out, false);
-    void *dptrs[] = {c->d_bitems, c->d_kitems, c->d_words, c->d_bytes, c->d_ticket};
+    void *dptrs[] = {c->d_bitems, c->d_kitems, c->d_words, c->d_bytes, c->d_ticket, c->d_mlp, c->d_w1, c->d_w2,
+                     c->d_w2t, c->d_w3, c->d_adam_m, c->d_adam_v, c->d_grad, c->d_loss, c->d_scratch,
+                     c->d_orders};
     for (void *p : dptrs)
         if (p)
             cudaFree(p);
@@ -373,8 +485,35 @@ int canon_sync(canon_ctx *c, canon_results *r) {
 int canon_set_ordering(canon_ctx *c, const canon_mlp_weights *w) {
     if (!c)
         return CANON_EINVAL;
-    if (w)
-        return fail(c, CANON_EINVAL, "learned ordering is not available in this build");
+    if (!w) {
+        c->order_on = false;
+        return CANON_OK;
+    }
+    if (w->in_dim != 64 || w->hidden != 128 || !w->w1 || !w->w2 || !w->w3 || !w->b1 || !w->b2 || !w->b3)
+        return fail(c, CANON_EINVAL, "ordering: need in_dim 64, hidden 128 and all weights");
+    // BF16 weights -> the flat FP32 vector the kernels read
+    std::vector<float> p(canon::mlp::N_PARAMS);
+    auto f32 = [](uint16_t h) {
+        uint32_t u = (uint32_t)h << 16;
+        float f;
+        std::memcpy(&f, &u, 4);
+        return f;
+    };
+    for (int i = 0; i < 128 * 64; ++i)
+        p[P_W1 + i] = f32(w->w1[i]);
+    for (int i = 0; i < 128 * 128; ++i)
+        p[P_W2 + i] = f32(w->w2[i]);
+    for (int i = 0; i < 128; ++i) {
+        p[P_W3 + i] = f32(w->w3[i]);
+        p[P_B1 + i] = w->b1[i];
+        p[P_B2 + i] = w->b2[i];
+    }
+    p[P_B3] = w->b3[0];
+    cudaSetDevice(c->device);
+    cudaError_t e = upload_params(c, p.data());
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "ordering upload");
+    c->order_on = true;
     return CANON_OK;
 }
 
@@ -423,10 +562,31 @@ int canon_check_bibd_device(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, ui
                     "REFERENCE_ORDER");
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
+    uint64_t *orders = nullptr;
     cudaEventRecord(c->ev0, s);
+    if (c->order_on) {
+        // learned order of the first rows: features, scores and the sort are part of the timed check
+        const size_t need = (size_t)n * 8 + 256;
+        cudaError_t e0 = cudaSuccess;
+        if (!c->d_orders_bytes || c->d_orders_bytes < need) {
+            if (c->d_orders)
+                cudaFree(c->d_orders);
+            c->d_orders = nullptr;
+            c->d_orders_bytes = 0;
+            e0 = cudaMalloc((void **)&c->d_orders, need);
+            if (e0 == cudaSuccess)
+                c->d_orders_bytes = need;
+        }
+        if (e0 == cudaSuccess)
+            e0 = compute_orders(c, n, v, b, d_rows, c->d_orders, s);
+        if (e0 != cudaSuccess)
+            return cuda_fail(c, e0, "learned order");
+        orders = c->d_orders;
+        c->launches += 3 * ((n + 65535) / 65536);
+    }
     cudaError_t e = canon::launch_bibd_check_uniform(n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut,
                                                      d_status, d_trials, c->cfg.max_trials, c->d_ticket,
-                                                     c->num_sms, s);
+                                                     c->num_sms, s, orders);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "check launch");
     ++c->launches;
@@ -513,6 +673,128 @@ int canon_stream_sync(canon_ctx *c) {
     cudaSetDevice(c->device);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "stream sync");
+}
+
+int canon_mlp_features(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, const uint64_t *d_rows, void *d_feat) {
+    if (!c || !d_rows || !d_feat || v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX)
+        return fail(c, CANON_EINVAL, "features: bad arguments");
+    cudaSetDevice(c->device);
+    cudaError_t e = canon::mlp::features(n, v, b, 0, d_rows, d_feat, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    ++c->launches;
+    return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "features");
+}
+
+int canon_label_first_rows(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                           uint16_t *d_first_rows, uint64_t *d_nodes, const uint64_t *d_orders) {
+    if (!c || !d_rows || v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX)
+        return fail(c, CANON_EINVAL, "labels: bad arguments");
+    cudaSetDevice(c->device);
+    cudaEventRecord(c->ev0, c->stream);
+    cudaError_t e = canon::launch_bibd_labels(n, v, b, flags, d_rows, d_first_rows, d_nodes, d_orders,
+                                              c->cfg.max_trials, c->d_ticket, c->num_sms, c->stream);
+    cudaEventRecord(c->ev1, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    ++c->launches;
+    return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "labels");
+}
+
+int canon_mlp_forward(canon_ctx *c, uint64_t n, const void *d_x, const float *params, float *d_logits) {
+    if (!c || !d_x || !d_logits || !params)
+        return fail(c, CANON_EINVAL, "forward: bad arguments");
+    cudaSetDevice(c->device);
+    cudaError_t e = upload_params(c, params);
+    if (e == cudaSuccess)
+        e = mlp_forward_installed(c, (long)n, d_x, d_logits, nullptr, nullptr, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    ++c->launches;
+    return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "forward");
+}
+
+// one forward + backward over rows [0, n) of (d_x, d_labels) into c->d_grad (zeroed first)
+static cudaError_t mlp_grad_pass(canon_ctx *c, long n, const void *d_x, const float *d_labels) {
+    const size_t act = (size_t)n * 128;
+    cudaError_t e = ensure_scratch(c, (size_t)n * 4 + act * 2 * 2 + (size_t)n * 4 + act * 4 * 2 + 1024);
+    if (e != cudaSuccess)
+        return e;
+    char *base = static_cast<char *>(c->d_scratch);
+    float *logit = reinterpret_cast<float *>(base);
+    void *h1 = base + (size_t)n * 4;
+    void *h2 = base + (size_t)n * 4 + act * 2;
+    float *dy = reinterpret_cast<float *>(base + (size_t)n * 4 + act * 4);
+    float *dh2 = reinterpret_cast<float *>(base + (size_t)n * 8 + act * 4);
+    float *dh1 = dh2 + act;
+    cudaStream_t s = c->stream;
+    cudaMemsetAsync(c->d_grad, 0, canon::mlp::N_PARAMS * 4, s);
+    cudaMemsetAsync(c->d_loss, 0, 4, s);
+    e = mlp_forward_installed(c, n, d_x, logit, h1, h2, s);
+    if (e == cudaSuccess)
+        e = canon::mlp::backward(n, logit, d_labels, h1, h2, c->d_w3, c->d_w2t, dy, dh2, dh1, c->d_loss, c->num_sms, s);
+    if (e == cudaSuccess)
+        e = canon::mlp::weight_grads(n, dh1, dh2, dy, d_x, h1, h2, c->d_grad, c->num_sms, s);
+    c->launches += 6;
+    return e;
+}
+
+int canon_mlp_grad(canon_ctx *c, uint64_t n, const void *d_x, const float *d_labels, const float *params, float *grad,
+                   float *loss) {
+    if (!c || !d_x || !d_labels || !params || !grad || !n)
+        return fail(c, CANON_EINVAL, "grad: bad arguments");
+    cudaSetDevice(c->device);
+    cudaError_t e = upload_params(c, params);
+    if (e == cudaSuccess)
+        e = mlp_grad_pass(c, (long)n, d_x, d_labels);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(grad, c->d_grad, canon::mlp::N_PARAMS * 4, cudaMemcpyDeviceToHost, c->stream);
+    float l = 0.f;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&l, c->d_loss, 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    if (loss)
+        *loss = l / (float)n;
+    return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "grad");
+}
+
+int canon_mlp_train(canon_ctx *c, uint64_t n, const void *d_x, const float *d_labels, uint32_t epochs,
+                    uint32_t batch, float lr, float *params, float *epoch_loss) {
+    if (!c || !d_x || !d_labels || !params || !n || !batch)
+        return fail(c, CANON_EINVAL, "train: bad arguments");
+    cudaSetDevice(c->device);
+    cudaError_t e = upload_params(c, params);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "train upload");
+    cudaMemsetAsync(c->d_adam_m, 0, canon::mlp::N_PARAMS * 4, c->stream);
+    cudaMemsetAsync(c->d_adam_v, 0, canon::mlp::N_PARAMS * 4, c->stream);
+    int step = 0;
+    for (uint32_t ep = 0; ep < epochs; ++ep) {
+        double lsum = 0.0;
+        for (uint64_t off = 0; off < n; off += batch) {
+            const long cnt = (long)((n - off < batch) ? n - off : batch);
+            e = mlp_grad_pass(c, cnt, static_cast<const char *>(d_x) + off * 128, d_labels + off);
+            if (e == cudaSuccess)
+                e = canon::mlp::adam(canon::mlp::N_PARAMS, c->d_mlp, c->d_grad, c->d_adam_m, c->d_adam_v, lr, ++step,
+                                     c->d_w1, c->d_w2, c->d_w2t, c->d_w3, c->stream);
+            float l = 0.f;
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(&l, c->d_loss, 4, cudaMemcpyDeviceToHost, c->stream);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(c->stream);
+            if (e != cudaSuccess)
+                return cuda_fail(c, e, "train step");
+            lsum += l;
+            ++c->launches;
+        }
+        if (epoch_loss)
+            epoch_loss[ep] = (float)(lsum / (double)n);
+    }
+    e = cudaMemcpyAsync(params, c->d_mlp, canon::mlp::N_PARAMS * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "train");
 }
 
 int canon_check_bibd_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,

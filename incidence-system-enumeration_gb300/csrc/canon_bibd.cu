@@ -44,7 +44,8 @@ __global__ void __launch_bounds__(TPB) bibd_uniform_kernel(uint32_t n_items, uin
                                                            uint32_t flags, const uint64_t *__restrict__ rows,
                                                            uint8_t *canonical, uint8_t *witness16, uint64_t *aut,
                                                            uint8_t *status, uint64_t *trials_out,
-                                                           uint64_t max_trials, unsigned *ticket) {
+                                                           uint64_t max_trials, unsigned *ticket,
+                                                           const uint64_t *__restrict__ orders) {
     __shared__ uint64_t s_rows[VMAX * TPB];
     __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
     __shared__ uint32_t s_vd[VMAX * TPB];
@@ -57,7 +58,8 @@ __global__ void __launch_bounds__(TPB) bibd_uniform_kernel(uint32_t n_items, uin
         if (it >= n_items)
             break;
         CheckOut o;
-        check_one(sm, rows + (size_t)it * v, v, b, flags & ~F_SAVE_AUTS, max_trials, nullptr, 0, o);
+        check_one(sm, rows + (size_t)it * v, v, b, flags & ~F_SAVE_AUTS, max_trials, nullptr, 0, o,
+                  orders ? orders[it] : ID16);
         canonical[it] = o.canonical;
         if (witness16)
             store_witness(witness16 + (size_t)it * 16u, o.witness, v);
@@ -113,6 +115,34 @@ __global__ void __launch_bounds__(TPB) bibd_canonize_kernel(uint32_t n_items, ui
     }
 }
 
+// Training labels of the learned order: for every matrix the set of rows that
+// start a labeling reaching its canonical form (the first rows of the lex-max
+// search's leaves), with |Aut| and the node count of the plain order.
+__global__ void __launch_bounds__(TPB) bibd_label_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
+                                                         const uint64_t *__restrict__ rows, uint16_t *first_rows,
+                                                         uint64_t *nodes, const uint64_t *__restrict__ orders,
+                                                         uint64_t max_nodes, unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint16_t s_cm[64 * TPB];
+    __shared__ uint8_t s_pc[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, s_pc + tid, s_cm + tid, s_vd + tid};
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= n_items)
+            break;
+        MaxOut mo{false, false, 0, 0, 0};
+        if (load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW))
+            max_search(sm, v, b, max_nodes, mo, orders ? orders[it] : ID16);
+        if (first_rows)
+            first_rows[it] = (uint16_t)(mo.timeout ? 0 : mo.first_rows);
+        if (nodes)
+            nodes[it] = mo.nodes;
+    }
+}
+
 int blocks_for(const void *kernel, int num_sms) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TPB, 0);
@@ -139,7 +169,8 @@ cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint6
 cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                                       const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16,
                                       uint64_t *d_aut, uint8_t *d_status, uint64_t *d_trials,
-                                      uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
+                                      uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s,
+                                      const uint64_t *d_orders) {
     if (!n)
         return cudaSuccess;
     cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
@@ -148,7 +179,21 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
     if (grid > need)
         grid = need;
     bibd_uniform_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut, d_status,
-                                             d_trials, max_trials, tk);
+                                             d_trials, max_trials, tk, d_orders);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bibd_labels(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                               uint16_t *d_first_rows, uint64_t *d_nodes, const uint64_t *d_orders,
+                               uint64_t max_nodes, unsigned *tk, int num_sms, cudaStream_t s) {
+    if (!n)
+        return cudaSuccess;
+    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
+    int grid = blocks_for((const void *)bibd_label_kernel, num_sms);
+    const int need = (int)((n + TPB - 1) / TPB);
+    if (grid > need)
+        grid = need;
+    bibd_label_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_first_rows, d_nodes, d_orders, max_nodes, tk);
     return cudaGetLastError();
 }
 

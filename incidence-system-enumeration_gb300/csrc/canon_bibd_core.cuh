@@ -567,6 +567,7 @@ struct MaxOut {
     bool timeout;
     uint64_t leaves;    // |Aut|
     uint64_t nodes;
+    unsigned first_rows;  // rows that start a labeling reaching the canonical form
 };
 
 // The arranged column masks for level lv+1 after row `cand` was taken at level
@@ -597,7 +598,10 @@ __device__ __forceinline__ void refine_arranged(Smem sm, unsigned lv, unsigned c
     }
 }
 
-__device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o) {
+// order0: the order in which the rows are tried as the first row (nibble-packed;
+// ID16 = increasing, the plain order).  Only the search order changes with it.
+__device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o,
+                           uint64_t order0 = ID16) {
     const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     const uint64_t cols = (1ull << b) - 1ull;
     const uint64_t sentinel = 1ull << b;
@@ -605,6 +609,7 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
     o.timeout = false;
     o.leaves = 0;
     o.nodes = 0;
+    o.first_rows = 0;
     unsigned valid = n;        // rows 0..valid-1 of the bound (and levels 0..valid) are set
     unsigned used = 0;
     uint64_t perm = 0;
@@ -614,6 +619,7 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
         if (enter) {
             if (i == n) {
                 ++o.leaves;
+                o.first_rows |= 1u << pg(perm, 0);
                 enter = false;
                 --i;
                 used &= ~(1u << pg(perm, i));
@@ -691,6 +697,7 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                 if (state == 1) {
                     o.improved = true;
                     o.leaves = 0;
+                    o.first_rows = 0;
                 }
                 R_(i) = arr;
                 L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
@@ -708,8 +715,17 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
             used &= ~(1u << pg(perm, i));
             continue;
         }
-        const unsigned x = __ffs(rem) - 1;
-        VD_(i) = rem & (rem - 1);
+        unsigned x = __ffs(rem) - 1;
+        if (i == 0 && order0 != ID16) {
+            for (unsigned q = 0; q < n; ++q) {
+                const unsigned c = pg(order0, q);
+                if ((rem >> c) & 1u) {
+                    x = c;
+                    break;
+                }
+            }
+        }
+        VD_(i) = rem & ~(1u << x);
         refine_arranged(sm, i, x, b);
         perm = ps(perm, i, x);
         used |= 1u << x;
@@ -787,7 +803,8 @@ __device__ void check_reference(Smem sm, unsigned n, unsigned b, unsigned flags,
 // short search did not reject.  Verdict, witness, rowToChange and |Aut| are
 // identical either way; `trials` counts the reference-order trials spent.
 __device__ void check_one(Smem sm, const uint64_t *src, unsigned n, unsigned b, unsigned flags,
-                          uint64_t max_trials, uint8_t *aut_dst, unsigned aut_cap, CheckOut &o) {
+                          uint64_t max_trials, uint8_t *aut_dst, unsigned aut_cap, CheckOut &o,
+                          uint64_t order0 = ID16) {
     reset_out(o);
     if (!load_rows(sm, src, n, b, flags)) {
         o.status = ST_BADINPUT;
@@ -808,7 +825,7 @@ __device__ void check_one(Smem sm, const uint64_t *src, unsigned n, unsigned b, 
             const uint64_t quick = o.trials;
             o.status = 0;
             MaxOut mo;
-            max_search(sm, n, b, max_trials, mo);
+            max_search(sm, n, b, max_trials, mo, order0);
             if (mo.timeout) {
                 o.status = ST_TIMEOUT;
             } else if (!decided) {

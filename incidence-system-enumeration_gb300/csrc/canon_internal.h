@@ -54,7 +54,29 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
                                       const uint64_t *d_rows, uint8_t *d_canonical,
                                       uint8_t *d_witness16, uint64_t *d_aut, uint8_t *d_status,
                                       uint64_t *d_trials, uint64_t max_trials, unsigned *d_ticket,
-                                      int num_sms, cudaStream_t s);
+                                      int num_sms, cudaStream_t s, const uint64_t *d_orders = nullptr);
+cudaError_t launch_bibd_labels(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                               uint16_t *d_first_rows, uint64_t *d_nodes, const uint64_t *d_orders,
+                               uint64_t max_nodes, unsigned *d_ticket, int num_sms, cudaStream_t s);
+// order of the rows as first-row candidates by decreasing score (scores: n x v floats)
+cudaError_t launch_order_by_score(uint32_t n, uint32_t v, const float *d_scores, uint64_t *d_orders,
+                                  cudaStream_t s);
+
+namespace mlp {
+// flat FP32 parameter vector: w1[128][64] | b1[128] | w2[128][128] | b2[128] | w3[128] | b3[1]
+constexpr int N_PARAMS = 128 * 64 + 128 + 128 * 128 + 128 + 128 + 1;
+cudaError_t forward(long n, const void *x, const void *w1, const float *b1, const void *w2, const float *b2,
+                    const void *w3, const float *b3, float *y, void *h1, void *h2, int num_sms, cudaStream_t s);
+cudaError_t backward(long n, const float *logit, const float *label, const void *h1, const void *h2,
+                     const void *w3, const void *w2t, float *dy, float *dh2, float *dh1, float *loss,
+                     int num_sms, cudaStream_t s);
+cudaError_t weight_grads(long n, const float *dh1, const float *dh2, const float *dy, const void *x,
+                         const void *h1, const void *h2, float *grad, int num_sms, cudaStream_t s);
+cudaError_t adam(int count, float *p, const float *grad, float *m, float *v, float lr, int step, void *w1,
+                 void *w2, void *w2t, void *w3, cudaStream_t s);
+cudaError_t features(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *rows, void *feat,
+                     cudaStream_t s);
+}  // namespace mlp
 cudaError_t launch_bibd_canonize(uint32_t n, uint32_t v, uint32_t b, uint64_t *d_rows,
                                  uint64_t *d_aut, uint8_t *d_status, uint32_t stride_items,
                                  uint32_t first_item, uint64_t max_trials, unsigned *d_ticket,

@@ -1,0 +1,460 @@
+// canon_mlp.cu -- the learned search order: a BF16 MLP 64 -> 128 -> 128 -> 1 that
+// scores every row of a matrix as the first row of the canonical labeling.
+//
+// Inference and the forward pass of training run on the tensor cores
+// (mma.sync m16n8k16, BF16 operands, FP32 accumulation), one warp per 16 rows;
+// the hidden activations stay in registers and feed the next layer as A
+// fragments.  The backward pass propagates through the same layers (the hidden
+// gradient dH1 = dH2 * W2 also on the tensor cores), the weight gradients are
+// tiled FP32 reductions over the batch, and Adam keeps FP32 master weights from
+// which the BF16 copies are refreshed after every step.  No counterpart in the
+// reference.
+#include <cuda_bf16.h>
+
+#include "canon_internal.h"
+
+namespace canon {
+
+namespace {
+
+constexpr int IN = 64, HID = 128;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat16 l = __float2bfloat16_rn(lo), h = __float2bfloat16_rn(hi);
+    return (uint32_t)__bfloat16_as_ushort(l) | ((uint32_t)__bfloat16_as_ushort(h) << 16);
+}
+
+__device__ __forceinline__ float bf_lo(uint32_t v) { return __bfloat162float(__ushort_as_bfloat16((unsigned short)(v & 0xFFFFu))); }
+__device__ __forceinline__ float bf_hi(uint32_t v) { return __bfloat162float(__ushort_as_bfloat16((unsigned short)(v >> 16))); }
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// two consecutive bf16 of a row-major matrix as one 32-bit word (0 outside the rows)
+__device__ __forceinline__ uint32_t ld2(const __nv_bfloat16 *m, long rows, long row, int ld, int col) {
+    if (row >= rows)
+        return 0u;
+    return *reinterpret_cast<const uint32_t *>(m + row * ld + col);
+}
+
+struct MlpDev {
+    const __nv_bfloat16 *w1;   // [128][64]
+    const float *b1;           // [128]
+    const __nv_bfloat16 *w2;   // [128][128]
+    const float *b2;           // [128]
+    const __nv_bfloat16 *w3;   // [128]
+    const float *b3;           // [1]
+};
+
+// Forward pass of 16 rows per warp.  Writes logits; when h1/h2 are given also the
+// (BF16, post-ReLU) hidden activations for the backward pass.
+__global__ void mlp_forward_kernel(long n, const __nv_bfloat16 *__restrict__ x, MlpDev w, float *__restrict__ y,
+                                   __nv_bfloat16 *__restrict__ h1out, __nv_bfloat16 *__restrict__ h2out) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, tg = lane & 3;
+    const long tiles = (n + 15) / 16;
+    for (long tile = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < tiles;
+         tile += (long)gridDim.x * (blockDim.x >> 5)) {
+        const long r0 = tile * 16;
+        uint32_t a[4][4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            a[t][0] = ld2(x, n, r0 + g, IN, 16 * t + 2 * tg);
+            a[t][1] = ld2(x, n, r0 + g + 8, IN, 16 * t + 2 * tg);
+            a[t][2] = ld2(x, n, r0 + g, IN, 16 * t + 8 + 2 * tg);
+            a[t][3] = ld2(x, n, r0 + g + 8, IN, 16 * t + 8 + 2 * tg);
+        }
+        // layer 1: 16 x 128 = relu(X W1^T + b1), kept as packed BF16 A fragments of layer 2
+        uint32_t h1[16][2];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const uint32_t b0 = ld2(w.w1, HID, 8 * j + g, IN, 16 * t + 2 * tg);
+                const uint32_t b1 = ld2(w.w1, HID, 8 * j + g, IN, 16 * t + 8 + 2 * tg);
+                mma_bf16(acc, a[t], b0, b1);
+            }
+            const float bb0 = w.b1[8 * j + 2 * tg], bb1 = w.b1[8 * j + 2 * tg + 1];
+            h1[j][0] = pack_bf16(fmaxf(acc[0] + bb0, 0.f), fmaxf(acc[1] + bb1, 0.f));
+            h1[j][1] = pack_bf16(fmaxf(acc[2] + bb0, 0.f), fmaxf(acc[3] + bb1, 0.f));
+            if (h1out) {
+                if (r0 + g < n)
+                    *reinterpret_cast<uint32_t *>(h1out + (r0 + g) * HID + 8 * j + 2 * tg) = h1[j][0];
+                if (r0 + g + 8 < n)
+                    *reinterpret_cast<uint32_t *>(h1out + (r0 + g + 8) * HID + 8 * j + 2 * tg) = h1[j][1];
+            }
+        }
+        // layer 2 and the output layer, one 8-wide tile at a time
+        float part0 = 0.f, part1 = 0.f;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const uint32_t af[4] = {h1[2 * t][0], h1[2 * t][1], h1[2 * t + 1][0], h1[2 * t + 1][1]};
+                const uint32_t b0 = ld2(w.w2, HID, 8 * j + g, HID, 16 * t + 2 * tg);
+                const uint32_t b1 = ld2(w.w2, HID, 8 * j + g, HID, 16 * t + 8 + 2 * tg);
+                mma_bf16(acc, af, b0, b1);
+            }
+            const float bb0 = w.b2[8 * j + 2 * tg], bb1 = w.b2[8 * j + 2 * tg + 1];
+            const uint32_t p0 = pack_bf16(fmaxf(acc[0] + bb0, 0.f), fmaxf(acc[1] + bb1, 0.f));
+            const uint32_t p1 = pack_bf16(fmaxf(acc[2] + bb0, 0.f), fmaxf(acc[3] + bb1, 0.f));
+            if (h2out) {
+                if (r0 + g < n)
+                    *reinterpret_cast<uint32_t *>(h2out + (r0 + g) * HID + 8 * j + 2 * tg) = p0;
+                if (r0 + g + 8 < n)
+                    *reinterpret_cast<uint32_t *>(h2out + (r0 + g + 8) * HID + 8 * j + 2 * tg) = p1;
+            }
+            const float w30 = __bfloat162float(w.w3[8 * j + 2 * tg]), w31 = __bfloat162float(w.w3[8 * j + 2 * tg + 1]);
+            part0 += bf_lo(p0) * w30 + bf_hi(p0) * w31;
+            part1 += bf_lo(p1) * w30 + bf_hi(p1) * w31;
+        }
+        part0 += __shfl_xor_sync(0xFFFFFFFFu, part0, 1);
+        part0 += __shfl_xor_sync(0xFFFFFFFFu, part0, 2);
+        part1 += __shfl_xor_sync(0xFFFFFFFFu, part1, 1);
+        part1 += __shfl_xor_sync(0xFFFFFFFFu, part1, 2);
+        if (tg == 0) {
+            if (r0 + g < n)
+                y[r0 + g] = part0 + w.b3[0];
+            if (r0 + g + 8 < n)
+                y[r0 + g + 8] = part1 + w.b3[0];
+        }
+    }
+}
+
+// Backward of the binary cross-entropy on the logits: dy, dH2 = dy w3 [H2 > 0]
+// and dH1 = (dH2 W2) [H1 > 0] (tensor cores; w2t is W2 transposed, [in][out]).
+__global__ void mlp_backward_kernel(long n, const float *__restrict__ logit, const float *__restrict__ label,
+                                    const __nv_bfloat16 *__restrict__ h1, const __nv_bfloat16 *__restrict__ h2,
+                                    const __nv_bfloat16 *__restrict__ w3, const __nv_bfloat16 *__restrict__ w2t,
+                                    float *__restrict__ dy, float *__restrict__ dh2, float *__restrict__ dh1,
+                                    float *__restrict__ loss_sum) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, tg = lane & 3;
+    const long tiles = (n + 15) / 16;
+    const float inv_n = 1.f / (float)n;
+    for (long tile = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < tiles;
+         tile += (long)gridDim.x * (blockDim.x >> 5)) {
+        const long r0 = tile * 16;
+        const long ra = r0 + g, rb = r0 + g + 8;
+        float dya = 0.f, dyb = 0.f;
+        if (ra < n) {
+            const float z = logit[ra], t = label[ra];
+            dya = (1.f / (1.f + __expf(-z)) - t) * inv_n;
+        }
+        if (rb < n) {
+            const float z = logit[rb], t = label[rb];
+            dyb = (1.f / (1.f + __expf(-z)) - t) * inv_n;
+        }
+        if (tg == 0) {
+            // loss (sum of BCE terms), one lane per row pair
+            float l = 0.f;
+            if (ra < n) {
+                const float z = logit[ra], t = label[ra];
+                l += fmaxf(z, 0.f) - z * t + log1pf(__expf(-fabsf(z)));
+            }
+            if (rb < n) {
+                const float z = logit[rb], t = label[rb];
+                l += fmaxf(z, 0.f) - z * t + log1pf(__expf(-fabsf(z)));
+            }
+            atomicAdd(loss_sum, l);
+        }
+        if (tg == 0) {
+            if (ra < n)
+                dy[ra] = dya;
+            if (rb < n)
+                dy[rb] = dyb;
+        }
+        // dH2 in the A-fragment layout (k = layer-2 outputs)
+        uint32_t a2[8][4];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int c = 8 * j + 2 * tg;
+            const float w30 = __bfloat162float(w3[c]), w31 = __bfloat162float(w3[c + 1]);
+            const uint32_t ha = ld2(h2, n, ra, HID, c), hb = ld2(h2, n, rb, HID, c);
+            const float g0 = bf_lo(ha) > 0.f ? dya * w30 : 0.f, g1 = bf_hi(ha) > 0.f ? dya * w31 : 0.f;
+            const float g2 = bf_lo(hb) > 0.f ? dyb * w30 : 0.f, g3 = bf_hi(hb) > 0.f ? dyb * w31 : 0.f;
+            if (ra < n) {
+                dh2[ra * HID + c] = g0;
+                dh2[ra * HID + c + 1] = g1;
+            }
+            if (rb < n) {
+                dh2[rb * HID + c] = g2;
+                dh2[rb * HID + c + 1] = g3;
+            }
+            const int t = j >> 1;
+            if (j & 1) {
+                a2[t][2] = pack_bf16(g0, g1);
+                a2[t][3] = pack_bf16(g2, g3);
+            } else {
+                a2[t][0] = pack_bf16(g0, g1);
+                a2[t][1] = pack_bf16(g2, g3);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const uint32_t b0 = ld2(w2t, HID, 8 * j + g, HID, 16 * t + 2 * tg);
+                const uint32_t b1 = ld2(w2t, HID, 8 * j + g, HID, 16 * t + 8 + 2 * tg);
+                mma_bf16(acc, a2[t], b0, b1);
+            }
+            const int c = 8 * j + 2 * tg;
+            const uint32_t ha = ld2(h1, n, ra, HID, c), hb = ld2(h1, n, rb, HID, c);
+            if (ra < n) {
+                dh1[ra * HID + c] = bf_lo(ha) > 0.f ? acc[0] : 0.f;
+                dh1[ra * HID + c + 1] = bf_hi(ha) > 0.f ? acc[1] : 0.f;
+            }
+            if (rb < n) {
+                dh1[rb * HID + c] = bf_lo(hb) > 0.f ? acc[2] : 0.f;
+                dh1[rb * HID + c + 1] = bf_hi(hb) > 0.f ? acc[3] : 0.f;
+            }
+        }
+    }
+}
+
+// grad_w[o][i] += sum_rows dh[row][o] * act[row][i] (act BF16), grad_b[o] += sum dh[row][o]:
+// a 32 x 32 output tile per block, a slice of the rows per blockIdx.z.
+__global__ void weight_grad_kernel(long n, int out_dim, int in_dim, const float *__restrict__ dh,
+                                   const __nv_bfloat16 *__restrict__ act, float *__restrict__ gw,
+                                   float *__restrict__ gb) {
+    __shared__ float sd[32][33];
+    __shared__ float sa[32][33];
+    const int o0 = blockIdx.y * 32, i0 = blockIdx.x * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    float accb = 0.f;
+    const long per = (n + gridDim.z - 1) / gridDim.z;
+    const long lo = (long)blockIdx.z * per, hi = (lo + per < n) ? lo + per : n;
+    for (long r = lo; r < hi; r += 32) {
+        for (int q = ty; q < 32; q += 8) {
+            const long row = r + q;
+            sd[q][tx] = (row < hi && o0 + tx < out_dim) ? dh[row * out_dim + o0 + tx] : 0.f;
+            sa[q][tx] = (row < hi && i0 + tx < in_dim) ? __bfloat162float(act[row * in_dim + i0 + tx]) : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int q = 0; q < 32; ++q) {
+            const float av = sa[q][tx];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                acc[u] += sd[q][ty + 8 * u] * av;
+            if (blockIdx.x == 0 && ty == 0)
+                accb += sd[q][tx];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int o = o0 + ty + 8 * u, i = i0 + tx;
+        if (o < out_dim && i < in_dim)
+            atomicAdd(&gw[o * in_dim + i], acc[u]);
+    }
+    if (blockIdx.x == 0 && ty == 0 && o0 + tx < out_dim)
+        atomicAdd(&gb[o0 + tx], accb);
+}
+
+// output layer: grad_w3[i] += sum dy*h2[row][i], grad_b3 += sum dy
+__global__ void out_grad_kernel(long n, const float *__restrict__ dy, const __nv_bfloat16 *__restrict__ h2,
+                                float *__restrict__ gw3, float *__restrict__ gb3) {
+    const int i = threadIdx.x;   // 128 threads
+    float acc = 0.f, accb = 0.f;
+    for (long r = blockIdx.x; r < n; r += gridDim.x) {
+        const float d = dy[r];
+        acc += d * __bfloat162float(h2[r * HID + i]);
+        if (i == 0)
+            accb += d;
+    }
+    atomicAdd(&gw3[i], acc);
+    if (i == 0)
+        atomicAdd(gb3, accb);
+}
+
+// Adam over the flat FP32 parameter vector; refreshes the BF16 copies (and W2^T).
+__global__ void adam_kernel(int count, float *__restrict__ p, const float *__restrict__ grad, float *__restrict__ m,
+                            float *__restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2,
+                            __nv_bfloat16 *__restrict__ w1, __nv_bfloat16 *__restrict__ w2,
+                            __nv_bfloat16 *__restrict__ w2t, __nv_bfloat16 *__restrict__ w3) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count)
+        return;
+    const float gk = grad[k];
+    const float mk = b1 * m[k] + (1.f - b1) * gk;
+    const float vk = b2 * v[k] + (1.f - b2) * gk * gk;
+    m[k] = mk;
+    v[k] = vk;
+    const float pk = p[k] - lr * (mk / c1) / (sqrtf(vk / c2) + eps);
+    p[k] = pk;
+    // layout of the flat vector: w1 | b1 | w2 | b2 | w3 | b3
+    const int W1 = HID * IN, B1 = W1 + HID, W2 = B1 + HID * HID, B2 = W2 + HID, W3 = B2 + HID;
+    if (k < W1) {
+        w1[k] = __float2bfloat16_rn(pk);
+    } else if (k >= B1 && k < W2) {
+        const int q = k - B1;
+        w2[q] = __float2bfloat16_rn(pk);
+        w2t[(q % HID) * HID + q / HID] = __float2bfloat16_rn(pk);
+    } else if (k >= B2 && k < W3) {
+        w3[k - B2] = __float2bfloat16_rn(pk);
+    }
+}
+
+// ---- features and labels -----------------------------------------------------
+
+// 64 features of every row of a normalised incidence matrix as the first row:
+// [0,16) histogram of |R_x & R_y| over the other rows; [16,32) histogram over the
+// other rows y of the number of rows z meeting R_x & R_y; [32,48) histogram of the
+// column weights of the columns of R_x; [48,64) row index one-hot, fill depth
+// n/16, shape b/64, |R_x|/b.  Scaled to [0, 1].
+__global__ void features_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t nrows, uint32_t flags,
+                                const uint64_t *__restrict__ rows, __nv_bfloat16 *__restrict__ feat) {
+    const uint32_t it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= n_items)
+        return;
+    uint64_t R[VMAX];
+    for (uint32_t r = 0; r < VMAX; ++r)
+        R[r] = (r < nrows) ? rows[(size_t)it * v + r] : 0ull;
+    (void)flags;
+    unsigned colw[64];
+    for (uint32_t c = 0; c < b; ++c) {
+        unsigned w = 0;
+        for (uint32_t r = 0; r < nrows; ++r)
+            w += (unsigned)((R[r] >> c) & 1u);
+        colw[c] = w;
+    }
+    for (uint32_t x = 0; x < nrows; ++x) {
+        float f[64];
+        for (int q = 0; q < 64; ++q)
+            f[q] = 0.f;
+        const float inv = 1.f / (float)(nrows > 1 ? nrows - 1 : 1);
+        for (uint32_t y = 0; y < nrows; ++y) {
+            if (y == x)
+                continue;
+            const uint64_t xy = R[x] & R[y];
+            f[min(__popcll(xy), 15)] += inv;
+            unsigned meet = 0;
+            for (uint32_t z = 0; z < nrows; ++z)
+                if (z != x && z != y && (xy & R[z]))
+                    ++meet;
+            f[16 + min(meet, 15u)] += inv;
+        }
+        const float invc = 1.f / (float)(__popcll(R[x]) ? __popcll(R[x]) : 1);
+        for (uint32_t c = 0; c < b; ++c)
+            if ((R[x] >> c) & 1u)
+                f[32 + min(colw[c], 15u)] += invc;
+        f[48 + (x & 15u)] = 1.f;
+        __nv_bfloat16 *dst = feat + ((size_t)it * v + x) * 64;
+        for (int q = 0; q < 48; ++q)
+            dst[q] = __float2bfloat16_rn(f[q]);
+        for (int q = 48; q < 64; ++q)
+            dst[q] = __float2bfloat16_rn(f[q]);
+        dst[63] = __float2bfloat16_rn((float)nrows / 16.f);
+        dst[62] = __float2bfloat16_rn((float)b / 64.f);
+        dst[61] = __float2bfloat16_rn((float)__popcll(R[x]) / (float)b);
+    }
+}
+
+// rows of every matrix sorted by decreasing score (ties: lower row first), nibble-packed
+__global__ void order_kernel(uint32_t n, uint32_t v, const float *__restrict__ scores, uint64_t *__restrict__ orders) {
+    const uint32_t it = blockIdx.x * blockDim.x + threadIdx.x;
+    if (it >= n)
+        return;
+    const float *sc = scores + (size_t)it * v;
+    uint64_t ord = 0xFEDCBA9876543210ull;
+    for (uint32_t x = 0; x < v; ++x) {
+        unsigned rank = 0;
+        for (uint32_t y = 0; y < v; ++y)
+            rank += (sc[y] > sc[x]) || (sc[y] == sc[x] && y < x);
+        ord = (ord & ~(15ull << (4 * rank))) | ((uint64_t)x << (4 * rank));
+    }
+    orders[it] = ord;
+}
+
+}  // namespace
+
+cudaError_t launch_order_by_score(uint32_t n, uint32_t v, const float *d_scores, uint64_t *d_orders, cudaStream_t s) {
+    if (!n)
+        return cudaSuccess;
+    order_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, v, d_scores, d_orders);
+    return cudaGetLastError();
+}
+
+namespace mlp {
+
+cudaError_t forward(long n, const void *x, const void *w1, const float *b1, const void *w2, const float *b2,
+                    const void *w3, const float *b3, float *y, void *h1, void *h2, int num_sms, cudaStream_t s) {
+    MlpDev w{(const __nv_bfloat16 *)w1, b1, (const __nv_bfloat16 *)w2, b2, (const __nv_bfloat16 *)w3, b3};
+    const long tiles = (n + 15) / 16;
+    long grid = (tiles + 3) / 4;
+    if (grid > 32L * num_sms)
+        grid = 32L * num_sms;
+    if (grid < 1)
+        grid = 1;
+    mlp_forward_kernel<<<(int)grid, 128, 0, s>>>(n, (const __nv_bfloat16 *)x, w, y, (__nv_bfloat16 *)h1,
+                                                  (__nv_bfloat16 *)h2);
+    return cudaGetLastError();
+}
+
+cudaError_t backward(long n, const float *logit, const float *label, const void *h1, const void *h2, const void *w3,
+                     const void *w2t, float *dy, float *dh2, float *dh1, float *loss, int num_sms, cudaStream_t s) {
+    const long tiles = (n + 15) / 16;
+    long grid = (tiles + 3) / 4;
+    if (grid > 32L * num_sms)
+        grid = 32L * num_sms;
+    if (grid < 1)
+        grid = 1;
+    mlp_backward_kernel<<<(int)grid, 128, 0, s>>>(n, logit, label, (const __nv_bfloat16 *)h1,
+                                                   (const __nv_bfloat16 *)h2, (const __nv_bfloat16 *)w3,
+                                                   (const __nv_bfloat16 *)w2t, dy, dh2, dh1, loss);
+    return cudaGetLastError();
+}
+
+cudaError_t weight_grads(long n, const float *dh1, const float *dh2, const float *dy, const void *x, const void *h1,
+                         const void *h2, float *grad, int num_sms, cudaStream_t s) {
+    const int W1 = HID * IN, B1 = W1 + HID, W2 = B1 + HID * HID, B2 = W2 + HID, W3 = B2 + HID, B3 = W3 + HID;
+    int zs = (int)((n + 2047) / 2048);
+    if (zs > 4 * num_sms)
+        zs = 4 * num_sms;
+    if (zs < 1)
+        zs = 1;
+    weight_grad_kernel<<<dim3(IN / 32, HID / 32, zs), 256, 0, s>>>(n, HID, IN, dh1, (const __nv_bfloat16 *)x,
+                                                                   grad, grad + W1);
+    weight_grad_kernel<<<dim3(HID / 32, HID / 32, zs), 256, 0, s>>>(n, HID, HID, dh2, (const __nv_bfloat16 *)h1,
+                                                                    grad + B1, grad + W2);
+    int og = (int)((n + 255) / 256);
+    if (og > 8 * num_sms)
+        og = 8 * num_sms;
+    if (og < 1)
+        og = 1;
+    out_grad_kernel<<<og, HID, 0, s>>>(n, dy, (const __nv_bfloat16 *)h2, grad + B2, grad + W3);
+    (void)B3;
+    return cudaGetLastError();
+}
+
+cudaError_t adam(int count, float *p, const float *grad, float *m, float *v, float lr, int step, void *w1, void *w2,
+                 void *w2t, void *w3, cudaStream_t s) {
+    const float b1 = 0.9f, b2 = 0.999f;
+    float c1 = 1.f, c2 = 1.f;
+    for (int i = 0; i < step; ++i) {
+        c1 *= b1;
+        c2 *= b2;
+    }
+    adam_kernel<<<(count + 255) / 256, 256, 0, s>>>(count, p, grad, m, v, lr, b1, b2, 1e-8f, 1.f - c1, 1.f - c2,
+                                                    (__nv_bfloat16 *)w1, (__nv_bfloat16 *)w2, (__nv_bfloat16 *)w2t,
+                                                    (__nv_bfloat16 *)w3);
+    return cudaGetLastError();
+}
+
+cudaError_t features(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *rows, void *feat,
+                     cudaStream_t s) {
+    features_kernel<<<(n + 127) / 128, 128, 0, s>>>(n, v, b, v, flags, rows, (__nv_bfloat16 *)feat);
+    return cudaGetLastError();
+}
+
+}  // namespace mlp
+
+}  // namespace canon

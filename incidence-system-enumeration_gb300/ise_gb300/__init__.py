@@ -54,8 +54,10 @@ HEADER_SYMBOLS = [
     "canon_sync", "canon_set_ordering", "canon_canonize_bibd", "canon_check_bibd_device",
     "canon_generate_sts_device", "canon_device_alloc", "canon_device_free", "canon_memcpy_d2h",
     "canon_memcpy_h2d", "canon_last_kernel_ms", "canon_kernel_launches", "canon_stream_sync",
-    "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys",
+    "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys", "canon_mlp_features",
+    "canon_label_first_rows", "canon_mlp_forward", "canon_mlp_grad", "canon_mlp_train",
 ]
+MLP_PARAMS = 128 * 64 + 128 + 128 * 128 + 128 + 128 + 1
 
 
 class CanonError(RuntimeError):
@@ -98,6 +100,13 @@ class EnumStats(ctypes.Structure):
 
 DESIGN_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint32,
                              ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64)
+
+
+class MlpWeights(ctypes.Structure):
+    _fields_ = [("in_dim", ctypes.c_uint32), ("hidden", ctypes.c_uint32),
+                ("w1", ctypes.POINTER(ctypes.c_uint16)), ("w2", ctypes.POINTER(ctypes.c_uint16)),
+                ("w3", ctypes.POINTER(ctypes.c_uint16)), ("b1", ctypes.POINTER(ctypes.c_float)),
+                ("b2", ctypes.POINTER(ctypes.c_float)), ("b3", ctypes.POINTER(ctypes.c_float))]
 
 
 class Results(ctypes.Structure):
@@ -155,12 +164,41 @@ def load_library(path=LIB_PATH):
     L.canon_check_bibd_noalloc.argtypes = [u32, u32, u32, u32, vp, vp, ctypes.POINTER(DeviceOutputs), u64, vp]
     L.canon_enumerate_bibd.argtypes = [vp, u32, u32, u32, u32, u32, DESIGN_CB, vp, ctypes.POINTER(EnumStats)]
     L.canon_enumerate_ksys.argtypes = [vp, u32, DESIGN_CB, vp, ctypes.POINTER(EnumStats)]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.canon_mlp_features.argtypes = [vp, u32, u32, u32, vp, vp]
+    L.canon_label_first_rows.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp, vp]
+    L.canon_mlp_forward.argtypes = [vp, u64, vp, fp, vp]
+    L.canon_mlp_grad.argtypes = [vp, u64, vp, vp, fp, fp, fp]
+    L.canon_mlp_train.argtypes = [vp, u64, vp, vp, u32, u32, ctypes.c_float, fp, fp]
+    L.canon_set_ordering.argtypes = [vp, ctypes.POINTER(MlpWeights)]
     _lib = L
     return L
 
 
 def _ptr(a, ct):
     return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def to_bf16_bits(a):
+    """FP32 -> BF16 bit patterns (round to nearest even)."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = u + 0x7FFF + ((u >> 16) & 1)
+    return (u >> 16).astype(np.uint16)
+
+
+def bf16_round(a):
+    """FP32 values rounded to BF16 precision (as FP32)."""
+    return (to_bf16_bits(a).astype(np.uint32) << 16).view(np.float32)
+
+
+def init_mlp_params(seed):
+    """He-initialised flat parameter vector of the 64-128-128-1 network."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros(MLP_PARAMS, np.float32)
+    p[:8192] = rng.normal(0, np.sqrt(2 / 64), 8192)
+    p[8320:24704] = rng.normal(0, np.sqrt(2 / 128), 16384)
+    p[24832:24960] = rng.normal(0, np.sqrt(1 / 128), 128)
+    return p
 
 
 def pack_rows(M):
@@ -313,6 +351,48 @@ class Context:
         st = EnumStats()
         self._check(self.lib.canon_enumerate_ksys(self.h, np_, c, None, ctypes.byref(st)))
         return found, st
+
+    # ---- learned search order ----
+    def mlp_features(self, n, v, b, d_rows, d_feat):
+        self._check(self.lib.canon_mlp_features(self.h, n, v, b, d_rows, d_feat))
+
+    def label_first_rows(self, n, v, b, flags, d_rows, d_first_rows, d_nodes=None, d_orders=None):
+        self._check(self.lib.canon_label_first_rows(self.h, n, v, b, flags, d_rows, d_first_rows, d_nodes,
+                                                    d_orders))
+
+    def mlp_forward(self, n, d_x, params, d_logits):
+        params = np.ascontiguousarray(params, np.float32)
+        self._check(self.lib.canon_mlp_forward(self.h, n, d_x, _ptr(params, ctypes.c_float), d_logits))
+
+    def mlp_grad(self, n, d_x, d_labels, params):
+        params = np.ascontiguousarray(params, np.float32)
+        grad = np.zeros(MLP_PARAMS, np.float32)
+        loss = ctypes.c_float()
+        self._check(self.lib.canon_mlp_grad(self.h, n, d_x, d_labels, _ptr(params, ctypes.c_float),
+                                            _ptr(grad, ctypes.c_float), ctypes.byref(loss)))
+        return grad, loss.value
+
+    def mlp_train(self, n, d_x, d_labels, params, epochs, batch, lr):
+        params = np.array(params, np.float32, copy=True)
+        losses = np.zeros(epochs, np.float32)
+        self._check(self.lib.canon_mlp_train(self.h, n, d_x, d_labels, epochs, batch, lr,
+                                             _ptr(params, ctypes.c_float), _ptr(losses, ctypes.c_float)))
+        return params, losses
+
+    def set_ordering(self, params):
+        """Install (or with None remove) the learned first-row order from flat FP32 params."""
+        if params is None:
+            self._check(self.lib.canon_set_ordering(self.h, None))
+            return
+        p = np.asarray(params, np.float32)
+        bf = lambda a: (to_bf16_bits(a))
+        w1, b1 = bf(p[:8192]), p[8192:8320].copy()
+        w2, b2 = bf(p[8320:24704]), p[24704:24832].copy()
+        w3, b3 = bf(p[24832:24960]), p[24960:24961].copy()
+        self._keep = (w1, b1, w2, b2, w3, b3)
+        w = MlpWeights(64, 128, _ptr(w1, ctypes.c_uint16), _ptr(w2, ctypes.c_uint16), _ptr(w3, ctypes.c_uint16),
+                       _ptr(b1, ctypes.c_float), _ptr(b2, ctypes.c_float), _ptr(b3, ctypes.c_float))
+        self._check(self.lib.canon_set_ordering(self.h, ctypes.byref(w)))
 
     def stream_sync(self):
         self._check(self.lib.canon_stream_sync(self.h))

@@ -217,6 +217,33 @@ int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uin
  * TripleSys.cpp:80-775, check at checkCurrentResult.cpp:91).  np even, <= 12. */
 int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *user, canon_enum_stats *stats);
 
+/* ---- the learned search order (no counterpart in the reference) ----
+ * A BF16 MLP 64 -> 128 -> 128 -> 1 (ReLU) scores each row of a matrix as the first
+ * row of the labeling that reaches its canonical form.  With weights installed by
+ * canon_set_ordering, canon_check_bibd_device tries the rows at the first level of
+ * the lex-max search in decreasing score; verdicts, |Aut| and witnesses do not
+ * change, only the search order.  Parameters travel as one flat FP32 vector of
+ * CANON_MLP_PARAMS floats: w1[128][64] | b1[128] | w2[128][128] | b2[128] | w3[128] | b3. */
+#define CANON_MLP_PARAMS (128 * 64 + 128 + 128 * 128 + 128 + 128 + 1)
+/* 64 BF16 features of every row of n device-resident matrices (d_feat: n*v*64 BF16). */
+int canon_mlp_features(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, const uint64_t *d_rows, void *d_feat);
+/* Training labels from the exact search: for every matrix the rows that start a
+ * labeling reaching its canonical form (bit x of d_first_rows[i]), and the number
+ * of lex-max nodes visited (d_nodes, optional) in the order given by d_orders
+ * (optional, n nibble-packed orders; NULL = plain). */
+int canon_label_first_rows(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                           uint16_t *d_first_rows, uint64_t *d_nodes, const uint64_t *d_orders);
+/* Logits of n feature rows (device) under `params` (host, CANON_MLP_PARAMS floats). */
+int canon_mlp_forward(canon_ctx *ctx, uint64_t n, const void *d_x, const float *params, float *d_logits);
+/* Gradient of the mean binary cross-entropy over n rows (labels 0/1, device) with
+ * respect to `params`, into grad (host, CANON_MLP_PARAMS floats); loss (host) = the mean. */
+int canon_mlp_grad(canon_ctx *ctx, uint64_t n, const void *d_x, const float *d_labels, const float *params,
+                   float *grad, float *loss);
+/* Adam training (lr, batches of `batch` rows, `epochs` passes) of params in place
+ * (host); epoch_loss (host, optional) gets the mean loss of every epoch. */
+int canon_mlp_train(canon_ctx *ctx, uint64_t n, const void *d_x, const float *d_labels, uint32_t epochs,
+                    uint32_t batch, float lr, float *params, float *epoch_loss);
+
 /* ---- checking without allocating ---- */
 /* Device output arrays of canon_check_bibd_noalloc (one entry per matrix, same
  * meaning as the canon_results fields).  auts may be NULL unless CANON_SAVE_AUTS

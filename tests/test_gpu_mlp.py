@@ -1,0 +1,155 @@
+"""The learned search order: tensor-core MLP forward, hand-written backward and
+Adam against a NumPy FP64 reference of the same BF16 arithmetic, and the order's
+only effect being the search order."""
+import numpy as np
+import pytest
+
+import ise_gb300 as G
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def ref_forward(p, X):
+    """FP64 reference of the kernels' arithmetic: BF16 inputs, weights and hidden
+    activations, FP32-exact sums."""
+    Xb = G.bf16_round(X).astype(np.float64)
+    W1 = G.bf16_round(p[:8192]).reshape(128, 64).astype(np.float64)
+    b1 = p[8192:8320].astype(np.float64)
+    W2 = G.bf16_round(p[8320:24704]).reshape(128, 128).astype(np.float64)
+    b2 = p[24704:24832].astype(np.float64)
+    w3 = G.bf16_round(p[24832:24960]).astype(np.float64)
+    b3 = float(p[24960])
+    h1 = G.bf16_round(np.maximum(Xb @ W1.T + b1, 0).astype(np.float32)).astype(np.float64)
+    h2 = G.bf16_round(np.maximum(h1 @ W2.T + b2, 0).astype(np.float32)).astype(np.float64)
+    y = h2 @ w3 + b3
+    return Xb, W2, w3, h1, h2, y
+
+
+def ref_grad(p, X, t):
+    Xb, W2, w3, h1, h2, y = ref_forward(p, X)
+    n = len(t)
+    dy = (1 / (1 + np.exp(-y)) - t) / n
+    dh2 = np.outer(dy, w3) * (h2 > 0)
+    dh2b = G.bf16_round(dh2.astype(np.float32)).astype(np.float64)
+    dh1 = (dh2b @ W2) * (h1 > 0)
+    g = np.zeros(G.MLP_PARAMS)
+    g[:8192] = (dh1.T @ Xb).ravel()
+    g[8192:8320] = dh1.sum(0)
+    g[8320:24704] = (dh2.T @ h1).ravel()
+    g[24704:24832] = dh2.sum(0)
+    g[24832:24960] = dy @ h2
+    g[24960] = dy.sum()
+    loss = np.mean(np.maximum(y, 0) - y * t + np.log1p(np.exp(-np.abs(y))))
+    return g, loss, y
+
+
+def to_device(ctx, a):
+    d = ctx.alloc(a.nbytes)
+    ctx.h2d(d, a)
+    return d
+
+
+@pytest.fixture(scope="module")
+def data():
+    rng = np.random.default_rng(3)
+    n = 1000
+    X = rng.random((n, 64)).astype(np.float32)
+    t = (X[:, 0] + 0.5 * X[:, 5] > 0.8).astype(np.float32)
+    return X, t
+
+
+def test_forward_matches_reference(ctx, data):
+    X, _ = data
+    p = G.init_mlp_params(11)
+    p[8192:8320] = 0.05
+    dx = to_device(ctx, G.to_bf16_bits(X))
+    dy = ctx.alloc(4 * len(X))
+    try:
+        ctx.mlp_forward(len(X), dx, p, dy)
+        y = ctx.d2h(np.zeros(len(X), np.float32), dy)
+    finally:
+        ctx.free(dx)
+        ctx.free(dy)
+    _, _, _, _, _, yr = ref_forward(p, X)
+    assert np.allclose(y, yr, rtol=2e-2, atol=2e-2), np.abs(y - yr).max()
+
+
+def test_gradients_match_reference(ctx, data):
+    X, t = data
+    p = G.init_mlp_params(12)
+    dx = to_device(ctx, G.to_bf16_bits(X))
+    dt = to_device(ctx, t)
+    try:
+        g, loss = ctx.mlp_grad(len(X), dx, dt, p)
+    finally:
+        ctx.free(dx)
+        ctx.free(dt)
+    gr, lr, _ = ref_grad(p, X, t)
+    assert abs(loss - lr) < 1e-2 * max(1.0, abs(lr))
+    # tolerance: BF16 hidden activations and the BF16 dH2 operand of the dH1 product
+    for lo, hi in [(0, 8192), (8192, 8320), (8320, 24704), (24704, 24832), (24832, 24960), (24960, 24961)]:
+        a, b = g[lo:hi], gr[lo:hi]
+        assert np.linalg.norm(a - b) <= 3e-2 * np.linalg.norm(b) + 1e-6, (lo, np.linalg.norm(a - b),
+                                                                          np.linalg.norm(b))
+
+
+def test_training_lowers_the_loss(ctx, data):
+    X, t = data
+    p = G.init_mlp_params(13)
+    dx = to_device(ctx, G.to_bf16_bits(X))
+    dt = to_device(ctx, t)
+    try:
+        p2, losses = ctx.mlp_train(len(X), dx, dt, p, epochs=60, batch=256, lr=3e-3)
+        dy = ctx.alloc(4 * len(X))
+        ctx.mlp_forward(len(X), dx, p2, dy)
+        y = ctx.d2h(np.zeros(len(X), np.float32), dy)
+        ctx.free(dy)
+    finally:
+        ctx.free(dx)
+        ctx.free(dt)
+    assert losses[-1] < 0.6 * losses[0]
+    assert ((y > 0) == (t > 0.5)).mean() > 0.9
+
+
+def test_learned_order_changes_only_the_search_order(ctx):
+    n = 512
+    d_rows = ctx.alloc(n * 15 * 8)
+    outs = []
+    try:
+        ctx.generate_sts_device(n, 15, 99, True, d_rows)
+        for params in (None, G.init_mlp_params(14)):
+            ctx.set_ordering(params)
+            bufs = [ctx.alloc(n), ctx.alloc(16 * n), ctx.alloc(16 * n), ctx.alloc(n)]
+            ctx.check_bibd_device(n, 15, 35, G.COMPLETE | G.RAW | G.AUT_CANON, d_rows, *bufs)
+            ctx.stream_sync()
+            outs.append([ctx.d2h(np.zeros(n * k, dt), b) for b, k, dt in
+                         zip(bufs, (1, 16, 2, 1), (np.uint8, np.uint8, np.uint64, np.uint8))])
+            for b in bufs:
+                ctx.free(b)
+    finally:
+        ctx.set_ordering(None)
+        ctx.free(d_rows)
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+
+
+def test_first_row_labels_start_a_canonical_labeling(ctx):
+    n = 64
+    d_rows = ctx.alloc(n * 15 * 8)
+    d_lab = ctx.alloc(2 * n)
+    try:
+        ctx.generate_sts_device(n, 15, 7, False, d_rows)
+        ctx.label_first_rows(n, 15, 35, G.RAW, d_rows, d_lab)
+        rows = ctx.d2h(np.zeros(n * 15, np.uint64), d_rows).reshape(n, 15)
+        lab = ctx.d2h(np.zeros(n, np.uint16), d_lab)
+    finally:
+        ctx.free(d_rows)
+        ctx.free(d_lab)
+    for i in range(24):
+        M = oracle.rows_to_matrix(rows[i], 35)
+        _, aut, _ = oracle.bibd_canonize(M)
+        k = bin(int(lab[i])).count("1")
+        # the first rows of the labelings reaching the canonical form are one orbit of
+        # Aut(M) on the rows: at least one row, and their number divides |Aut|
+        assert k >= 1 and aut % k == 0, (i, k, aut)
