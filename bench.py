@@ -468,6 +468,81 @@ def run_mix(args):
     ctx.close()
 
 
+def run_learned(args):
+    """Config 4: the learned first-row order against the plain order."""
+    import ise_gb300 as G
+    n_train = 333_334                       # x 15 rows = 5.0M (features, label) pairs
+    n_eval = args.items
+    ctx = G.Context(max_items=16, aut_cap=1)
+    t0 = time.perf_counter()
+    d_rows = ctx.alloc(n_train * V * 8)
+    ctx.generate_sts_device(n_train, V, SEED, True, d_rows)
+    d_lab = ctx.alloc(2 * n_train)
+    d_nodes = ctx.alloc(8 * n_train)
+    ctx.label_first_rows(n_train, V, B, G.RAW, d_rows, d_lab, d_nodes)
+    lab = ctx.d2h(np.zeros(n_train, np.uint16), d_lab)
+    labels = ((lab[:, None] >> np.arange(V, dtype=np.uint16)) & 1).astype(np.float32).reshape(-1)
+    d_feat = ctx.alloc(n_train * V * 64 * 2)
+    ctx.mlp_features(n_train, V, B, d_rows, d_feat)
+    d_y = ctx.alloc(labels.nbytes)
+    ctx.h2d(d_y, labels)
+    params0 = G.init_mlp_params(SEED)
+    params, losses = ctx.mlp_train(n_train * V, d_feat, d_y, params0, epochs=3, batch=65536, lr=1e-3)
+    train_s = time.perf_counter() - t0
+    for p_ in (d_rows, d_lab, d_nodes, d_feat, d_y):
+        ctx.free(p_)
+
+    # evaluation on a fresh batch
+    d_rows = ctx.alloc(n_eval * V * 8)
+    ctx.generate_sts_device(n_eval, V, SEED + 1, True, d_rows)
+    flags = G.COMPLETE | G.RAW | G.AUT_CANON
+    res = {}
+    for name, prm in (("plain", None), ("learned", params)):
+        ctx.set_ordering(prm)
+        bufs = [ctx.alloc(n_eval), ctx.alloc(16 * n_eval), ctx.alloc(16 * n_eval), ctx.alloc(n_eval)]
+        for _ in range(args.warmup):
+            ctx.check_bibd_device(n_eval, V, B, flags, d_rows, *bufs)
+            ctx.stream_sync()
+        ms = []
+        for _ in range(args.steps):
+            ctx.check_bibd_device(n_eval, V, B, flags, d_rows, *bufs)
+            ctx.stream_sync()
+            ms.append(ctx.last_kernel_ms())
+        outs = [ctx.d2h(np.zeros(n_eval * k, np.uint8), b) for b, k in zip(bufs, (1, 16, 16, 1))]
+        res[name] = (n_eval * args.steps / (sum(ms) / 1e3), outs)
+        for b in bufs:
+            ctx.free(b)
+    identical = all(np.array_equal(a, b) for a, b in zip(res["plain"][1], res["learned"][1]))
+    # lex-max nodes in both orders and the top-1 hit rate of the network
+    d_lab = ctx.alloc(2 * n_eval)
+    d_nodes = ctx.alloc(8 * n_eval)
+    ctx.set_ordering(None)
+    ctx.label_first_rows(n_eval, V, B, G.RAW, d_rows, d_lab, d_nodes)
+    nodes_plain = ctx.d2h(np.zeros(n_eval, np.uint64), d_nodes).astype(np.float64)
+    lab = ctx.d2h(np.zeros(n_eval, np.uint16), d_lab)
+    d_feat = ctx.alloc(65536 * V * 64 * 2)
+    d_log = ctx.alloc(65536 * V * 4)
+    ctx.mlp_features(65536, V, B, d_rows, d_feat)
+    ctx.mlp_forward(65536 * V, d_feat, params, d_log)
+    logit = ctx.d2h(np.zeros(65536 * V, np.float32), d_log).reshape(65536, V)
+    top1 = float(np.mean((lab[:65536] >> np.argmax(logit, axis=1).astype(np.uint16)) & 1))
+    for p_ in (d_lab, d_nodes, d_feat, d_log, d_rows):
+        ctx.free(p_)
+    line = {"metric": "exact canonicity checks/sec, learned-ordered vs plain (config 4)",
+            "value": res["learned"][0], "unit": "checks/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 MLP / u64 bit rows", "data": "synthetic",
+            "config": {"workload": "train: %d STS(15) (seed %d, %d rows, labels from the exact search); eval: "
+                                   "%d fresh STS(15) (seed %d)" % (n_train, SEED, n_train * V, n_eval, SEED + 1),
+                       "mlp": "64-128-128-1 BF16, FP32 accumulate, Adam 3 epochs, batch 65536"},
+            "plain_checks_per_s": res["plain"][0], "learned_over_plain": res["learned"][0] / res["plain"][0],
+            "outputs_identical": identical, "train_loss_per_epoch": [float(x) for x in losses],
+            "train_seconds": train_s, "top1_hit_rate": top1,
+            "lexmax_nodes_plain_mean": float(nodes_plain.mean())}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -478,7 +553,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--items", type=int, default=N_ITEMS,
                     help="matrices per step (default: the full 1,048,576; smaller only for profiling)")
-    ap.add_argument("--workload", default="check-sts15", choices=["check-sts15", "mix"] + sorted(ENUM_WORKLOADS),
+    ap.add_argument("--workload", default="check-sts15",
+                    choices=["check-sts15", "mix", "learned"] + sorted(ENUM_WORKLOADS),
                     help="check-sts15 (default, the metric's configuration) or a whole enumeration")
     ap.add_argument("--mode", default="autcanon", choices=["autcanon", "plain"],
                     help="autcanon: |Aut| of rejected matrices via canonization (the workload); "
@@ -488,6 +564,9 @@ def main():
     if args.workload == "mix":
         if rank == 0:
             run_mix(args)
+    elif args.workload == "learned":
+        if rank == 0:
+            run_learned(args)
     elif args.workload != "check-sts15":
         if rank == 0:
             run_enum(args)
