@@ -74,6 +74,82 @@ __global__ void __launch_bounds__(TPB) bibd_uniform_kernel(uint32_t n_items, uin
     }
 }
 
+// The resident check in two passes.  Pass 1 (this kernel): the lex-max search of
+// every matrix gives the verdict and |Aut|; it needs neither permColumn nor the
+// reference search's state, so it runs with less shared memory (the column masks
+// sized by BCAP) and fewer registers.  Pass 2 (bibd_witness_kernel): the
+// reference-order search, only for the matrices found non-canonical, gives the
+// first rejecting permutation.
+template <int BCAP>
+__global__ void __launch_bounds__(TPB) bibd_max_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
+                                                       const uint64_t *__restrict__ rows, uint8_t *canonical,
+                                                       uint64_t *aut, uint8_t *status, uint64_t max_nodes,
+                                                       unsigned *ticket, const uint64_t *__restrict__ orders) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint16_t s_cm[BCAP * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= n_items)
+            break;
+        MaxOut mo{false, false, 0, 0, 0};
+        uint8_t st = 0;
+        if (!load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW)) {
+            st = ST_BADINPUT;
+        } else {
+            max_search(sm, v, b, max_nodes, mo, orders ? orders[it] : ID16);
+            if (mo.timeout)
+                st = ST_TIMEOUT;
+        }
+        const bool can = !st && !mo.improved;
+        canonical[it] = can ? 1 : 0;
+        if (status)
+            status[it] = st;
+        if (aut) {
+            const bool has = !st && (can || (flags & (F_AUT_CANON | F_FULL_AUT)));
+            aut[2 * (size_t)it] = has ? mo.leaves : 0;
+            aut[2 * (size_t)it + 1] = 0;
+        }
+    }
+}
+
+// Pass 2: the first rejecting permutation (reference order) of the matrices that
+// pass 1 found non-canonical; the others get the 0xFF witness.
+__global__ void __launch_bounds__(TPB) bibd_witness_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
+                                                           const uint64_t *__restrict__ rows,
+                                                           const uint8_t *__restrict__ canonical,
+                                                           uint8_t *witness16, uint8_t *status, uint64_t *trials_out,
+                                                           uint64_t max_trials, unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint16_t s_cm[64 * TPB];
+    __shared__ uint8_t s_pc[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, s_pc + tid, s_cm + tid, s_vd + tid};
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= n_items)
+            break;
+        const uint8_t st0 = status ? status[it] : 0;
+        CheckOut o;
+        reset_out(o);
+        if (!canonical[it] && !st0) {
+            load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW);
+            search(sm, v, b, flags & F_COMPLETE, max_trials, nullptr, 0, o);
+            if ((o.status & ST_TIMEOUT) && status)
+                status[it] = o.status;
+        }
+        if (witness16)
+            store_witness(witness16 + (size_t)it * 16u, o.witness, v);
+        if (trials_out)
+            trials_out[it] = o.trials;
+    }
+}
+
 // CanonizeMatrix(k = 0), MatrixCanonChecker.cpp:420-564: the matrix is replaced by
 // its canonical form, the lex-max matrix that the reference reaches by repeated
 // checks; the lex-max search finds it directly, together with |Aut|.
@@ -173,9 +249,37 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
                                       const uint64_t *d_orders) {
     if (!n)
         return cudaSuccess;
+    const int need = (int)((n + TPB - 1) / TPB);
+    if (!(flags & (F_SAVE_AUTS | F_REFERENCE_ORDER)) && (flags & (F_AUT_CANON | F_FULL_AUT))) {
+        // |Aut| wanted for every matrix: two passes, the lex-max search for all,
+        // the reference-order witness for the rejected ones.  (Without it the
+        // single pass below rejects most non-canonical matrices in a few trials
+        // of the reference order and runs the lex-max search only for the rest.)
+        cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
+        int grid = b <= 40 ? blocks_for((const void *)bibd_max_kernel<40>, num_sms)
+                           : blocks_for((const void *)bibd_max_kernel<64>, num_sms);
+        if (grid > need)
+            grid = need;
+        if (b <= 40)
+            bibd_max_kernel<40><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status, max_trials,
+                                                     tk, d_orders);
+        else
+            bibd_max_kernel<64><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status, max_trials,
+                                                     tk, d_orders);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+            return e;
+        if (d_witness16 || d_trials) {
+            int g2 = blocks_for((const void *)bibd_witness_kernel, num_sms);
+            if (g2 > need)
+                g2 = need;
+            bibd_witness_kernel<<<g2, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_witness16, d_status,
+                                                   d_trials, max_trials, tk + 1);
+        }
+        return cudaGetLastError();
+    }
     cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
     int grid = blocks_for((const void *)bibd_uniform_kernel, num_sms);
-    const int need = (int)((n + TPB - 1) / TPB);
     if (grid > need)
         grid = need;
     bibd_uniform_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut, d_status,
