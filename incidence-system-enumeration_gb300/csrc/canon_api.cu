@@ -402,11 +402,20 @@ int canon_sync(canon_ctx *c, canon_results *r) {
                 return cuda_fail(c, e, "mixed check launch");
             ++c->launches;
         } else if (c->n_bitems) {
-            e = canon::launch_bibd_check(c->d_bitems, c->n_bitems, c->d_words, c->d_out, c->cfg.max_trials,
-                                         c->d_ticket, c->num_sms, s);
+            // items that all want |Aut| without the reference order take the two-pass check
+            bool two_pass = true;
+            for (uint32_t i = 0; i < c->n_bitems && two_pass; ++i) {
+                const uint8_t f = c->h_bitems[i].flags;
+                two_pass = (f & (canon::F_AUT_CANON | canon::F_FULL_AUT)) &&
+                           !(f & (canon::F_SAVE_AUTS | canon::F_REFERENCE_ORDER));
+            }
+            e = two_pass ? canon::launch_bibd_check_two_pass(c->d_bitems, c->n_bitems, c->d_words, c->d_out,
+                                                             c->cfg.max_trials, c->d_ticket, c->num_sms, s)
+                         : canon::launch_bibd_check(c->d_bitems, c->n_bitems, c->d_words, c->d_out,
+                                                    c->cfg.max_trials, c->d_ticket, c->num_sms, s);
             if (e != cudaSuccess)
                 return cuda_fail(c, e, "bibd check launch");
-            ++c->launches;
+            c->launches += two_pass ? 2 : 1;
         } else if (c->n_kitems) {
             e = canon::launch_ksys_check(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, c->d_ticket + 1,
                                          c->num_sms, s);

@@ -150,6 +150,74 @@ __global__ void __launch_bounds__(TPB) bibd_witness_kernel(uint32_t n_items, uin
     }
 }
 
+// The two passes over work items of any shape (the batched path).
+__global__ void __launch_bounds__(TPB) bibd_items_max_kernel(const Item *__restrict__ items, uint32_t n_items,
+                                                             const uint64_t *__restrict__ words, Outputs out,
+                                                             uint64_t max_nodes, unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint16_t s_cm[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= n_items)
+            break;
+        const Item item = items[it];
+        const unsigned n = item.nrows, b = item.ncols, o_i = item.out_idx;
+        MaxOut mo{false, false, 0, 0, 0};
+        uint8_t st = 0;
+        if (item.kind != KIND_BIBD || n < 1 || n > VMAX || b < 1 || b > BMAX ||
+            !load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW)) {
+            st = ST_BADINPUT;
+        } else {
+            max_search(sm, n, b, max_nodes, mo);
+            if (mo.timeout)
+                st = ST_TIMEOUT;
+        }
+        const bool can = !st && !mo.improved;
+        out.canonical[o_i] = can ? 1 : 0;
+        out.status[o_i] = st;
+        out.aut[2 * (size_t)o_i] = st ? 0 : mo.leaves;
+        out.aut[2 * (size_t)o_i + 1] = 0;
+        out.player_index[o_i] = -1;
+        out.n_auts[o_i] = 0;
+        out.len_aut[o_i] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) bibd_items_witness_kernel(const Item *__restrict__ items, uint32_t n_items,
+                                                                 const uint64_t *__restrict__ words, Outputs out,
+                                                                 uint64_t max_trials, unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint16_t s_cm[64 * TPB];
+    __shared__ uint8_t s_pc[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, s_pc + tid, s_cm + tid, s_vd + tid};
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= n_items)
+            break;
+        const Item item = items[it];
+        const unsigned n = item.nrows, b = item.ncols, o_i = item.out_idx;
+        CheckOut o;
+        reset_out(o);
+        if (!out.canonical[o_i] && !out.status[o_i]) {
+            load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW);
+            search(sm, n, b, item.flags & F_COMPLETE, max_trials, nullptr, 0, o);
+            if (o.status & ST_TIMEOUT)
+                out.status[o_i] = o.status;
+        }
+        out.reject_row[o_i] = o.reject_row;
+        out.row_to_change[o_i] = o.rtc;
+        store_witness(out.witness + (size_t)o_i * 16u, o.witness, n);
+        out.trials[o_i] = o.trials;
+    }
+}
+
 // CanonizeMatrix(k = 0), MatrixCanonChecker.cpp:420-564: the matrix is replaced by
 // its canonical form, the lex-max matrix that the reference reaches by repeated
 // checks; the lex-max search finds it directly, together with |Aut|.
@@ -239,6 +307,26 @@ cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint6
     if (grid > need)
         grid = need;
     bibd_items_kernel<<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bibd_check_two_pass(const Item *d_items, uint32_t n_items, const uint64_t *d_words, Outputs out,
+                                       uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
+    if (!n_items)
+        return cudaSuccess;
+    cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
+    const int need = (int)((n_items + TPB - 1) / TPB);
+    int grid = blocks_for((const void *)bibd_items_max_kernel, num_sms);
+    if (grid > need)
+        grid = need;
+    bibd_items_max_kernel<<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    int g2 = blocks_for((const void *)bibd_items_witness_kernel, num_sms);
+    if (g2 > need)
+        g2 = need;
+    bibd_items_witness_kernel<<<g2, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk + 1);
     return cudaGetLastError();
 }
 

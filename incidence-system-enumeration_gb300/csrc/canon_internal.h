@@ -50,6 +50,11 @@ constexpr uint8_t ST_BADINPUT = 1, ST_TIMEOUT = 2, ST_PERM_OVF = 4;
 cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint64_t *d_words,
                               Outputs out, uint64_t max_trials, unsigned *d_ticket, int num_sms,
                               cudaStream_t s);
+// the same check in two passes (lex-max search for all, witness for the rejected) for items that all
+// want |Aut| (CANON_AUT_CANON or CANON_FULL_AUT) without the reference order; d_ticket: two words
+cudaError_t launch_bibd_check_two_pass(const Item *d_items, uint32_t n_items, const uint64_t *d_words,
+                                       Outputs out, uint64_t max_trials, unsigned *d_ticket, int num_sms,
+                                       cudaStream_t s);
 cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                                       const uint64_t *d_rows, uint8_t *d_canonical,
                                       uint8_t *d_witness16, uint64_t *d_aut, uint8_t *d_status,
