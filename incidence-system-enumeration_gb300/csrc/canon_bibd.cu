@@ -488,7 +488,11 @@ cudaError_t launch_bibd_check_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    // the work counter is cleared by the launcher before the check runs
+    // the work counters are cleared by the launchers before the check runs; the
+    // route is the one canon_sync takes for the same flags
+    const bool two_pass = (flags & (F_AUT_CANON | F_FULL_AUT)) && !(flags & (F_SAVE_AUTS | F_REFERENCE_ORDER));
+    if (two_pass)
+        return launch_bibd_check_two_pass(items, n, d_rows, out, max_trials, counter, sms, s);
     return launch_bibd_check(items, n, d_rows, out, max_trials, counter, sms, s);
 }
 
