@@ -598,7 +598,9 @@ int canon_check_bibd_device(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, ui
                                                      c->num_sms, s, orders);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "check launch");
-    ++c->launches;
+    // the |Aut| route is two kernels (lex-max pass, witness pass)
+    const bool two = !(flags & (CANON_SAVE_AUTS | CANON_REFERENCE_ORDER)) && (flags & (CANON_AUT_CANON | CANON_FULL_AUT));
+    c->launches += two ? ((d_witness16 || d_trials) ? 2 : 1) : 1;
     cudaEventRecord(c->ev1, s);
     return CANON_OK;
 }
