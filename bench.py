@@ -317,14 +317,15 @@ def run_enum(args):
     """Whole enumerations with every level checked on the GPU (configs 1 and 5)."""
     import ise_gb300 as G
     kind, params, desc = ENUM_WORKLOADS[args.workload]
-    ctx = G.Context(max_items=1 << 16)
+    ctx = G.Context(max_items=1 << 20)
     runs = []
     for _ in range(args.warmup + args.steps):
         if kind == "bibd":
             found, st = ctx.enumerate_bibd(*params)
         else:
             found, st = ctx.enumerate_ksys(*params)
-        runs.append((len(found), st.checks, st.seconds, st.kernel_ms, st.batches))
+        runs.append((len(found), st.checks, st.seconds, st.kernel_ms, st.batches,
+                     [int(x) for x in st.level_checks], [round(float(x), 3) for x in st.level_kernel_ms]))
     timed = runs[args.warmup:]
     secs = sum(r[2] for r in timed)
     checks = sum(r[1] for r in timed)
@@ -347,7 +348,8 @@ def run_enum(args):
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 bit rows / u8",
             "data": "exhaustive", "config": {"workload": desc, "designs": timed[0][0],
-                                             "checks_per_step": timed[0][1], "batches_per_step": timed[0][4]},
+                                             "checks_per_step": timed[0][1], "batches_per_step": timed[0][4],
+                                             "level_checks": timed[0][5], "level_kernel_ms": timed[-1][6]},
             "checks_per_s": checks / secs, "kernel_ms_per_step": sum(r[3] for r in timed) / args.steps,
             "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)

@@ -712,6 +712,52 @@ int canon_label_first_rows(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uin
     return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "labels");
 }
 
+int canon_design_properties(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, const uint64_t *rows,
+                            uint8_t *simple, uint8_t *transitive) {
+    if (!c || (n && !rows) || v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX)
+        return fail(c, CANON_EINVAL, "design properties: bad arguments");
+    if (!n)
+        return CANON_OK;
+    if (simple) {
+        for (uint32_t i = 0; i < n; ++i) {
+            std::vector<uint32_t> colpat(b, 0u);
+            for (uint32_t r = 0; r < v; ++r)
+                for (uint32_t col = 0; col < b; ++col)
+                    colpat[col] |= (uint32_t)((rows[(size_t)i * v + r] >> col) & 1u) << r;
+            std::sort(colpat.begin(), colpat.end());
+            simple[i] = std::adjacent_find(colpat.begin(), colpat.end()) == colpat.end();
+        }
+    }
+    if (!transitive)
+        return CANON_OK;
+    cudaSetDevice(c->device);
+    uint64_t *d_rows = nullptr;
+    uint16_t *d_first = nullptr;
+    cudaError_t e = cudaMalloc(&d_rows, (size_t)n * v * sizeof(uint64_t));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&d_first, (size_t)n * sizeof(uint16_t));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_rows, rows, (size_t)n * v * sizeof(uint64_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        e = canon::launch_bibd_labels(n, v, b, canon::F_RAW | canon::F_COMPLETE, d_rows, d_first, nullptr, nullptr,
+                                      c->cfg.max_trials, c->d_ticket, c->num_sms, c->stream);
+        ++c->launches;
+    }
+    std::vector<uint16_t> first(n);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(first.data(), d_first, (size_t)n * sizeof(uint16_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_rows);
+    cudaFree(d_first);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "design properties");
+    const unsigned all = (v >= 16) ? 0xFFFFu : ((1u << v) - 1u);
+    for (uint32_t i = 0; i < n; ++i)
+        transitive[i] = first[i] == all;
+    return CANON_OK;
+}
+
 int canon_mlp_forward(canon_ctx *c, uint64_t n, const void *d_x, const float *params, float *d_logits) {
     if (!c || !d_x || !d_logits || !params)
         return fail(c, CANON_EINVAL, "forward: bad arguments");
@@ -842,3 +888,18 @@ int canon_check_bibd_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
 }
 
 }  // extern "C"
+
+namespace canon {
+
+// The largest batch of matrices with `words` 64-bit words (BIBD) or `bytes` bytes
+// (k-systems) each that one canon_submit_* call can queue on an empty context.
+uint32_t batch_capacity(const canon_ctx *c, uint32_t words, uint32_t bytes) {
+    uint64_t n = c->cfg.max_items;
+    if (words && c->cfg.max_words / words < n)
+        n = c->cfg.max_words / words;
+    if (bytes && c->max_bytes / bytes < n)
+        n = c->max_bytes / bytes;
+    return (uint32_t)n;
+}
+
+}  // namespace canon

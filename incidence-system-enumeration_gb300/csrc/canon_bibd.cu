@@ -279,7 +279,9 @@ __global__ void __launch_bounds__(TPB) bibd_label_kernel(uint32_t n_items, uint3
             break;
         MaxOut mo{false, false, 0, 0, 0};
         if (load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW))
-            max_search(sm, v, b, max_nodes, mo, orders ? orders[it] : ID16);
+            // unpruned when node counts are asked for: they stay comparable between
+            // search orders (the first rows are the same either way)
+            max_search(sm, v, b, max_nodes, mo, orders ? orders[it] : ID16, nodes == nullptr);
         if (first_rows)
             first_rows[it] = (uint16_t)(mo.timeout ? 0 : mo.first_rows);
         if (nodes)

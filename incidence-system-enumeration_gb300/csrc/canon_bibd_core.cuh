@@ -561,7 +561,20 @@ __device__ void search(Smem sm, unsigned n, unsigned b, unsigned flags, uint64_t
 // The rows of M serve as the first bound; a greater row replaces the bound from
 // that level down (the subtrees already searched are all smaller than it), so M
 // is canonical iff the bound never rises.  On return R_() holds the canonical
-// form.  No automorphism pruning: every leaf is a distinct row permutation.
+// form.
+//
+// Automorphism pruning (prune = true), while the bound is still M: the identity
+// path is searched first; below it, a subtree is left at its first leaf, which is
+// an automorphism fixing the rows above the branch point d and moving row d.  The
+// row orbits of all automorphisms found so far are then those of the pointwise
+// stabilizer of rows 0..d-1 (every one was found below level d), so at level d
+// only orbit leaders are branched on, and |Aut| is the product over d of the
+// length of the orbit of d -- the orbit-stabilizer count of Update_Orbits() /
+// updateGroupOrder() (GroupOrder.h:30-73), with the leaders tried in increasing
+// order as next_permutation() does.  Skipped subtrees are images of searched ones
+// under an automorphism of M, so they hold no greater matrix: once the bound
+// rises the search goes on unpruned and counts the leaves that reach the new
+// bound, exactly as without pruning.
 struct MaxOut {
     bool improved;      // M is not canonical
     bool timeout;
@@ -599,12 +612,17 @@ __device__ __forceinline__ void refine_arranged(Smem sm, unsigned lv, unsigned c
 }
 
 // order0: the order in which the rows are tried as the first row (nibble-packed;
-// ID16 = increasing, the plain order).  Only the search order changes with it.
+// ID16 = increasing, the plain order).  Only the search order changes with it;
+// a reordered first level turns the automorphism pruning off (it needs the
+// identity path first).  stop_on_improve: return as soon as M is known not to be
+// canonical (leaves, first_rows and R_() are then incomplete).
 __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o,
-                           uint64_t order0 = ID16) {
+                           uint64_t order0 = ID16, bool prune = true, bool stop_on_improve = false) {
     const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     const uint64_t cols = (1ull << b) - 1ull;
     const uint64_t sentinel = 1ull << b;
+    const uint64_t nmask1 = (n >= 16) ? NIB1 : (NIB1 & ((1ull << (4 * n)) - 1ull));
+    prune = prune && order0 == ID16;
     o.improved = false;
     o.timeout = false;
     o.leaves = 0;
@@ -613,16 +631,31 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
     unsigned valid = n;        // rows 0..valid-1 of the bound (and levels 0..valid) are set
     unsigned used = 0;
     uint64_t perm = 0;
+    uint64_t orb = ID16;       // row orbits of the automorphisms found (pruned mode)
+    uint64_t order = 1;        // product of the orbit lengths of the finished levels
+    unsigned id_top = 0;       // perm[0..id_top-1] is the identity
     unsigned i = 0;
     bool enter = true;         // entering the node at level i (else: next child of level i)
     for (;;) {
+        const bool pr = prune && !o.improved;
         if (enter) {
             if (i == n) {
+                if (pr && id_top < n) {
+                    // an automorphism moving row id_top: merge its orbits and go back
+                    // to the identity node it branched from
+                    orb = merge_orbits(perm, orb, n, id_top, nmask1);
+                    i = id_top;
+                    used = (1u << i) - 1u;
+                    enter = false;
+                    continue;
+                }
                 ++o.leaves;
                 o.first_rows |= 1u << pg(perm, 0);
                 enter = false;
                 --i;
                 used &= ~(1u << pg(perm, i));
+                if (id_top > i)
+                    id_top = i;
                 continue;
             }
             if (++o.nodes > max_nodes) {
@@ -688,9 +721,11 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                 // smaller than the bound: every extension is smaller too
                 enter = false;
                 if (i == 0)
-                    return;
+                    break;
                 --i;
                 used &= ~(1u << pg(perm, i));
+                if (id_top > i)
+                    id_top = i;
                 continue;
             }
             if (state == 1 || !have_bound) {
@@ -698,6 +733,8 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                     o.improved = true;
                     o.leaves = 0;
                     o.first_rows = 0;
+                    if (stop_on_improve)
+                        return;
                 }
                 R_(i) = arr;
                 L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
@@ -706,13 +743,26 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
             VD_(i) = tied;            // children still to visit
         }
         // next child of the node at level i
-        const unsigned rem = VD_(i);
+        unsigned rem = VD_(i);
+        if (pr && id_top >= i) {
+            // at an identity node only orbit leaders are branched on
+            while (rem && pg(orb, __ffs(rem) - 1) != (unsigned)(__ffs(rem) - 1))
+                rem &= rem - 1;
+        }
         if (!rem) {
+            if (pr && id_top >= i) {
+                unsigned len = 0;
+                for (unsigned q = i; q < n; ++q)
+                    len += pg(orb, q) == i;
+                order *= len;
+            }
             if (i == 0)
-                return;
+                break;
             enter = false;
             --i;
             used &= ~(1u << pg(perm, i));
+            if (id_top > i)
+                id_top = i;
             continue;
         }
         unsigned x = __ffs(rem) - 1;
@@ -729,13 +779,25 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
         refine_arranged(sm, i, x, b);
         perm = ps(perm, i, x);
         used |= 1u << x;
+        if (id_top == i && x == i)
+            id_top = i + 1;
         ++i;
         enter = true;
     }
+    if (prune && !o.improved) {
+        o.leaves = order;
+        unsigned fr = 0;
+        for (unsigned q = 0; q < n; ++q)
+            fr |= (pg(orb, q) == 0 ? 1u : 0u) << q;
+        o.first_rows = fr;
+    }
 }
 
-// Trials the reference-order search may spend before the lex-max search decides.
-constexpr uint64_t QUICK_TRIALS = 256;
+// Trials the reference-order search may spend before the lex-max search decides:
+// a complete canonical matrix needs far more in the reference order (~52K for an
+// STS(15)), a partial one often far fewer than the lex-max search's nodes.
+constexpr uint64_t QUICK_TRIALS_COMPLETE = 256;
+constexpr uint64_t QUICK_TRIALS_PARTIAL = 2048;
 
 __device__ __forceinline__ void reset_out(CheckOut &o) {
     o.canonical = 1;
@@ -811,41 +873,49 @@ __device__ void check_one(Smem sm, const uint64_t *src, unsigned n, unsigned b, 
         o.canonical = 0;
         return;
     }
-    const bool want_aut = (flags & (F_AUT_CANON | F_FULL_AUT)) || o.canonical;
     if (flags & (F_SAVE_AUTS | F_REFERENCE_ORDER)) {
         check_reference(sm, n, b, flags, max_trials, aut_dst, aut_cap, o);
     } else {
         const unsigned sflags = flags & ~(F_FULL_AUT | F_AUT_CANON);
-        search(sm, n, b, sflags, QUICK_TRIALS < max_trials ? QUICK_TRIALS : max_trials, nullptr, 0, o);
-        const bool decided = !o.canonical && !(o.status & ST_TIMEOUT);
-        if (decided && !(flags & (F_AUT_CANON | F_FULL_AUT))) {
-            o.aut_lo = 0;                // rejected: the reference leaves |Aut| undefined
-            o.aut_hi = 0;
+        const bool aut_always = flags & (F_AUT_CANON | F_FULL_AUT);
+        const uint64_t quick_cap = (flags & F_COMPLETE) ? QUICK_TRIALS_COMPLETE : QUICK_TRIALS_PARTIAL;
+        search(sm, n, b, sflags, quick_cap < max_trials ? quick_cap : max_trials, nullptr, 0, o);
+        if (!(o.status & ST_TIMEOUT)) {
+            // the reference-order search finished within the short budget (typical for
+            // rejected matrices and for partial matrices with large groups)
+            if (!o.canonical) {
+                o.aut_lo = 0;            // rejected: the reference leaves |Aut| undefined
+                o.aut_hi = 0;
+                if (aut_always) {
+                    MaxOut mo;
+                    max_search(sm, n, b, max_trials, mo, order0);
+                    if (mo.timeout)
+                        o.status = ST_TIMEOUT;
+                    else
+                        o.aut_lo = mo.leaves;
+                }
+            }
         } else {
             const uint64_t quick = o.trials;
             o.status = 0;
             MaxOut mo;
-            max_search(sm, n, b, max_trials, mo, order0);
+            max_search(sm, n, b, max_trials, mo, order0, true, !aut_always);
             if (mo.timeout) {
                 o.status = ST_TIMEOUT;
-            } else if (!decided) {
-                if (mo.improved) {
-                    // non-canonical, rejected late in the reference order: find its witness
-                    load_rows(sm, src, n, b, flags);
-                    reset_out(o);
-                    search(sm, n, b, sflags, max_trials, nullptr, 0, o);
-                    o.trials += quick;
-                } else {
-                    o.canonical = 1;
-                }
-            }
-            if (!o.status) {
-                const bool has = !mo.improved || (flags & (F_AUT_CANON | F_FULL_AUT));
-                o.aut_lo = has ? mo.leaves : 0;
+            } else if (mo.improved) {
+                // non-canonical, rejected late in the reference order: find its witness
+                load_rows(sm, src, n, b, flags);
+                reset_out(o);
+                search(sm, n, b, sflags, max_trials, nullptr, 0, o);
+                o.trials += quick;
+                o.aut_lo = aut_always ? mo.leaves : 0;
+                o.aut_hi = 0;
+            } else {
+                o.canonical = 1;
+                o.aut_lo = mo.leaves;
                 o.aut_hi = 0;
             }
         }
-        (void)want_aut;
     }
     if (o.status & ST_TIMEOUT)
         o.canonical = 0;

@@ -11,9 +11,14 @@
 // canonical complete matrices is the same as the depth-first search finds.
 #include <chrono>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "../../include/canon_gb300.h"
+
+namespace canon {
+uint32_t batch_capacity(const canon_ctx *c, uint32_t words, uint32_t bytes);
+}
 
 namespace {
 
@@ -164,6 +169,40 @@ struct KsysGen {
     }
 };
 
+// children of every parent of a level, generated on all host cores; the
+// concatenation keeps the parents' order, so the result does not depend on the
+// number of threads
+template <typename Gen, typename T>
+void level_children(const Gen &proto, const std::vector<T> &level, size_t stride, int n, std::vector<T> &out) {
+    const size_t parents = level.size() / stride;
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt < 1)
+        nt = 1;
+    if (nt > 32)
+        nt = 32;
+    if (parents < 64)
+        nt = 1;
+    std::vector<std::vector<T>> part(nt);
+    auto work = [&](unsigned t) {
+        Gen g = proto;
+        const size_t lo = parents * t / nt, hi = parents * (t + 1) / nt;
+        for (size_t p = lo; p < hi; ++p)
+            g.children(level.data() + p * stride, n, part[t]);
+    };
+    if (nt == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; ++t)
+            th.emplace_back(work, t);
+        for (auto &x : th)
+            x.join();
+    }
+    out.clear();
+    for (auto &v : part)
+        out.insert(out.end(), v.begin(), v.end());
+}
+
 }  // namespace
 
 extern "C" {
@@ -183,11 +222,12 @@ int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uin
     gen.r = (int)r;
     gen.k = (int)k;
     gen.lambda = (int)lambda;
-    const uint32_t chunk = 1u << 15;
+    const uint32_t chunk = canon::batch_capacity(ctx, v, 0);
+    if (!chunk)
+        return CANON_ENOMEM;
     while (n < (int)v && !level.empty()) {
         std::vector<uint64_t> cand;
-        for (size_t p = 0; p < level.size() / n; ++p)
-            gen.children(level.data() + p * n, n, cand);
+        level_children(gen, level, (size_t)n, n, cand);
         const int m = n + 1;
         const size_t count = cand.size() / m;
         const bool complete = m == (int)v;
@@ -203,6 +243,8 @@ int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uin
                 return rc;
             st.checks += cnt;
             st.kernel_ms += res.kernel_ms;
+            st.level_checks[m - 1] += cnt;
+            st.level_kernel_ms[m - 1] += res.kernel_ms;
             ++st.batches;
             for (uint32_t i = 0; i < cnt; ++i) {
                 if (!res.canonical[i])
@@ -238,12 +280,13 @@ int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *
     int n = 1;
     KsysGen gen{};
     gen.np = (int)np;
-    const uint32_t chunk = 1u << 15;
+    const uint32_t chunk = canon::batch_capacity(ctx, 0, np * (np - 1));
+    if (!chunk)
+        return CANON_ENOMEM;
     const int rounds = (int)np - 1;
     while (n < rounds && !level.empty()) {
         std::vector<uint8_t> cand;
-        for (size_t p = 0; p < level.size() / (n * np); ++p)
-            gen.children(level.data() + p * n * np, n, cand);
+        level_children(gen, level, (size_t)n * np, n, cand);
         const int m = n + 1;
         const size_t count = cand.size() / (m * np);
         std::vector<uint8_t> next;
@@ -258,6 +301,8 @@ int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *
                 return rc;
             st.checks += cnt;
             st.kernel_ms += res.kernel_ms;
+            st.level_checks[m - 1] += cnt;
+            st.level_kernel_ms[m - 1] += res.kernel_ms;
             ++st.batches;
             for (uint32_t i = 0; i < cnt; ++i) {
                 if (!res.canonical[i])

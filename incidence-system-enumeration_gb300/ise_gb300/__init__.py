@@ -56,6 +56,7 @@ HEADER_SYMBOLS = [
     "canon_memcpy_h2d", "canon_last_kernel_ms", "canon_kernel_launches", "canon_stream_sync",
     "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys", "canon_mlp_features",
     "canon_label_first_rows", "canon_mlp_forward", "canon_mlp_grad", "canon_mlp_train",
+    "canon_design_properties", "canon_report_bibd", "canon_ksys_cycles", "canon_report_ksys",
 ]
 MLP_PARAMS = 128 * 64 + 128 + 128 * 128 + 128 + 128 + 1
 
@@ -95,7 +96,8 @@ class DeviceOutputs(ctypes.Structure):
 
 class EnumStats(ctypes.Structure):
     _fields_ = [("checks", ctypes.c_uint64), ("designs", ctypes.c_uint64), ("levels", ctypes.c_uint32),
-                ("batches", ctypes.c_uint32), ("seconds", ctypes.c_double), ("kernel_ms", ctypes.c_double)]
+                ("batches", ctypes.c_uint32), ("seconds", ctypes.c_double), ("kernel_ms", ctypes.c_double),
+                ("level_checks", ctypes.c_uint64 * 16), ("level_kernel_ms", ctypes.c_double * 16)]
 
 
 DESIGN_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint32,
@@ -171,6 +173,15 @@ def load_library(path=LIB_PATH):
     L.canon_mlp_grad.argtypes = [vp, u64, vp, vp, fp, fp, fp]
     L.canon_mlp_train.argtypes = [vp, u64, vp, vp, u32, u32, ctypes.c_float, fp, fp]
     L.canon_set_ordering.argtypes = [vp, ctypes.POINTER(MlpWeights)]
+    u8p, sz = ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t
+    L.canon_design_properties.argtypes = [vp, u32, u32, u32, u64p, u8p, u8p]
+    L.canon_report_bibd.argtypes = [u32, u32, u32, u32, u32, u32, u64p, u8p, u8p, u64, ctypes.c_double,
+                                    ctypes.c_char_p, sz]
+    L.canon_report_bibd.restype = sz
+    L.canon_ksys_cycles.argtypes = [u32, u32, u8p, ctypes.c_char_p, sz]
+    L.canon_ksys_cycles.restype = sz
+    L.canon_report_ksys.argtypes = [u32, u32, u32, u8p, u64p, ctypes.c_char_p, sz]
+    L.canon_report_ksys.restype = sz
     _lib = L
     return L
 
@@ -199,6 +210,45 @@ def init_mlp_params(seed):
     p[8320:24704] = rng.normal(0, np.sqrt(2 / 128), 16384)
     p[24832:24960] = rng.normal(0, np.sqrt(1 / 128), 128)
     return p
+
+
+def _text(call):
+    """Runs a snprintf-convention writer twice: once for the length, once to fill."""
+    n = call(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    call(buf, n + 1)
+    return buf.value.decode()
+
+
+def report_bibd(params, auts, simple=None, transitive=None, fully_constructed=0, seconds=0.0, lib=None):
+    """The |Aut(D)| table of a BIBD run (canon_report_bibd), as text."""
+    L = lib or load_library()
+    v, b, r, k, lam = params
+    n = len(auts)
+    a = np.ascontiguousarray(auts, np.uint64)
+    s_ = None if simple is None else np.ascontiguousarray(simple, np.uint8)
+    t_ = None if transitive is None else np.ascontiguousarray(transitive, np.uint8)
+    u8p = ctypes.POINTER(ctypes.c_uint8)
+    return _text(lambda buf, cap: L.canon_report_bibd(
+        v, b, r, k, lam, n, _ptr(a, ctypes.c_uint64), None if s_ is None else _ptr(s_, ctypes.c_uint8),
+        None if t_ is None else _ptr(t_, ctypes.c_uint8), int(fully_constructed), float(seconds), buf, cap))
+
+
+def ksys_cycles(M, lib=None):
+    """Cycle descriptor of one k-system matrix (rounds x np, result() form)."""
+    L = lib or load_library()
+    M = np.ascontiguousarray(M, np.uint8)
+    return _text(lambda buf, cap: L.canon_ksys_cycles(M.shape[1], M.shape[0], _ptr(M, ctypes.c_uint8), buf, cap))
+
+
+def report_ksys(matrices, auts, lib=None):
+    """The |Aut(M)| x cycles table of a k-system run (canon_report_ksys), as text."""
+    L = lib or load_library()
+    X = np.ascontiguousarray(np.stack(matrices), np.uint8)
+    a = np.ascontiguousarray(auts, np.uint64)
+    n, rounds, np_ = X.shape
+    return _text(lambda buf, cap: L.canon_report_ksys(np_, rounds, n, _ptr(X, ctypes.c_uint8),
+                                                      _ptr(a, ctypes.c_uint64), buf, cap))
 
 
 def pack_rows(M):
@@ -339,6 +389,19 @@ class Context:
         st = EnumStats()
         self._check(self.lib.canon_enumerate_bibd(self.h, v, b, r, k, lam, c, None, ctypes.byref(st)))
         return found, st
+
+    def design_properties(self, designs):
+        """(simple, transitive) flags of complete designs (v x b 0/1 matrices)."""
+        designs = list(designs)
+        if not designs:
+            return np.zeros(0, np.uint8), np.zeros(0, np.uint8)
+        v, b = designs[0].shape
+        rows = np.ascontiguousarray(np.stack([pack_rows(M) for M in designs]), np.uint64)
+        simple = np.zeros(len(designs), np.uint8)
+        trans = np.zeros(len(designs), np.uint8)
+        self._check(self.lib.canon_design_properties(self.h, len(designs), v, b, _ptr(rows, ctypes.c_uint64),
+                                                     _ptr(simple, ctypes.c_uint8), _ptr(trans, ctypes.c_uint8)))
+        return simple, trans
 
     def enumerate_ksys(self, np_):
         """All 1-factorizations of K_np up to isomorphism: [(rounds x np uint8, |Aut|)], stats."""

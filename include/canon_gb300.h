@@ -198,6 +198,10 @@ typedef struct {
     uint32_t batches;     /* canon_sync calls */
     double   seconds;     /* wall time */
     double   kernel_ms;   /* device time of the checks */
+    /* per level: matrices with l+1 rows (rounds) checked, and their device time;
+     * level_checks[v-1] counts the complete matrices constructed */
+    uint64_t level_checks[16];
+    double   level_kernel_ms[16];
 } canon_enum_stats;
 
 /* Called for every canonical complete matrix: BIBD rows as rows x uint64 (cast to
@@ -216,6 +220,38 @@ int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uin
  * group size 2 with the check at every level (k-Factorization/TripleSys/Source/
  * TripleSys.cpp:80-775, check at checkCurrentResult.cpp:91).  np even, <= 12. */
 int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *user, canon_enum_stats *stats);
+
+/* ---- result tables (the reference's text output of a finished run) ----
+ * Per complete design: simple[i] = no two equal columns (no replicated blocks) and
+ * transitive[i] = Aut(D) transitive on the points, the properties that the
+ * reference counts as Ns and Ndt (CGroupsInfo, Source/GroupsInfo.h:4-11; the
+ * transitivity test groupIsTransitive(), Source/CanonicityChecker.cpp:292-304).
+ * Transitivity comes from the lex-max search on the GPU: the rows that start a
+ * labeling reaching the canonical form form one orbit of Aut(D).  Host rows
+ * (n*v words); either output may be NULL. */
+int canon_design_properties(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, const uint64_t *rows,
+                            uint8_t *simple, uint8_t *transitive);
+/* The |Aut(D)| table that closes a BIBD run (CGroupsInfo::printGroupInfo,
+ * Source/GroupsInfo.cpp:72-150, in the layout of Results/BIBDs/V = v/<v>_<k>_<l>.txt):
+ * one line per group order with Nd / Ns / Ndt / Nst, the totals and the run's
+ * counters.  aut[i] = |Aut| of design i; simple / transitive may be NULL (all 0).
+ * Host only.  Writes at most cap bytes including the final 0 and returns the full
+ * length (snprintf convention). */
+size_t canon_report_bibd(uint32_t v, uint32_t b, uint32_t r, uint32_t k, uint32_t lambda, uint32_t n,
+                         const uint64_t *aut, const uint8_t *simple, const uint8_t *transitive,
+                         uint64_t fully_constructed, double seconds, char *buf, size_t cap);
+/* The cycle descriptor of one k-system matrix (alldata::matrixStatOutput,
+ * k-Factorization/TripleSys/Source/p1fCheck.cpp:499-515, without its "Cycles:"
+ * prefix): for every pair of rounds the cycle lengths of their union, the cycle
+ * sets in increasing order, each as "count(l1:l2:...) ".  rounds x np bytes in
+ * result() form.  Host only; snprintf convention. */
+size_t canon_ksys_cycles(uint32_t np, uint32_t rounds, const uint8_t *matrix, char *buf, size_t cap);
+/* The |Aut(M)| x cycles table of a k-system run (MatrixDB::printRecord and
+ * DescrStorage::reportResult, k-Factorization/TripleSys/Include/MatrixDB.h, in the
+ * layout of K_Results.txt, without its time stamp): n matrices of rounds x np
+ * bytes, aut[i] = |Aut(M)|.  Host only; snprintf convention. */
+size_t canon_report_ksys(uint32_t np, uint32_t rounds, uint32_t n, const uint8_t *matrices, const uint64_t *aut,
+                         char *buf, size_t cap);
 
 /* ---- the learned search order (no counterpart in the reference) ----
  * A BF16 MLP 64 -> 128 -> 128 -> 1 (ReLU) scores each row of a matrix as the first

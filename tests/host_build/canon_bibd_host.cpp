@@ -31,9 +31,10 @@ extern "C" int emu_check(const uint64_t *rows, unsigned n, unsigned b, unsigned 
     aut[0] = o.aut_lo; aut[1] = o.aut_hi; *trials = o.trials;
     return 0;
 }
-// the lex-max search alone: canonical form into rows_out, |Aut| and node count
+// the lex-max search alone: canonical form into rows_out, |Aut|, node count and
+// the first rows of the labelings; prune selects the automorphism pruning
 extern "C" int emu_maxsearch(const uint64_t *rows, unsigned n, unsigned b, uint64_t *rows_out, uint64_t *leaves,
-                             uint64_t *nodes, uint8_t *improved) {
+                             uint64_t *nodes, uint8_t *improved, int prune, unsigned *first_rows) {
     static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
     static uint32_t s_vd[VMAX * TPB];
     static uint16_t s_cm[64 * TPB];
@@ -42,8 +43,10 @@ extern "C" int emu_maxsearch(const uint64_t *rows, unsigned n, unsigned b, uint6
     if (!load_rows(sm, rows, n, b, F_RAW))
         return -1;
     MaxOut mo;
-    max_search(sm, n, b, 1ull << 30, mo);
+    max_search(sm, n, b, 1ull << 30, mo, ID16, prune != 0);
     for (unsigned r = 0; r < n; ++r) rows_out[r] = R_(r);
     *leaves = mo.leaves; *nodes = mo.nodes; *improved = mo.improved;
+    if (first_rows)
+        *first_rows = mo.first_rows;
     return mo.timeout ? -2 : 0;
 }

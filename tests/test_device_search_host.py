@@ -80,21 +80,64 @@ def test_sts15_canonical_fixture_aut(host):
         assert e["canonical"] and e["aut"] == aut
 
 
+def maxsearch(L, rows, n, b, prune):
+    u64 = ctypes.c_uint64
+    rows = np.ascontiguousarray(rows, np.uint64)
+    out = np.zeros(n, np.uint64)
+    leaves, nodes, imp, fr = u64(), u64(), ctypes.c_uint8(), ctypes.c_uint()
+    rc = L.emu_maxsearch(rows.ctypes.data_as(ctypes.POINTER(u64)), n, b, out.ctypes.data_as(ctypes.POINTER(u64)),
+                         ctypes.byref(leaves), ctypes.byref(nodes), ctypes.byref(imp), int(prune), ctypes.byref(fr))
+    assert rc == 0
+    return dict(rows=out, aut=leaves.value, nodes=nodes.value, improved=bool(imp.value), first_rows=fr.value)
+
+
 def test_lex_max_search_gives_canonical_form(host):
     import ise_gb300 as G
     canon = {M.tobytes(): a for M, a in cases.load_sts15()}
-    u64 = ctypes.c_uint64
     for i in range(25):
         rows = oracle.sts_random_rows(15, 4242, i)
-        out = np.zeros(15, np.uint64)
-        leaves, nodes, imp = u64(), u64(), ctypes.c_uint8()
-        rc = host.emu_maxsearch(rows.ctypes.data_as(ctypes.POINTER(u64)), 15, 35,
-                                out.ctypes.data_as(ctypes.POINTER(u64)), ctypes.byref(leaves),
-                                ctypes.byref(nodes), ctypes.byref(imp))
-        assert rc == 0
-        C = G.unpack_rows(out, 35)
-        Co, ao, _ = oracle.bibd_canonize(oracle.rows_to_matrix(rows, 35))
-        assert np.array_equal(C, Co) and leaves.value == ao == canon[C.tobytes()]
+        for prune in (False, True):
+            r = maxsearch(host, rows, 15, 35, prune)
+            C = G.unpack_rows(r["rows"], 35)
+            Co, ao, _ = oracle.bibd_canonize(oracle.rows_to_matrix(rows, 35))
+            assert np.array_equal(C, Co) and r["aut"] == ao == canon[C.tobytes()]
+
+
+def _same_search_results(L, rows, n, b):
+    full = maxsearch(L, rows, n, b, False)
+    pruned = maxsearch(L, rows, n, b, True)
+    for k in ("aut", "improved", "first_rows"):
+        assert pruned[k] == full[k], (k, pruned[k], full[k])
+    assert np.array_equal(pruned["rows"], full["rows"])
+    assert pruned["nodes"] <= full["nodes"]
+    return full, pruned
+
+
+def test_automorphism_pruning_keeps_every_output(host):
+    """The pruned lex-max search gives the canonical form, |Aut|, the verdict and the
+    first-row orbit of the unpruned one, on canonical designs (large groups: up to
+    20160), their row/column-permuted copies and partial matrices of both."""
+    import ise_gb300 as G
+    rng = np.random.default_rng(5)
+    sts = cases.load_sts15()
+    ratio = {}
+    for M, aut in sts:
+        full, pruned = _same_search_results(host, G.pack_rows(M), 15, 35)
+        assert full["aut"] == aut and not full["improved"]
+        ratio[aut] = full["nodes"] / pruned["nodes"]
+        P = cases.permute_normalize(M, rng)
+        _same_search_results(host, G.pack_rows(P), 15, 35)
+        for k in (4, 7, 10, 13):
+            _same_search_results(host, G.pack_rows(oracle.bibd_normalize(P[:k])), k, 35)
+    assert ratio[20160] > 20          # PG(3,2): the pruned search visits far fewer nodes
+    for params in [(8, 14, 7, 4, 3), (11, 11, 5, 5, 2), (13, 26, 6, 3, 1), (9, 12, 4, 3, 1)]:
+        v, b = params[0], params[1]
+        for M, _ in cases.bibd_designs(*params):
+            _same_search_results(host, G.pack_rows(M), v, b)
+            for _ in range(3):
+                P = cases.permute_normalize(M, rng)
+                for k in range(2, v + 1):
+                    _same_search_results(host, G.pack_rows(oracle.bibd_normalize(P[:k])), k, b)
 
 
 def test_partial_prefixes(host):
