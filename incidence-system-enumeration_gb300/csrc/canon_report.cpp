@@ -105,9 +105,10 @@ size_t canon_report_bibd(uint32_t v, uint32_t b, uint32_t r, uint32_t k, uint32_
             e.second.ndt, e.second.nst);
     out += rule;
     add(out, "        Total:%16llu%16llu%16llu%16llu\n\n", total.nd, total.ns, total.ndt, total.nst);
-    add(out, "%10llu matrices constructed in %5.2f\n", total.nd, seconds);
-    add(out, "%10llu matrices have no replicated blocks\n", total.ns);
-    add(out, "%10llu matrices were fully constructed\n", (unsigned long long)fully_constructed);
+    const unsigned long long fc = (unsigned long long)fully_constructed;
+    add(out, "%10llu matri%s constructed in %5.2f\n", total.nd, total.nd == 1 ? "x" : "ces", seconds);
+    add(out, "%10llu matri%s no replicated blocks\n", total.ns, total.ns == 1 ? "x has" : "ces have");
+    add(out, "%10llu matri%s fully constructed\n", fc, fc == 1 ? "x was" : "ces were");
     return emit(out, buf, cap);
 }
 

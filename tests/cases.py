@@ -68,3 +68,49 @@ def ksys_relabel_random(R, rng):
             a, b = b, a
         lab[a], lab[b] = 2 * new_g, 2 * new_g + 1
     return ksys_sorted_form(lab[R])
+
+
+def load_result_tables():
+    import json
+    with open(os.path.join(GOLDEN, "bibd_result_tables.json")) as f:
+        return json.load(f)
+
+
+def simple_design(M):
+    """No replicated block: all columns distinct."""
+    cols = {bytes(M[:, c]) for c in range(M.shape[1])}
+    return len(cols) == M.shape[1]
+
+
+def oracle_transitive(M):
+    """Aut(D) transitive on the points, from the row automorphisms that the oracle's
+    TestCanonicity stores (union of their cycles)."""
+    o = oracle.bibd_test(M, oracle.SAVE_ROW_PERM | oracle.SAVE_AUT_ROWS, perm_cap=1 << 14)
+    assert o["canonical"] and not o["perm_overflow"]
+    v = M.shape[0]
+    parent = list(range(v))
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    for p in o["perms"]:
+        for i in range(v):
+            a, b = find(i), find(int(p[i]))
+            if a != b:
+                parent[max(a, b)] = min(a, b)
+    return len({find(i) for i in range(v)}) == 1
+
+
+def table_rows(designs, simple, transitive):
+    """[[|Aut|, Nd, Ns, Ndt, Nst], ...] by increasing |Aut|, as the reference counts them."""
+    rows = {}
+    for (_, aut), s, t in zip(designs, simple, transitive):
+        r = rows.setdefault(aut, [aut, 0, 0, 0, 0])
+        r[1] += 1
+        r[2] += bool(s)
+        r[3] += bool(t)
+        r[4] += bool(s and t)
+    return [rows[a] for a in sorted(rows)]

@@ -9,6 +9,11 @@ reference tree; the GPU machine never runs this).
   sts15_canonical.txt   the 80 canonical STS(15) (one per isomorphism class) as
                         built by the oracle's orderly enumeration; pinned by the
                         reference's STS(15) |Aut| histogram (checked here)
+  bibd_result_tables.json  the |Aut(D)| tables (Nd, Ns, Ndt, Nst per group order,
+                        totals) of every BIBD result file with v <= 16 and
+                        b <= 63, and for files in the current layout the exact
+                        text from the BIBD( line to the "fully constructed" line
+  k10_results_table.txt the |Aut(M)| x cycles table of K_Results.txt for K10
 
 Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT]
 """
@@ -57,6 +62,51 @@ def parse_k10(path):
     return out
 
 
+def parse_bibd_table(path):
+    lines = open(path, encoding="latin-1").read().splitlines()
+    t = next(i for i, l in enumerate(lines) if l.startswith("BIBD("))
+    h = next(i for i, l in enumerate(lines) if "|Aut(D)|" in l)
+    rows, i = [], h + 2
+    while not lines[i].strip().startswith("_"):
+        rows.append([int(x) for x in lines[i].split()[:5]])
+        i += 1
+    entry = dict(rows=rows, total=[int(x) for x in lines[i + 1].split()[1:5]],
+                 wide="Nd:             Ns:" in lines[h])
+    if entry["wide"]:
+        end = next(j for j in range(i, len(lines)) if "fully constructed" in lines[j])
+        entry["text"] = "\n".join(lines[t:end + 1]) + "\n"
+        secs = next(l for l in lines[i:end] if "constructed in" in l)
+        entry["seconds"] = float(re.search(r"constructed in\s+([\d.]+)", secs).group(1))
+        entry["fully_constructed"] = int(lines[end].split()[0])
+    return entry
+
+
+def bibd_result_tables(ref):
+    tables = {}
+    base = os.path.join(ref, "Results", "BIBDs")
+    for d in sorted(os.listdir(base)):
+        if not d.startswith("V ="):
+            continue
+        for f in sorted(os.listdir(os.path.join(base, d))):
+            m = re.fullmatch(r"(\d+)_(\d+)_(\d+)\.txt", f)
+            if not m:
+                continue
+            path = os.path.join(base, d, f)
+            text = open(path, encoding="latin-1").read()
+            title = next(l for l in text.splitlines() if l.startswith("BIBD("))
+            v, b, r, k, lam = map(int, re.findall(r"\d+", title)[:5])
+            if v <= 16 and b <= 63 and "|Aut(D)|" in text:      # runs that finished
+                tables["%d,%d,%d,%d,%d" % (v, b, r, k, lam)] = parse_bibd_table(path)
+    return tables
+
+
+def k10_results_table(path):
+    lines = open(path, encoding="latin-1").read().splitlines()
+    t = next(i for i, l in enumerate(lines) if "Factorization of K(10)" in l)
+    end = next(i for i in range(t, len(lines)) if "Total:" in lines[i]) + 1
+    return "\n".join(lines[t:end + 1]) + "\n\n\n"
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     hists = {}
@@ -73,6 +123,12 @@ def main():
         f.write("# 396 canonical 1-factorizations of K10: |Aut| then 9 rounds of 10 players\n")
         for aut, rows in k10:
             f.write("%d %s\n" % (aut, " | ".join(rows)))
+
+    with open(os.path.join(HERE, "bibd_result_tables.json"), "w") as f:
+        json.dump(bibd_result_tables(ref), f, indent=1, sort_keys=True)
+    kdir = os.path.join(ref, "k-Factorization", "Results", "Complete_graphs", "10", "10x9x2")
+    with open(os.path.join(HERE, "k10_results_table.txt"), "w") as f:
+        f.write(k10_results_table(os.path.join(kdir, "K_Results.txt")))
 
     import oracle  # noqa: E402  (CPU oracle, test infrastructure)
     found, _ = oracle.bibd_enumerate(15, 35, 7, 3, 1)

@@ -50,3 +50,40 @@ def test_small_complete_graphs(ctx):
     f8, _ = ctx.enumerate_ksys(8)
     ref8, _ = oracle.ksys_enumerate(8)
     assert {R.tobytes(): a for R, a in f8} == {R.tobytes(): a for R, a in ref8}
+
+
+TABLES = cases.load_result_tables()
+TABLE_KEYS = ["6,10,5,3,2", "6,20,10,3,4", "6,30,15,3,6", "6,40,20,3,8", "6,50,25,3,10", "6,60,30,3,12",
+              "7,7,3,3,1", "7,14,6,3,2", "7,21,9,3,3", "7,28,12,3,4", "7,35,15,3,5", "7,42,18,3,6",
+              "8,14,7,4,3", "8,28,14,4,6", "9,12,4,3,1", "9,18,8,4,3", "9,24,8,3,2", "10,15,6,4,2",
+              "10,18,9,5,4", "10,30,9,3,2", "11,11,5,5,2", "13,13,4,4,1", "13,26,6,3,1", "15,15,7,7,3",
+              "15,35,7,3,1", "16,16,6,6,2", "16,20,5,4,1"]
+
+
+@pytest.mark.parametrize("key", TABLE_KEYS)
+def test_bibd_result_table(ctx, key):
+    """Enumeration, |Aut|, simplicity and point-transitivity all on the GPU give the
+    reference's |Aut(D)| table (Nd / Ns / Ndt / Nst per group order); for result
+    files in the current layout the whole text block, run time and the
+    reference's fully-constructed count passed through."""
+    import re
+    import ise_gb300 as G
+    ref = TABLES[key]
+    params = tuple(map(int, key.split(",")))
+    found, st = ctx.enumerate_bibd(*params)
+    simple, trans = ctx.design_properties([M for M, _ in found])
+    assert cases.table_rows(found, simple, trans) == ref["rows"]
+    text = G.report_bibd(params, [a for _, a in found], simple, trans,
+                         fully_constructed=ref.get("fully_constructed", 0), seconds=ref.get("seconds", 0.0))
+    if ref["wide"]:
+        norm = lambda t: re.sub(r"constructed in +", "constructed in ", t)
+        assert norm(text) == norm(ref["text"])
+    assert st.level_checks[params[0] - 1] > 0
+
+
+def test_k10_results_table(ctx):
+    import ise_gb300 as G
+    found, _ = ctx.enumerate_ksys(10)
+    text = G.report_ksys([R for R, _ in found], [a for _, a in found])
+    with open(os.path.join(cases.GOLDEN, "k10_results_table.txt")) as f:
+        assert text == f.read()
