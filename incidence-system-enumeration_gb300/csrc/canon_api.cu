@@ -15,42 +15,11 @@
 
 #include "../../include/canon_gb300.h"
 #include "canon_internal.h"
+#include "canon_ctx.h"
 
 using canon::Item;
 using canon::Outputs;
 
-struct canon_ctx {
-    int device = 0;
-    int num_sms = 0;
-    canon_cfg cfg{};
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // queued host input (pinned)
-    Item *h_bitems = nullptr, *h_kitems = nullptr;
-    uint64_t *h_words = nullptr;
-    uint8_t *h_bytes = nullptr;
-    uint32_t n_bitems = 0, n_kitems = 0, n_words = 0, n_bytes = 0;
-    uint32_t max_bytes = 0;
-    // device buffers
-    Item *d_bitems = nullptr, *d_kitems = nullptr;
-    uint64_t *d_words = nullptr;
-    uint8_t *d_bytes = nullptr;
-    unsigned *d_ticket = nullptr;      // work-stealing counters (2 words)
-    Outputs d_out{}, h_out{};
-    std::vector<uint8_t> item_kind;   // per out_idx
-    // learned order: installed weights (device) and lazily grown scratch
-    bool order_on = false;
-    float *d_mlp = nullptr;            // flat FP32 parameters (canon::mlp::N_PARAMS)
-    uint16_t *d_w1 = nullptr, *d_w2 = nullptr, *d_w2t = nullptr, *d_w3 = nullptr;   // BF16 copies
-    float *d_adam_m = nullptr, *d_adam_v = nullptr, *d_grad = nullptr, *d_loss = nullptr;
-    void *d_scratch = nullptr;
-    size_t scratch_bytes = 0;
-    uint64_t *d_orders = nullptr;
-    size_t d_orders_bytes = 0;
-    std::string err;
-    float last_ms = 0.f;
-    uint64_t launches = 0;
-};
 
 namespace {
 
@@ -308,7 +277,7 @@ int canon_submit_bibd(canon_ctx *c, const canon_bibd_batch *bt) {
         return CANON_OK;
     if (!bt->rows || bt->v < 1 || bt->v > canon::VMAX || bt->b < 1 || bt->b > canon::BMAX)
         return fail(c, CANON_EINVAL, "bibd batch: need rows, 1 <= v <= 16, 1 <= b <= 63");
-    if (bt->flags & ~0x3Fu)
+    if (bt->flags & ~0x7Fu)
         return fail(c, CANON_EINVAL, "bibd batch: unknown flags");
     const uint32_t total = c->n_bitems + c->n_kitems;
     if ((uint64_t)total + bt->n > c->cfg.max_items)
@@ -859,7 +828,7 @@ int canon_check_bibd_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                              void *stream) {
     if (n > CANON_NOALLOC_MAX_ITEMS)
         return CANON_ESIZE;
-    if (!out || !d_rows || v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x3Fu))
+    if (!out || !d_rows || v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x7Fu))
         return CANON_EINVAL;
     if (!out->canonical || !out->status || !out->reject_row || !out->row_to_change || !out->player_index ||
         !out->witness || !out->aut || !out->trials || !out->n_auts || !out->len_aut)

@@ -902,6 +902,10 @@ __device__ void check_one(Smem sm, const uint64_t *src, unsigned n, unsigned b, 
             max_search(sm, n, b, max_trials, mo, order0, true, !aut_always);
             if (mo.timeout) {
                 o.status = ST_TIMEOUT;
+            } else if (mo.improved && (flags & F_VERDICT_ONLY)) {
+                o.canonical = 0;
+                o.aut_lo = aut_always ? mo.leaves : 0;
+                o.aut_hi = 0;
             } else if (mo.improved) {
                 // non-canonical, rejected late in the reference order: find its witness
                 load_rows(sm, src, n, b, flags);

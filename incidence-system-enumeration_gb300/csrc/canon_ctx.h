@@ -1,0 +1,40 @@
+// canon_ctx.h -- the context behind the C ABI's opaque canon_ctx handle.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/canon_gb300.h"
+#include "canon_internal.h"
+
+struct canon_ctx {
+    int device = 0;
+    int num_sms = 0;
+    canon_cfg cfg{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // queued host input (pinned)
+    canon::Item *h_bitems = nullptr, *h_kitems = nullptr;
+    uint64_t *h_words = nullptr;
+    uint8_t *h_bytes = nullptr;
+    uint32_t n_bitems = 0, n_kitems = 0, n_words = 0, n_bytes = 0;
+    uint32_t max_bytes = 0;
+    // device buffers
+    canon::Item *d_bitems = nullptr, *d_kitems = nullptr;
+    uint64_t *d_words = nullptr;
+    uint8_t *d_bytes = nullptr;
+    unsigned *d_ticket = nullptr;      // work-stealing counters (2 words)
+    canon::Outputs d_out{}, h_out{};
+    std::vector<uint8_t> item_kind;   // per out_idx
+    // learned order: installed weights (device) and lazily grown scratch
+    bool order_on = false;
+    float *d_mlp = nullptr;            // flat FP32 parameters (canon::mlp::N_PARAMS)
+    uint16_t *d_w1 = nullptr, *d_w2 = nullptr, *d_w2t = nullptr, *d_w3 = nullptr;   // BF16 copies
+    float *d_adam_m = nullptr, *d_adam_v = nullptr, *d_grad = nullptr, *d_loss = nullptr;
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint64_t *d_orders = nullptr;
+    size_t d_orders_bytes = 0;
+    std::string err;
+    float last_ms = 0.f;
+    uint64_t launches = 0;
+};

@@ -1,12 +1,12 @@
-// canon_enum.cpp -- frontier-batched orderly enumeration on top of the GPU check.
+// canon_enum.cpp -- frontier-batched orderly enumeration of k-systems on top of
+// the GPU check (the BIBD enumerator keeps its levels on the GPU: canon_levels.cu).
 //
 // The reference enumerates depth-first and checks one partial matrix at a time
-// (CEnumerator::Enumerate, Source/Enumerator.cpp:540-1024, check at :446-447 and
-// :364; alldata::Run, k-Factorization/TripleSys/Source/TripleSys.cpp:80-775, check
-// at checkCurrentResult.cpp:91).  Here the search runs level by level: every
-// canonical partial matrix of level n is extended by all admissible next rows on
-// the host, the whole level is checked in batches on the GPU, and the canonical
-// ones form level n+1.  Orderly generation makes the result independent of the
+// (alldata::Run, k-Factorization/TripleSys/Source/TripleSys.cpp:80-775, check at
+// checkCurrentResult.cpp:91).  Here the search runs level by level: every
+// canonical partial matrix of level n is extended by all admissible next rounds
+// on the host, the whole level is checked in batches on the GPU, and the
+// canonical ones form level n+1.  Orderly generation makes the result independent of the
 // visiting order: every prefix of a canonical matrix is canonical, so the set of
 // canonical complete matrices is the same as the depth-first search finds.
 #include <chrono>
@@ -26,103 +26,6 @@ struct Timer {
     std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
     double seconds() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    }
-};
-
-// ---- BIBD rows -------------------------------------------------------------
-// The next row is chosen as a number of 1s per column orbit (the row solutions of
-// CRowSolution / CInSysSolver): r ones in total, lambda in common with every row
-// above, no column above k, and columns that need all remaining rows forced.
-struct BibdGen {
-    int v, b, r, k, lambda;
-    const uint64_t *rows;     // the n rows of the parent
-    int n;
-    int norb;
-    int start[64], len[64], weight[64];
-    uint64_t onesmask[64];    // bit i: row i has 1s in this orbit
-    int x[64];
-    int lam_left[16];
-    std::vector<uint64_t> *out;
-
-    void emit() {
-        uint64_t row = 0;
-        for (int q = 0; q < norb; ++q)
-            if (x[q])
-                row |= ((1ull << x[q]) - 1ull) << start[q];
-        out->insert(out->end(), rows, rows + n);
-        out->push_back(row);
-    }
-    void rec(int q, int left) {
-        if (q == norb) {
-            if (left)
-                return;
-            for (int i = 0; i < n; ++i)
-                if (lam_left[i])
-                    return;
-            emit();
-            return;
-        }
-        // capacity left in the orbits after q bounds the choice
-        int cap_after = 0;
-        for (int t = q + 1; t < norb; ++t)
-            cap_after += (weight[t] < k) ? len[t] : 0;
-        const int rem_rows = v - n - 1;
-        int minx = (k - weight[q] > rem_rows) ? len[q] : 0;
-        int maxx = (weight[q] >= k) ? 0 : len[q];
-        if (maxx > left)
-            maxx = left;
-        if (minx < left - cap_after)
-            minx = left - cap_after;
-        for (int xv = maxx; xv >= minx; --xv) {
-            bool ok = true;
-            for (int i = 0; i < n; ++i)
-                if (((onesmask[q] >> i) & 1u) && lam_left[i] < xv) {
-                    ok = false;
-                    break;
-                }
-            if (!ok)
-                continue;
-            for (int i = 0; i < n; ++i)
-                if ((onesmask[q] >> i) & 1u)
-                    lam_left[i] -= xv;
-            x[q] = xv;
-            rec(q + 1, left - xv);
-            for (int i = 0; i < n; ++i)
-                if ((onesmask[q] >> i) & 1u)
-                    lam_left[i] += xv;
-        }
-    }
-    void children(const uint64_t *parent, int nrows, std::vector<uint64_t> &dst) {
-        rows = parent;
-        n = nrows;
-        out = &dst;
-        // orbits of level n: runs of columns equal in rows 0..n-1
-        norb = 0;
-        int s = 0;
-        for (int c = 1; c <= b; ++c) {
-            bool same = c < b;
-            for (int i = 0; same && i < n; ++i)
-                if (((rows[i] >> c) & 1u) != ((rows[i] >> (c - 1)) & 1u))
-                    same = false;
-            if (!same) {
-                start[norb] = s;
-                len[norb] = c - s;
-                int w = 0;
-                uint64_t om = 0;
-                for (int i = 0; i < n; ++i)
-                    if ((rows[i] >> s) & 1u) {
-                        ++w;
-                        om |= 1ull << i;
-                    }
-                weight[norb] = w;
-                onesmask[norb] = om;
-                ++norb;
-                s = c;
-            }
-        }
-        for (int i = 0; i < n; ++i)
-            lam_left[i] = lambda;
-        rec(0, r);
     }
 };
 
@@ -207,68 +110,6 @@ void level_children(const Gen &proto, const std::vector<T> &level, size_t stride
 
 extern "C" {
 
-int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uint32_t k, uint32_t lambda,
-                         canon_design_cb cb, void *user, canon_enum_stats *stats) {
-    if (!ctx || v < 2 || v > 16 || b < 1 || b > 63 || r < 1 || r > b || k < 1 || k > v)
-        return CANON_EINVAL;
-    Timer t;
-    canon_enum_stats st{};
-    // row 0 is forced: r ones first
-    std::vector<uint64_t> level = {(1ull << r) - 1ull};
-    int n = 1;
-    BibdGen gen{};
-    gen.v = (int)v;
-    gen.b = (int)b;
-    gen.r = (int)r;
-    gen.k = (int)k;
-    gen.lambda = (int)lambda;
-    const uint32_t chunk = canon::batch_capacity(ctx, v, 0);
-    if (!chunk)
-        return CANON_ENOMEM;
-    while (n < (int)v && !level.empty()) {
-        std::vector<uint64_t> cand;
-        level_children(gen, level, (size_t)n, n, cand);
-        const int m = n + 1;
-        const size_t count = cand.size() / m;
-        const bool complete = m == (int)v;
-        std::vector<uint64_t> next;
-        for (size_t off = 0; off < count; off += chunk) {
-            const uint32_t cnt = (uint32_t)((count - off < chunk) ? count - off : chunk);
-            canon_bibd_batch bt{cnt, (uint32_t)m, b, complete ? CANON_COMPLETE : 0u, cand.data() + off * m, nullptr};
-            int rc = canon_submit_bibd(ctx, &bt);
-            canon_results res{};
-            if (rc == CANON_OK)
-                rc = canon_sync(ctx, &res);
-            if (rc != CANON_OK)
-                return rc;
-            st.checks += cnt;
-            st.kernel_ms += res.kernel_ms;
-            st.level_checks[m - 1] += cnt;
-            st.level_kernel_ms[m - 1] += res.kernel_ms;
-            ++st.batches;
-            for (uint32_t i = 0; i < cnt; ++i) {
-                if (!res.canonical[i])
-                    continue;
-                const uint64_t *rowsp = cand.data() + (off + i) * m;
-                if (complete) {
-                    ++st.designs;
-                    if (cb)
-                        cb(user, (const uint8_t *)rowsp, v, b, res.aut[2 * i], res.aut[2 * i + 1]);
-                } else {
-                    next.insert(next.end(), rowsp, rowsp + m);
-                }
-            }
-        }
-        level.swap(next);
-        n = m;
-        ++st.levels;
-    }
-    st.seconds = t.seconds();
-    if (stats)
-        *stats = st;
-    return CANON_OK;
-}
-
 int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *user, canon_enum_stats *stats) {
     if (!ctx || np < 4 || np > 12 || (np & 1u))
         return CANON_EINVAL;
@@ -286,7 +127,9 @@ int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *
     const int rounds = (int)np - 1;
     while (n < rounds && !level.empty()) {
         std::vector<uint8_t> cand;
+        Timer tg;
         level_children(gen, level, (size_t)n * np, n, cand);
+        st.gen_seconds += tg.seconds();
         const int m = n + 1;
         const size_t count = cand.size() / (m * np);
         std::vector<uint8_t> next;

@@ -42,7 +42,7 @@ struct Outputs {
 
 // flags (same values as the public CANON_* flags)
 constexpr uint32_t F_COMPLETE = 0x1, F_RAW = 0x2, F_FULL_AUT = 0x4, F_SAVE_AUTS = 0x8, F_AUT_CANON = 0x10,
-                   F_REFERENCE_ORDER = 0x20;
+                   F_REFERENCE_ORDER = 0x20, F_VERDICT_ONLY = 0x40;
 constexpr uint8_t ST_BADINPUT = 1, ST_TIMEOUT = 2, ST_PERM_OVF = 4;
 
 // launchers (stream-ordered; return cudaGetLastError())

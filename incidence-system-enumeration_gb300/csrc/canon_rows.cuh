@@ -1,0 +1,180 @@
+// canon_rows.cuh -- the admissible next rows of a partial BIBD incidence matrix,
+// as host and device code (the device enumerator runs it one thread per parent;
+// a host build of the same code is tested against the oracle's enumeration).
+//
+// The next row is chosen as a number of 1s per column orbit of the parent (the
+// row solutions that CRowSolution / CInSysSolver enumerate, Source/RowSolution.h,
+// Source/InSysSolver.h): r ones in total, lambda in common with every row above,
+// no column above k, columns that need every remaining row forced to 1, and the
+// row not greater than the row above it (a canonical matrix has non-increasing
+// rows: a greater row n would win by swapping it with row n-1).  Inside each
+// orbit the 1s come first, so every child is again in orbit normal form.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define CANON_HD __host__ __device__
+#else
+#define CANON_HD
+#endif
+
+namespace canon {
+namespace rows {
+
+struct Params {
+    int v, b, r, k, lambda;
+};
+
+// Children of one parent with n rows (bit c of word i = row i, column c), in a
+// fixed order: orbits left to right, more 1s first.  EMIT: child j is written to
+// out[j*(n+1) .. j*(n+1)+n] (the parent's rows, then the new row) for j < out_cap.
+// Returns the number of children.
+template <bool EMIT>
+CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint64_t *out, uint32_t out_cap) {
+    const int b = d.b, k = d.k;
+    uint8_t start[64], len[64], weight[64];
+    uint16_t ones[64];
+    int norb = 0;
+    int s = 0;
+    for (int c = 1; c <= b; ++c) {
+        bool same = c < b;
+        for (int i = 0; same && i < n; ++i)
+            if (((parent[i] >> c) & 1u) != ((parent[i] >> (c - 1)) & 1u))
+                same = false;
+        if (!same) {
+            start[norb] = (uint8_t)s;
+            len[norb] = (uint8_t)(c - s);
+            int w = 0;
+            unsigned om = 0;
+            for (int i = 0; i < n; ++i)
+                if ((parent[i] >> s) & 1u) {
+                    ++w;
+                    om |= 1u << i;
+                }
+            weight[norb] = (uint8_t)w;
+            ones[norb] = (uint16_t)om;
+            ++norb;
+            s = c;
+        }
+    }
+    // hi/lo: the most / least 1s orbit q can take (full orbits none, orbits whose
+    // columns need every remaining row all); cap/need: suffix sums of hi/lo over
+    // the orbits that meet row i, so a row whose lambda can no longer be met ends
+    // the branch at once
+    const int rem_rows = d.v - n - 1;
+    uint8_t hi[64], lo[64];
+    uint8_t cap[65][16], need[65][16], cap_all[65], need_all[65];
+    for (int i = 0; i < n; ++i)
+        cap[norb][i] = need[norb][i] = 0;
+    cap_all[norb] = need_all[norb] = 0;
+    for (int q = norb - 1; q >= 0; --q) {
+        hi[q] = (weight[q] >= k) ? 0 : len[q];
+        lo[q] = (k - weight[q] > rem_rows) ? len[q] : 0;
+        cap_all[q] = (uint8_t)(cap_all[q + 1] + hi[q]);
+        need_all[q] = (uint8_t)(need_all[q + 1] + lo[q]);
+        for (int i = 0; i < n; ++i) {
+            const bool in = (ones[q] >> i) & 1u;
+            cap[q][i] = (uint8_t)(cap[q + 1][i] + (in ? hi[q] : 0));
+            need[q][i] = (uint8_t)(need[q + 1][i] + (in ? lo[q] : 0));
+        }
+    }
+    int lam[16];
+    for (int i = 0; i < n; ++i)
+        lam[i] = d.lambda;
+    // iterative depth-first search over the orbits: x[q] the 1s given to orbit q,
+    // nxt[q] the next value to try, left[q] the 1s still to place before orbit q,
+    // tied bit q: the row equals row n-1 on the orbits before q
+    uint8_t x[64], nxt[64], mn[64], left[65];
+    uint64_t tied = 1;
+    uint32_t count = 0;
+    int q = 0;
+    left[0] = (uint8_t)d.r;
+    bool enter = true;
+    for (;;) {
+        if (enter) {
+            if (q == norb) {
+                bool ok = left[q] == 0;
+                for (int i = 0; ok && i < n; ++i)
+                    ok = lam[i] == 0;
+                if (ok) {
+                    if (EMIT && count < out_cap) {
+                        uint64_t row = 0;
+                        for (int t = 0; t < norb; ++t)
+                            if (x[t])
+                                row |= ((1ull << x[t]) - 1ull) << start[t];
+                        uint64_t *dst = out + (size_t)count * (n + 1);
+                        for (int i = 0; i < n; ++i)
+                            dst[i] = parent[i];
+                        dst[n] = row;
+                    }
+                    ++count;
+                }
+                if (q == 0)
+                    break;
+                --q;
+                enter = false;
+                continue;
+            }
+            const int lf = left[q];
+            int minx = lo[q], maxx = hi[q];
+            if (maxx > lf)
+                maxx = lf;
+            if (minx < lf - cap_all[q + 1])
+                minx = lf - cap_all[q + 1];
+            if (maxx > lf - need_all[q + 1])
+                maxx = lf - need_all[q + 1];
+            if (((tied >> q) & 1u) && !((ones[q] >> (n - 1)) & 1u) && maxx > 0)
+                maxx = 0;
+            mn[q] = (uint8_t)(minx < 0 ? 0 : minx);
+            nxt[q] = (uint8_t)(maxx + 1);          // values maxx .. minx, tried downwards
+            x[q] = 0xFF;                           // nothing applied yet
+            if (maxx < minx)
+                nxt[q] = mn[q];                    // empty range
+        }
+        // undo the value applied at level q, then try the next one
+        if (x[q] != 0xFF) {
+            for (int i = 0; i < n; ++i)
+                if ((ones[q] >> i) & 1u)
+                    lam[i] += x[q];
+            x[q] = 0xFF;
+        }
+        bool moved = false;
+        while (nxt[q] > mn[q]) {
+            const int xv = --nxt[q];
+            bool ok = true;
+            for (int i = 0; i < n && ok; ++i) {
+                const int l = lam[i] - (((ones[q] >> i) & 1u) ? xv : 0);
+                ok = l >= need[q + 1][i] && l <= cap[q + 1][i];
+            }
+            if (!ok)
+                continue;
+            for (int i = 0; i < n; ++i)
+                if ((ones[q] >> i) & 1u)
+                    lam[i] -= xv;
+            x[q] = (uint8_t)xv;
+            left[q + 1] = (uint8_t)(left[q] - xv);
+            // still equal to row n-1: its value on the orbit taken everywhere
+            const bool prev1 = (ones[q] >> (n - 1)) & 1u;
+            if (((tied >> q) & 1u) && xv == (prev1 ? len[q] : 0))
+                tied |= 1ull << (q + 1);
+            else
+                tied &= ~(1ull << (q + 1));
+            moved = true;
+            break;
+        }
+        if (moved) {
+            ++q;
+            enter = true;
+            continue;
+        }
+        if (q == 0)
+            break;
+        --q;
+        enter = false;
+    }
+    return count;
+}
+
+}  // namespace rows
+}  // namespace canon

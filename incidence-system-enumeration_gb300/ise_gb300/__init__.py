@@ -42,6 +42,7 @@ FULL_AUT = 0x4
 SAVE_AUTS = 0x8
 AUT_CANON = 0x10
 REFERENCE_ORDER = 0x20
+VERDICT_ONLY = 0x40
 
 # t_canonOutInfo of the reference (Source/CanonicityChecker.h:27-32)
 t_saveNothing = 0
@@ -97,7 +98,8 @@ class DeviceOutputs(ctypes.Structure):
 class EnumStats(ctypes.Structure):
     _fields_ = [("checks", ctypes.c_uint64), ("designs", ctypes.c_uint64), ("levels", ctypes.c_uint32),
                 ("batches", ctypes.c_uint32), ("seconds", ctypes.c_double), ("kernel_ms", ctypes.c_double),
-                ("level_checks", ctypes.c_uint64 * 16), ("level_kernel_ms", ctypes.c_double * 16)]
+                ("level_checks", ctypes.c_uint64 * 16), ("level_kernel_ms", ctypes.c_double * 16),
+                ("gen_seconds", ctypes.c_double)]
 
 
 DESIGN_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint32,

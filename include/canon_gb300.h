@@ -80,6 +80,12 @@ extern "C" {
  * and only the witness is taken from the reference order: every output except
  * `trials` is identical, and the check is several times faster. */
 #define CANON_REFERENCE_ORDER 0x20u
+/* Only the canonical flag (and |Aut| of canonical matrices) is wanted, as in an
+ * enumerator that keeps the canonical matrices of a level: a matrix that the
+ * lex-max search rejects gets no witness search, so witness, reject_row and
+ * row_to_change are undefined for it (trials counts the short search only).
+ * Ignored with CANON_SAVE_AUTS or CANON_REFERENCE_ORDER. */
+#define CANON_VERDICT_ONLY 0x40u
 
 /* ---- context ---- */
 typedef struct canon_ctx canon_ctx;
@@ -202,6 +208,7 @@ typedef struct {
      * level_checks[v-1] counts the complete matrices constructed */
     uint64_t level_checks[16];
     double   level_kernel_ms[16];
+    double   gen_seconds; /* host time spent generating the candidates */
 } canon_enum_stats;
 
 /* Called for every canonical complete matrix: BIBD rows as rows x uint64 (cast to

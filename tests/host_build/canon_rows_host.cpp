@@ -1,0 +1,10 @@
+// The device enumerator's row generator (canon_rows.cuh) compiled for the host.
+#include "../../incidence-system-enumeration_gb300/csrc/canon_rows.cuh"
+
+extern "C" uint32_t rows_children(int v, int b, int r, int k, int lambda, const uint64_t *parent, int n,
+                                  uint64_t *out, uint32_t cap) {
+    const canon::rows::Params d{v, b, r, k, lambda};
+    if (!out)
+        return canon::rows::children<false>(d, parent, n, nullptr, 0);
+    return canon::rows::children<true>(d, parent, n, out, cap);
+}

@@ -1,0 +1,83 @@
+"""The device enumerator's row generator (canon_rows.cuh), compiled for the host and
+driven level by level with the oracle as the checker: it must give the oracle's
+depth-first enumeration (designs and |Aut|) and the reference's result tables."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import cases
+import conftest
+import oracle
+
+SRC = os.path.join(conftest.REPO, "tests", "host_build", "canon_rows_host.cpp")
+OUT = os.path.join(conftest.REPO, "tests", "host_build", "_build", "libcanon_rows_host.so")
+FAMILIES = ["7,7,3,3,1", "7,14,6,3,2", "6,30,15,3,6", "8,14,7,4,3", "9,12,4,3,1", "9,18,8,4,3",
+            "10,15,6,4,2", "11,11,5,5,2", "13,13,4,4,1", "13,26,6,3,1", "16,20,5,4,1"]
+
+
+@pytest.fixture(scope="module")
+def gen():
+    os.makedirs(os.path.dirname(OUT), exist_ok=True)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", SRC, "-o", OUT], check=True)
+    L = ctypes.CDLL(OUT)
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    L.rows_children.argtypes = [ctypes.c_int] * 5 + [u64p, ctypes.c_int, u64p, ctypes.c_uint32]
+    L.rows_children.restype = ctypes.c_uint32
+    return L
+
+
+def children(L, params, parent):
+    n = len(parent)
+    p = np.ascontiguousarray(parent, np.uint64)
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    cnt = L.rows_children(*params, p.ctypes.data_as(u64p), n, None, 0)
+    out = np.zeros(max(cnt, 1) * (n + 1), np.uint64)
+    assert L.rows_children(*params, p.ctypes.data_as(u64p), n, out.ctypes.data_as(u64p), cnt) == cnt
+    return out[: cnt * (n + 1)].reshape(cnt, n + 1)
+
+
+def unpack(words, b):
+    return ((np.asarray(words, np.uint64)[:, None] >> np.arange(b, dtype=np.uint64)) & 1).astype(np.uint8)
+
+
+@pytest.mark.parametrize("key", FAMILIES)
+def test_level_enumeration_equals_oracle(gen, key):
+    params = tuple(map(int, key.split(",")))
+    v, b, r = params[:3]
+    level = [np.array([(1 << r) - 1], np.uint64)]
+    for m in range(2, v + 1):
+        nxt = []
+        for parent in level:
+            for child in children(gen, params, parent):
+                M = unpack(child, b)
+                flags = (oracle.SAVE_ROW_PERM | oracle.SAVE_ROW_TO_CHANGE) if m == v else 0
+                o = oracle.bibd_test(M, flags)
+                if o["canonical"]:
+                    nxt.append((child, o["aut"]))
+        level = [c for c, _ in nxt]
+    got = {unpack(c, b).tobytes(): a for c, a in nxt}
+    ref, _ = oracle.bibd_enumerate(*params)
+    assert got == {M.tobytes(): a for M, a in ref}
+    tab = cases.load_result_tables()[key]
+    designs = [(unpack(c, b), a) for c, a in nxt]
+    assert cases.table_rows(designs, [cases.simple_design(M) for M, _ in designs],
+                            [cases.oracle_transitive(M) for M, _ in designs]) == tab["rows"]
+
+
+def test_children_are_normal_and_non_increasing(gen):
+    """Every child is in orbit normal form and its new row is not greater than the
+    row above it (read column 0 first)."""
+    params = (15, 35, 7, 3, 1)
+    rng = np.random.default_rng(3)
+    sts = cases.load_sts15()
+    for M, _ in sts[::9]:
+        P = cases.permute_normalize(M, rng)
+        for k in (3, 6, 9):
+            parent = np.array([int("".join(str(x) for x in row[::-1]), 2) for row in P[:k]], np.uint64)
+            for child in children(gen, params, parent):
+                C = unpack(child, 35)
+                assert oracle.bibd_is_normal(C)
+                assert tuple(C[-1]) <= tuple(C[-2])
