@@ -5,10 +5,12 @@
 // The next row is chosen as a number of 1s per column orbit of the parent (the
 // row solutions that CRowSolution / CInSysSolver enumerate, Source/RowSolution.h,
 // Source/InSysSolver.h): r ones in total, lambda in common with every row above,
-// no column above k, columns that need every remaining row forced to 1, and the
-// row not greater than the row above it (a canonical matrix has non-increasing
-// rows: a greater row n would win by swapping it with row n-1).  Inside each
-// orbit the 1s come first, so every child is again in orbit normal form.
+// no column above k, columns that need every remaining row forced to 1, and no
+// earlier row i that the new row beats after a swap: exchanging rows i and n and
+// moving the new row's 1s first inside every column orbit of rows 0..i-1 leaves
+// rows 0..i-1 as they are, so a greater row i there means a greater matrix and
+// the child is not canonical.  Inside each orbit the 1s come first, so every
+// child is again in orbit normal form.
 #pragma once
 #include <cstddef>
 #include <cstdint>
@@ -34,6 +36,7 @@ template <bool EMIT>
 CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint64_t *out, uint32_t out_cap) {
     const int b = d.b, k = d.k;
     uint8_t start[64], len[64], weight[64];
+    uint8_t split[64];      // the first row in which orbit q differs from orbit q-1
     uint16_t ones[64];
     int norb = 0;
     int s = 0;
@@ -43,6 +46,10 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
             if (((parent[i] >> c) & 1u) != ((parent[i] >> (c - 1)) & 1u))
                 same = false;
         if (!same) {
+            int first = 0;
+            while (norb && first < n && ((parent[first] >> s) & 1u) == ((parent[first] >> (s - 1)) & 1u))
+                ++first;
+            split[norb] = (uint8_t)first;
             start[norb] = (uint8_t)s;
             len[norb] = (uint8_t)(c - s);
             int w = 0;
@@ -97,6 +104,22 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
                 bool ok = left[q] == 0;
                 for (int i = 0; ok && i < n; ++i)
                     ok = lam[i] == 0;
+                // the swap test against every row i >= 1 (the orbits of level i are
+                // runs of orbits not split by rows 0..i-1; row 0 has the same weight)
+                for (int i = 1; ok && i < n; ++i) {
+                    int c = 0, ri = 0;
+                    for (int t = 0; t <= norb; ++t) {
+                        if (t == norb || (t > 0 && split[t] < i)) {
+                            if (c > ri)
+                                ok = false;
+                            if (c != ri || t == norb)
+                                break;
+                            c = ri = 0;
+                        }
+                        c += x[t];
+                        ri += ((ones[t] >> i) & 1u) ? len[t] : 0;
+                    }
+                }
                 if (ok) {
                     if (EMIT && count < out_cap) {
                         uint64_t row = 0;
