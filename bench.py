@@ -310,7 +310,13 @@ ENUM_WORKLOADS = {
     "enum-sts13": ("bibd", (13, 26, 6, 3, 1), "config 1: all BIBD(13,26,6,3,1) (STS(13)) by orderly generation"),
     "enum-sts15": ("bibd", (15, 35, 7, 3, 1), "all BIBD(15,35,7,3,1) (STS(15)) by orderly generation"),
     "enum-k10": ("ksys", (10,), "config 5: all 1-factorizations of K10, every round checked"),
+    # larger families of the reference's result files (their published run times are
+    # 11.04 s and 1.10 s); the oracle's depth-first enumeration of them takes minutes,
+    # so they carry no CPU leg
+    "enum-12-22": ("bibd", (12, 22, 11, 6, 5), "all BIBD(12,22,11,6,5) (11,603 designs) by orderly generation"),
+    "enum-9-36": ("bibd", (9, 36, 12, 3, 3), "all BIBD(9,36,12,3,3) (22,521 designs) by orderly generation"),
 }
+ENUM_NO_CPU = {"enum-12-22", "enum-9-36"}
 
 
 def run_enum(args):
@@ -325,13 +331,14 @@ def run_enum(args):
         else:
             found, st = ctx.enumerate_ksys(*params)
         runs.append((len(found), st.checks, st.seconds, st.kernel_ms, st.batches,
-                     [int(x) for x in st.level_checks], [round(float(x), 3) for x in st.level_kernel_ms]))
+                     [int(x) for x in st.level_checks], [round(float(x), 3) for x in st.level_kernel_ms],
+                     st.gen_seconds))
     timed = runs[args.warmup:]
     secs = sum(r[2] for r in timed)
     checks = sum(r[1] for r in timed)
     designs = sum(r[0] for r in timed)
     cpu = None
-    if not args.no_cpu:
+    if not args.no_cpu and args.workload not in ENUM_NO_CPU:
         import time as _t
         sys.path.insert(0, os.path.join(REPO, "oracle"))
         import oracle
@@ -351,6 +358,7 @@ def run_enum(args):
                                              "checks_per_step": timed[0][1], "batches_per_step": timed[0][4],
                                              "level_checks": timed[0][5], "level_kernel_ms": timed[-1][6]},
             "checks_per_s": checks / secs, "kernel_ms_per_step": sum(r[3] for r in timed) / args.steps,
+            "gen_ms_per_step": 1e3 * sum(r[7] for r in timed) / args.steps,
             "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
     ctx.close()

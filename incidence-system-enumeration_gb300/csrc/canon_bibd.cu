@@ -289,6 +289,73 @@ __global__ void __launch_bounds__(TPB) bibd_label_kernel(uint32_t n_items, uint3
     }
 }
 
+// The verdict of a small batch with the lex-max search split by first row: one
+// thread per (matrix, first row), so a level of few matrices still fills the GPU
+// and a check's latency is that of its largest subtree, not of the whole search.
+// Thread j searches the subtrees that start with row j (row 0: the identity path,
+// which gives the orbit lengths below level 0); the first of a matrix's threads
+// to improve on M raises its stop flag.  bibd_split_combine_kernel then forms the
+// verdict and |Aut| = (rows in the orbit of row 0) x (row 0's product below).
+__global__ void __launch_bounds__(TPB) bibd_split_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
+                                                         const uint64_t *__restrict__ rows, SplitPart *parts,
+                                                         unsigned *stop, uint64_t max_nodes, unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint16_t s_cm[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    Smem sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    const uint64_t total = (uint64_t)n_items * v;
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= total)
+            break;
+        const unsigned item = it / v, j = it - item * v;
+        MaxOut mo{false, false, 0, 0, 0, 0};
+        uint8_t st = 0;
+        if (!load_rows(sm, rows + (size_t)item * v, v, b, flags & F_RAW)) {
+            st = ST_BADINPUT;
+        } else if (!((volatile unsigned *)stop)[item]) {
+            max_search(sm, v, b, max_nodes, mo, ID16, true, true, 1u << j, stop + item);
+            if (mo.timeout)
+                st = ST_TIMEOUT;
+            if (mo.improved)
+                atomicExch(stop + item, 1u);
+        }
+        SplitPart p;
+        p.leaves = mo.leaves;
+        p.orbit0 = (uint8_t)mo.orbit0;
+        p.improved = mo.improved ? 1 : 0;
+        p.status = st;
+        parts[it] = p;
+    }
+}
+
+__global__ void bibd_split_combine_kernel(uint32_t n_items, uint32_t v, const SplitPart *parts,
+                                          const unsigned *stop, uint8_t *canonical, uint64_t *aut,
+                                          uint8_t *status) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += gridDim.x * blockDim.x) {
+        const SplitPart *p = parts + (size_t)i * v;
+        uint8_t st = 0;
+        unsigned total0 = 0;
+        for (uint32_t j = 0; j < v; ++j) {
+            st |= p[j].status;
+            total0 += p[j].orbit0;
+        }
+        const bool improved = stop[i] != 0;
+        if (improved)
+            st &= (uint8_t)~ST_TIMEOUT;          // decided: another thread showed M not canonical
+        const bool can = !st && !improved;
+        canonical[i] = can ? 1 : 0;
+        if (aut) {
+            aut[2 * (size_t)i] = can ? (uint64_t)total0 * (p[0].leaves / (p[0].orbit0 ? p[0].orbit0 : 1)) : 0;
+            aut[2 * (size_t)i + 1] = 0;
+        }
+        if (status)
+            status[i] = st;
+    }
+}
+
 int blocks_for(const void *kernel, int num_sms) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TPB, 0);
@@ -388,6 +455,25 @@ cudaError_t launch_bibd_labels(uint32_t n, uint32_t v, uint32_t b, uint32_t flag
     if (grid > need)
         grid = need;
     bibd_label_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_first_rows, d_nodes, d_orders, max_nodes, tk);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bibd_check_split(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                                    uint8_t *d_canonical, uint64_t *d_aut, uint8_t *d_status, SplitPart *d_parts,
+                                    unsigned *d_stop, uint64_t max_trials, unsigned *tk, int num_sms,
+                                    cudaStream_t s) {
+    if (!n)
+        return cudaSuccess;
+    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
+    cudaMemsetAsync(d_stop, 0, (size_t)n * sizeof(unsigned), s);
+    const uint64_t work = (uint64_t)n * v;
+    int grid = blocks_for((const void *)bibd_split_kernel, num_sms);
+    const int need = (int)((work + TPB - 1) / TPB);
+    if (grid > need)
+        grid = need;
+    bibd_split_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_parts, d_stop, max_trials, tk);
+    const int g2 = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+    bibd_split_combine_kernel<<<g2, 256, 0, s>>>(n, v, d_parts, d_stop, d_canonical, d_aut, d_status);
     return cudaGetLastError();
 }
 

@@ -581,6 +581,7 @@ struct MaxOut {
     uint64_t leaves;    // |Aut|
     uint64_t nodes;
     unsigned first_rows;  // rows that start a labeling reaching the canonical form
+    unsigned orbit0;      // pruned search of a canonical M: the first rows found in the orbit of row 0
 };
 
 // The arranged column masks for level lv+1 after row `cand` was taken at level
@@ -615,9 +616,17 @@ __device__ __forceinline__ void refine_arranged(Smem sm, unsigned lv, unsigned c
 // ID16 = increasing, the plain order).  Only the search order changes with it;
 // a reordered first level turns the automorphism pruning off (it needs the
 // identity path first).  stop_on_improve: return as soon as M is known not to be
-// canonical (leaves, first_rows and R_() are then incomplete).
+// canonical (leaves, first_rows and R_() are then incomplete).  root_mask: the
+// rows that may come first (a search split over several threads by first row).
+// With pruning and M canonical, orbit0 counts the rows of root_mask found in the
+// orbit of row 0, and the thread whose root_mask holds row 0 alone has
+// leaves = the product of the orbit lengths below level 0; split searches then
+// combine as |Aut| = (sum of orbit0) x (that product).
+// stop: a flag that another thread of a split search raises once it has shown M
+// not to be canonical; it is read every 64 nodes and ends this share early.
 __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o,
-                           uint64_t order0 = ID16, bool prune = true, bool stop_on_improve = false) {
+                           uint64_t order0 = ID16, bool prune = true, bool stop_on_improve = false,
+                           unsigned root_mask = 0xFFFFu, const volatile unsigned *stop = nullptr) {
     const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     const uint64_t cols = (1ull << b) - 1ull;
     const uint64_t sentinel = 1ull << b;
@@ -628,6 +637,7 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
     o.leaves = 0;
     o.nodes = 0;
     o.first_rows = 0;
+    o.orbit0 = 0;
     unsigned valid = n;        // rows 0..valid-1 of the bound (and levels 0..valid) are set
     unsigned used = 0;
     uint64_t perm = 0;
@@ -662,6 +672,8 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                 o.timeout = true;
                 return;
             }
+            if (stop && !(o.nodes & 63u) && *stop)
+                return;
             // the greatest arranged row over the unused rows, orbit by orbit, compared
             // with the bound as it is built: 0 equal so far, 1 greater, 2 smaller
             const bool have_bound = i < valid;
@@ -740,7 +752,7 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                 L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
                 valid = i + 1;
             }
-            VD_(i) = tied;            // children still to visit
+            VD_(i) = (i == 0) ? (tied & root_mask) : tied;     // children still to visit
         }
         // next child of the node at level i
         unsigned rem = VD_(i);
@@ -755,6 +767,9 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                 for (unsigned q = i; q < n; ++q)
                     len += pg(orb, q) == i;
                 order *= len;
+                if (i == 0)
+                    for (unsigned q = 0; q < n; ++q)
+                        o.orbit0 += ((root_mask >> q) & 1u) && pg(orb, q) == 0;
             }
             if (i == 0)
                 break;

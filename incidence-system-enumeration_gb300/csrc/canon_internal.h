@@ -60,6 +60,18 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
                                       uint8_t *d_witness16, uint64_t *d_aut, uint8_t *d_status,
                                       uint64_t *d_trials, uint64_t max_trials, unsigned *d_ticket,
                                       int num_sms, cudaStream_t s, const uint64_t *d_orders = nullptr);
+// one share of a lex-max search split by first row (bibd_split_kernel)
+struct SplitPart {
+    uint64_t leaves;
+    uint8_t orbit0, improved, status, pad[5];
+};
+// verdict (and |Aut| of the canonical) of n matrices with v rows, one thread per
+// (matrix, first row); d_parts: n*v parts, d_stop: n words of scratch.  Outputs
+// other than the flag, |Aut| and status are not produced.
+cudaError_t launch_bibd_check_split(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                                    uint8_t *d_canonical, uint64_t *d_aut, uint8_t *d_status, SplitPart *d_parts,
+                                    unsigned *d_stop, uint64_t max_trials, unsigned *d_ticket, int num_sms,
+                                    cudaStream_t s);
 cudaError_t launch_bibd_labels(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
                                uint16_t *d_first_rows, uint64_t *d_nodes, const uint64_t *d_orders,
                                uint64_t max_nodes, unsigned *d_ticket, int num_sms, cudaStream_t s);

@@ -4,12 +4,14 @@
 // (CEnumerator::Enumerate, Source/Enumerator.cpp:540-1024; checks at :446-447 for
 // partial and :364 for complete matrices).  Here a whole level lives on the GPU:
 //   1. rows_count_kernel: one thread per canonical parent counts its admissible
-//      next rows (canon_rows.cuh);
+//      next rows (canon_rows.cuh) and keeps the first 16;
 //   2. an exclusive scan turns the counts into output offsets;
 //   3. rows_emit_kernel writes every child (the parent's rows and the new row),
-//      parents in order, children in the generator's order;
-//   4. the check kernel (bibd_uniform_kernel, verdict only) flags the canonical
-//      children;
+//      parents in order, children in the generator's order (copied from the kept
+//      rows, generated again only for parents with more than 16 children);
+//   4. the check kernel flags the canonical children: bibd_uniform_kernel
+//      (verdict only), or for small slices bibd_split_kernel, the lex-max search
+//      split over one thread per (child, first row);
 //   5. a scan of the flags and compact_kernel pack them into the next level.
 // The host reads one count per level (and per slice when a level is split to
 // bound memory) and, at the end, the complete designs.  Orderly generation makes
@@ -33,6 +35,9 @@ constexpr int SCAN_PER_THREAD = 16;
 constexpr int SCAN_TILE = SCAN_TPB * SCAN_PER_THREAD;
 // candidates checked per slice: bounds the device memory of one level
 constexpr uint64_t SLICE_CAP = 1ull << 24;
+// slices up to this size are checked with the search split by first row (one
+// thread per matrix and first row): small levels are latency bound
+constexpr uint64_t SPLIT_MAX = 1ull << 14;
 
 template <typename T>
 struct DevBuf {
@@ -65,28 +70,44 @@ struct DevBuf {
     ~DevBuf() { cudaFree(p); }
 };
 
+// new rows kept per parent by the counting pass, so that the emitting pass only
+// copies for parents with at most this many children
+constexpr uint32_t ROW_CACHE = 16;
+
 __global__ void __launch_bounds__(GEN_TPB) rows_count_kernel(canon::rows::Params d, const uint64_t *parents,
                                                              uint32_t n_par, int n, uint32_t *counts,
-                                                             unsigned *ticket) {
+                                                             uint64_t *cache, unsigned *ticket) {
     for (;;) {
         const unsigned p = atomicAdd(ticket, 1u);
         if (p >= n_par)
             break;
-        counts[p] = canon::rows::children<false>(d, parents + (size_t)p * n, n, nullptr, 0);
+        counts[p] = canon::rows::children<canon::rows::NEW_ROW>(d, parents + (size_t)p * n, n,
+                                                               cache + (size_t)p * ROW_CACHE, ROW_CACHE);
     }
 }
 
 __global__ void __launch_bounds__(GEN_TPB) rows_emit_kernel(canon::rows::Params d, const uint64_t *parents,
                                                             uint32_t p0, uint32_t p1, int n,
                                                             const uint64_t *offsets, const uint32_t *counts,
-                                                            uint64_t *out, unsigned *ticket) {
+                                                            const uint64_t *cache, uint64_t *out,
+                                                            unsigned *ticket) {
     const uint64_t base = offsets[p0];
     for (;;) {
         const unsigned p = p0 + atomicAdd(ticket, 1u);
         if (p >= p1)
             break;
-        canon::rows::children<true>(d, parents + (size_t)p * n, n, out + (offsets[p] - base) * (n + 1),
-                                    counts[p]);
+        const uint32_t cnt = counts[p];
+        const uint64_t *par = parents + (size_t)p * n;
+        uint64_t *dst = out + (offsets[p] - base) * (n + 1);
+        if (cnt <= ROW_CACHE) {
+            for (uint32_t j = 0; j < cnt; ++j) {
+                for (int i = 0; i < n; ++i)
+                    dst[(size_t)j * (n + 1) + i] = par[i];
+                dst[(size_t)j * (n + 1) + n] = cache[(size_t)p * ROW_CACHE + j];
+            }
+        } else {
+            canon::rows::children<canon::rows::CHILD>(d, par, n, dst, cnt);
+        }
     }
 }
 
@@ -241,10 +262,11 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
     cudaStream_t s = c->stream;
     canon_enum_stats st{};
     const canon::rows::Params prm{(int)v, (int)b, (int)r, (int)k, (int)lambda};
-    DevBuf<uint64_t> lev, next, cand, offs, coffs, sums, aut, aut_out;
+    DevBuf<uint64_t> lev, next, cand, offs, coffs, sums, aut, aut_out, rcache;
     DevBuf<uint32_t> counts;
     DevBuf<uint8_t> can, status;
-    DevBuf<unsigned> ticket;
+    DevBuf<unsigned> ticket, stop;
+    DevBuf<canon::SplitPart> parts;
     cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -277,12 +299,14 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
         e = counts.ensure(n_par);
         if (e == cudaSuccess)
             e = offs.ensure(n_par + 1);
+        if (e == cudaSuccess)
+            e = rcache.ensure((size_t)n_par * ROW_CACHE);
         if (e != cudaSuccess)
             return done(CANON_ENOMEM, "level buffers", e);
         cudaEventRecord(e0, s);
         cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
         rows_count_kernel<<<gen_grid((const void *)rows_count_kernel, c->num_sms, n_par), GEN_TPB, 0, s>>>(
-            prm, lev.p, (uint32_t)n_par, (int)n, counts.p, ticket.p);
+            prm, lev.p, (uint32_t)n_par, (int)n, counts.p, rcache.p, ticket.p);
         e = exclusive_scan(counts.p, n_par, offs.p, sums, s);
         uint64_t n_cand = 0;
         if (e == cudaSuccess)
@@ -342,13 +366,24 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
             cudaEventRecord(e0, s);
             cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
             rows_emit_kernel<<<gen_grid((const void *)rows_emit_kernel, c->num_sms, p1 - p0), GEN_TPB, 0, s>>>(
-                prm, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, offs.p, counts.p, cand.p, ticket.p);
+                prm, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, offs.p, counts.p, rcache.p, cand.p, ticket.p);
             cudaEventRecord(e1, s);
             // 4: the verdicts
-            e = canon::launch_bibd_check_uniform((uint32_t)ns, m, b,
-                                                 canon::F_VERDICT_ONLY | (complete ? canon::F_COMPLETE : 0u),
-                                                 cand.p, can.p, nullptr, complete ? aut.p : nullptr, status.p,
-                                                 nullptr, c->cfg.max_trials, c->d_ticket, c->num_sms, s);
+            if (ns <= SPLIT_MAX) {
+                e = parts.ensure((size_t)(ns ? ns : 1) * m);
+                if (e == cudaSuccess)
+                    e = stop.ensure(ns ? ns : 1);
+                if (e == cudaSuccess)
+                    e = canon::launch_bibd_check_split((uint32_t)ns, m, b,
+                                                       canon::F_VERDICT_ONLY | (complete ? canon::F_COMPLETE : 0u),
+                                                       cand.p, can.p, complete ? aut.p : nullptr, status.p, parts.p,
+                                                       stop.p, c->cfg.max_trials, c->d_ticket, c->num_sms, s);
+            } else {
+                e = canon::launch_bibd_check_uniform((uint32_t)ns, m, b,
+                                                     canon::F_VERDICT_ONLY | (complete ? canon::F_COMPLETE : 0u),
+                                                     cand.p, can.p, nullptr, complete ? aut.p : nullptr, status.p,
+                                                     nullptr, c->cfg.max_trials, c->d_ticket, c->num_sms, s);
+            }
             cudaEventRecord(e2, s);
             // 5: pack the canonical ones
             if (e == cudaSuccess)

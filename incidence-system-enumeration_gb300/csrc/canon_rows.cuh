@@ -28,11 +28,14 @@ struct Params {
     int v, b, r, k, lambda;
 };
 
+// What children() writes for child j < out_cap: nothing, the whole child at
+// out[j*(n+1) .. j*(n+1)+n] (the parent's rows, then the new row), or the new
+// row alone at out[j].
+enum Emit { COUNT = 0, CHILD = 1, NEW_ROW = 2 };
+
 // Children of one parent with n rows (bit c of word i = row i, column c), in a
-// fixed order: orbits left to right, more 1s first.  EMIT: child j is written to
-// out[j*(n+1) .. j*(n+1)+n] (the parent's rows, then the new row) for j < out_cap.
-// Returns the number of children.
-template <bool EMIT>
+// fixed order: orbits left to right, more 1s first.  Returns their number.
+template <int EMIT>
 CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint64_t *out, uint32_t out_cap) {
     const int b = d.b, k = d.k;
     uint8_t start[64], len[64], weight[64];
@@ -66,25 +69,25 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
         }
     }
     // hi/lo: the most / least 1s orbit q can take (full orbits none, orbits whose
-    // columns need every remaining row all); cap/need: suffix sums of hi/lo over
-    // the orbits that meet row i, so a row whose lambda can no longer be met ends
-    // the branch at once
+    // columns need every remaining row all); rc/rn: the sums of hi/lo over the
+    // orbits from the current one on that meet row i (ca/cn over all orbits), kept
+    // as the search moves, so a row whose lambda can no longer be met ends the
+    // branch at once
     const int rem_rows = d.v - n - 1;
     uint8_t hi[64], lo[64];
-    uint8_t cap[65][16], need[65][16], cap_all[65], need_all[65];
+    int rc[16], rn[16], ca = 0, cn = 0;
     for (int i = 0; i < n; ++i)
-        cap[norb][i] = need[norb][i] = 0;
-    cap_all[norb] = need_all[norb] = 0;
-    for (int q = norb - 1; q >= 0; --q) {
+        rc[i] = rn[i] = 0;
+    for (int q = 0; q < norb; ++q) {
         hi[q] = (weight[q] >= k) ? 0 : len[q];
         lo[q] = (k - weight[q] > rem_rows) ? len[q] : 0;
-        cap_all[q] = (uint8_t)(cap_all[q + 1] + hi[q]);
-        need_all[q] = (uint8_t)(need_all[q + 1] + lo[q]);
-        for (int i = 0; i < n; ++i) {
-            const bool in = (ones[q] >> i) & 1u;
-            cap[q][i] = (uint8_t)(cap[q + 1][i] + (in ? hi[q] : 0));
-            need[q][i] = (uint8_t)(need[q + 1][i] + (in ? lo[q] : 0));
-        }
+        ca += hi[q];
+        cn += lo[q];
+        for (int i = 0; i < n; ++i)
+            if ((ones[q] >> i) & 1u) {
+                rc[i] += hi[q];
+                rn[i] += lo[q];
+            }
     }
     int lam[16];
     for (int i = 0; i < n; ++i)
@@ -121,32 +124,44 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
                     }
                 }
                 if (ok) {
-                    if (EMIT && count < out_cap) {
+                    if (EMIT != COUNT && count < out_cap) {
                         uint64_t row = 0;
                         for (int t = 0; t < norb; ++t)
                             if (x[t])
                                 row |= ((1ull << x[t]) - 1ull) << start[t];
-                        uint64_t *dst = out + (size_t)count * (n + 1);
-                        for (int i = 0; i < n; ++i)
-                            dst[i] = parent[i];
-                        dst[n] = row;
+                        if (EMIT == CHILD) {
+                            uint64_t *dst = out + (size_t)count * (n + 1);
+                            for (int i = 0; i < n; ++i)
+                                dst[i] = parent[i];
+                            dst[n] = row;
+                        } else {
+                            out[count] = row;
+                        }
                     }
                     ++count;
                 }
                 if (q == 0)
                     break;
                 --q;
+                ca += hi[q];
+                cn += lo[q];
+                for (int i = 0; i < n; ++i)
+                    if ((ones[q] >> i) & 1u) {
+                        rc[i] += hi[q];
+                        rn[i] += lo[q];
+                    }
                 enter = false;
                 continue;
             }
             const int lf = left[q];
+            const int ca1 = ca - hi[q], cn1 = cn - lo[q];      // orbits after q
             int minx = lo[q], maxx = hi[q];
             if (maxx > lf)
                 maxx = lf;
-            if (minx < lf - cap_all[q + 1])
-                minx = lf - cap_all[q + 1];
-            if (maxx > lf - need_all[q + 1])
-                maxx = lf - need_all[q + 1];
+            if (minx < lf - ca1)
+                minx = lf - ca1;
+            if (maxx > lf - cn1)
+                maxx = lf - cn1;
             if (((tied >> q) & 1u) && !((ones[q] >> (n - 1)) & 1u) && maxx > 0)
                 maxx = 0;
             mn[q] = (uint8_t)(minx < 0 ? 0 : minx);
@@ -167,8 +182,9 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
             const int xv = --nxt[q];
             bool ok = true;
             for (int i = 0; i < n && ok; ++i) {
-                const int l = lam[i] - (((ones[q] >> i) & 1u) ? xv : 0);
-                ok = l >= need[q + 1][i] && l <= cap[q + 1][i];
+                const bool in = (ones[q] >> i) & 1u;
+                const int l = lam[i] - (in ? xv : 0);
+                ok = l >= rn[i] - (in ? lo[q] : 0) && l <= rc[i] - (in ? hi[q] : 0);
             }
             if (!ok)
                 continue;
@@ -187,6 +203,13 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
             break;
         }
         if (moved) {
+            ca -= hi[q];
+            cn -= lo[q];
+            for (int i = 0; i < n; ++i)
+                if ((ones[q] >> i) & 1u) {
+                    rc[i] -= hi[q];
+                    rn[i] -= lo[q];
+                }
             ++q;
             enter = true;
             continue;
@@ -194,6 +217,13 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
         if (q == 0)
             break;
         --q;
+        ca += hi[q];
+        cn += lo[q];
+        for (int i = 0; i < n; ++i)
+            if ((ones[q] >> i) & 1u) {
+                rc[i] += hi[q];
+                rn[i] += lo[q];
+            }
         enter = false;
     }
     return count;

@@ -5,6 +5,6 @@ extern "C" uint32_t rows_children(int v, int b, int r, int k, int lambda, const 
                                   uint64_t *out, uint32_t cap) {
     const canon::rows::Params d{v, b, r, k, lambda};
     if (!out)
-        return canon::rows::children<false>(d, parent, n, nullptr, 0);
-    return canon::rows::children<true>(d, parent, n, out, cap);
+        return canon::rows::children<canon::rows::COUNT>(d, parent, n, nullptr, 0);
+    return canon::rows::children<canon::rows::CHILD>(d, parent, n, out, cap);
 }

@@ -170,3 +170,48 @@ def test_trial_budget_ends_the_search_with_a_timeout_status(host):
         host.emu_check(rows.ctypes.data_as(ctypes.POINTER(u64)), 15, 35, flags, u64(4), ctypes.byref(can),
                        ctypes.byref(st), ctypes.byref(rr), ctypes.byref(w), aut, ctypes.byref(tr))
         assert st.value & 2 and not can.value
+
+
+def _split_result(L, rows, n, b):
+    """The search split into one thread per first row, combined as the split kernel does."""
+    u64 = ctypes.c_uint64
+    rows = np.ascontiguousarray(rows, np.uint64)
+    improved, total0, deep = False, 0, None
+    for j in range(n):
+        leaves, orb0, imp = u64(), ctypes.c_uint(), ctypes.c_uint8()
+        assert L.emu_maxsearch_root(rows.ctypes.data_as(ctypes.POINTER(u64)), n, b, 1 << j, ctypes.byref(leaves),
+                                    ctypes.byref(orb0), ctypes.byref(imp)) == 0
+        improved |= bool(imp.value)
+        total0 += orb0.value
+        if j == 0:
+            deep = leaves.value // max(orb0.value, 1)
+    return improved, (0 if improved else total0 * deep)
+
+
+def test_search_split_by_first_row_combines_to_the_whole(host):
+    """One thread per first row (the enumerator's small-batch check): the verdict is
+    the OR of the threads', |Aut| = (rows found in the orbit of row 0) x (the
+    identity thread's product below level 0) -- equal to the unsplit search."""
+    import ise_gb300 as G
+    rng = np.random.default_rng(8)
+    cases_ = []
+    for M, _ in cases.load_sts15()[::3]:
+        cases_.append((G.pack_rows(M), 35))
+        P = cases.permute_normalize(M, rng)
+        for k in (5, 9, 12, 15):
+            cases_.append((G.pack_rows(oracle.bibd_normalize(P[:k])), 35))
+    for params in [(8, 14, 7, 4, 3), (11, 11, 5, 5, 2), (13, 26, 6, 3, 1), (9, 12, 4, 3, 1)]:
+        for M, _ in cases.bibd_designs(*params):
+            cases_.append((G.pack_rows(M), params[1]))
+            P = cases.permute_normalize(M, rng)
+            for k in range(3, params[0] + 1, 2):
+                cases_.append((G.pack_rows(oracle.bibd_normalize(P[:k])), params[1]))
+    for i in range(10):
+        cases_.append((oracle.sts_random_rows(15, 77, i), 35))
+    for rows, b in cases_:
+        n = len(rows)
+        full = maxsearch(host, rows, n, b, True)
+        imp, aut = _split_result(host, rows, n, b)
+        assert imp == full["improved"]
+        if not imp:
+            assert aut == full["aut"]
