@@ -264,9 +264,9 @@ def run_gpu(args, rank, world, local, dist):
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             ctx.submit_bibd(host_rows, V, B, flags)
-            res = ctx.sync()
+            res = ctx.sync(raw=True)
         e2e_dt = (time.perf_counter() - t0) / e2e_steps
-        assert res["n"] == n and np.array_equal(res["canonical"].astype(np.uint8), can)
+        assert res["n"] == n and np.array_equal(res["canonical"], can)
     h2d = n * V * 8 + n * 16
     d2h = n * (1 + 1 + 1 + 1 + 4 + 16 + 16 + 8 + 2 + 1)
 

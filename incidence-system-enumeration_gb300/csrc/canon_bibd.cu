@@ -150,14 +150,16 @@ __global__ void __launch_bounds__(TPB) bibd_witness_kernel(uint32_t n_items, uin
     }
 }
 
-// The two passes over work items of any shape (the batched path).
+// The two passes over work items of any shape (the batched path); BCAP bounds the
+// columns of every item of the launch, as in bibd_max_kernel.
+template <unsigned BCAP>
 __global__ void __launch_bounds__(TPB) bibd_items_max_kernel(const Item *__restrict__ items, uint32_t n_items,
                                                              const uint64_t *__restrict__ words, Outputs out,
                                                              uint64_t max_nodes, unsigned *ticket) {
     __shared__ uint64_t s_rows[VMAX * TPB];
     __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
     __shared__ uint32_t s_vd[VMAX * TPB];
-    __shared__ uint16_t s_cm[64 * TPB];
+    __shared__ uint16_t s_cm[BCAP * TPB];
     const unsigned tid = threadIdx.x;
     Smem sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
     for (;;) {
@@ -168,7 +170,7 @@ __global__ void __launch_bounds__(TPB) bibd_items_max_kernel(const Item *__restr
         const unsigned n = item.nrows, b = item.ncols, o_i = item.out_idx;
         MaxOut mo{false, false, 0, 0, 0};
         uint8_t st = 0;
-        if (item.kind != KIND_BIBD || n < 1 || n > VMAX || b < 1 || b > BMAX ||
+        if (item.kind != KIND_BIBD || n < 1 || n > VMAX || b < 1 || b > BMAX || b > BCAP ||
             !load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW)) {
             st = ST_BADINPUT;
         } else {
@@ -380,15 +382,21 @@ cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint6
 }
 
 cudaError_t launch_bibd_check_two_pass(const Item *d_items, uint32_t n_items, const uint64_t *d_words, Outputs out,
-                                       uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
+                                       uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s,
+                                       uint32_t max_b) {
     if (!n_items)
         return cudaSuccess;
     cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
     const int need = (int)((n_items + TPB - 1) / TPB);
-    int grid = blocks_for((const void *)bibd_items_max_kernel, num_sms);
+    const bool narrow = max_b <= 40;
+    int grid = narrow ? blocks_for((const void *)bibd_items_max_kernel<40>, num_sms)
+                      : blocks_for((const void *)bibd_items_max_kernel<64>, num_sms);
     if (grid > need)
         grid = need;
-    bibd_items_max_kernel<<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+    if (narrow)
+        bibd_items_max_kernel<40><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+    else
+        bibd_items_max_kernel<64><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
@@ -580,7 +588,7 @@ cudaError_t launch_bibd_check_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32
     // route is the one canon_sync takes for the same flags
     const bool two_pass = (flags & (F_AUT_CANON | F_FULL_AUT)) && !(flags & (F_SAVE_AUTS | F_REFERENCE_ORDER));
     if (two_pass)
-        return launch_bibd_check_two_pass(items, n, d_rows, out, max_trials, counter, sms, s);
+        return launch_bibd_check_two_pass(items, n, d_rows, out, max_trials, counter, sms, s, b);
     return launch_bibd_check(items, n, d_rows, out, max_trials, counter, sms, s);
 }
 

@@ -1,25 +1,31 @@
-// canon_levels.cu -- BIBD enumeration with every level resident in HBM.
+// canon_levels.cu -- BIBD enumeration, level by level, checks and compaction on the GPU.
 //
 // The reference enumerates depth-first and checks one partial matrix at a time
 // (CEnumerator::Enumerate, Source/Enumerator.cpp:540-1024; checks at :446-447 for
-// partial and :364 for complete matrices).  Here a whole level lives on the GPU:
-//   1. rows_count_kernel: one thread per canonical parent counts its admissible
-//      next rows (canon_rows.cuh) and keeps the first 16;
-//   2. an exclusive scan turns the counts into output offsets;
-//   3. rows_emit_kernel writes every child (the parent's rows and the new row),
-//      parents in order, children in the generator's order (copied from the kept
-//      rows, generated again only for parents with more than 16 children);
-//   4. the check kernel flags the canonical children: bibd_uniform_kernel
-//      (verdict only), or for small slices bibd_split_kernel, the lex-max search
-//      split over one thread per (child, first row);
-//   5. a scan of the flags and compact_kernel pack them into the next level.
-// The host reads one count per level (and per slice when a level is split to
-// bound memory) and, at the end, the complete designs.  Orderly generation makes
-// the result independent of the visiting order: every prefix of a canonical
-// matrix is canonical, so the canonical complete matrices are exactly those the
-// depth-first search finds; the order is that of the host-generated levels.
+// partial and :364 for complete matrices).  Here a whole level is handled at once:
+//   1. the admissible next rows of every canonical parent (canon_rows.cuh) are
+//      counted, prefix-summed and written in order -- parents in order, children
+//      in the generator's order, so the result does not depend on where or on
+//      how many threads they are made: levels of fewer than 128K parents on all
+//      host cores into pinned memory, larger levels on the GPU (rows_count_kernel,
+//      a scan, rows_emit_kernel), one thread per parent;
+//   2. the candidates are checked in slices of at most 16M matrices;
+//   3. the check kernel flags the canonical ones: bibd_uniform_kernel (verdict
+//      only), or for small slices bibd_split_kernel, the lex-max search split
+//      over one thread per (candidate, first row);
+//   4. a scan of the flags and compact_kernel pack them into the next level.
+// The row generator is a serial depth-first search whose path differs from
+// parent to parent; on the GPU the 32 threads of a warp run 32 such paths one
+// after another.  A level of BIBD(8,28,14,4,6) (5,328 parents) took 296 ms there
+// against under 1 ms on one host core, while the levels of millions of heavy
+// searches of BIBD(12,22,11,6,5) took 2.7 s on the GPU against 17 s on 16 host
+// cores; hence the split by level size.  Orderly
+// generation makes the result independent of the visiting order: every prefix
+// of a canonical matrix is canonical, so the canonical complete matrices are
+// exactly those the depth-first search finds.
 #include <chrono>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "../../include/canon_gb300.h"
@@ -29,12 +35,15 @@
 
 namespace {
 
-constexpr int GEN_TPB = 128;
 constexpr int SCAN_TPB = 256;
 constexpr int SCAN_PER_THREAD = 16;
 constexpr int SCAN_TILE = SCAN_TPB * SCAN_PER_THREAD;
 // candidates checked per slice: bounds the device memory of one level
 constexpr uint64_t SLICE_CAP = 1ull << 24;
+constexpr int GEN_TPB = 128;
+// levels with at least this many parents generate their children on the GPU
+// (enough independent searches to fill it); smaller ones on the host cores
+constexpr uint64_t DEVICE_GEN_MIN = 1ull << 17;
 // slices up to this size are checked with the search split by first row (one
 // thread per matrix and first row): small levels are latency bound
 constexpr uint64_t SPLIT_MAX = 1ull << 14;
@@ -251,6 +260,49 @@ int gen_grid(const void *kernel, int num_sms, uint64_t work) {
     return (int)(g ? g : 1);
 }
 
+// pinned host memory that grows (contents not kept)
+struct PinBuf {
+    uint64_t *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= cap)
+            return cudaSuccess;
+        cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = n + n / 4 + 1024;
+        const cudaError_t e = cudaHostAlloc((void **)&p, want * sizeof(uint64_t), cudaHostAllocDefault);
+        if (e == cudaSuccess)
+            cap = want;
+        return e;
+    }
+    PinBuf() = default;
+    PinBuf(const PinBuf &) = delete;
+    PinBuf &operator=(const PinBuf &) = delete;
+    ~PinBuf() { cudaFreeHost(p); }
+};
+
+// fn(lo, hi) over [0, n) on all host cores, in contiguous ranges
+template <typename F>
+void parallel_ranges(uint64_t n, F fn) {
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt < 1)
+        nt = 1;
+    if (nt > 64)
+        nt = 64;
+    if (n < 256)
+        nt = 1;
+    if (nt == 1) {
+        fn((uint64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t)
+        th.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
+    for (auto &x : th)
+        x.join();
+}
+
 }  // namespace
 
 extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32_t r, uint32_t k, uint32_t lambda,
@@ -258,68 +310,87 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
     if (!c || v < 2 || v > canon::VMAX || b < 1 || b > canon::BMAX || r < 1 || r > b || k < 1 || k > v)
         return CANON_EINVAL;
     const auto t0 = std::chrono::steady_clock::now();
+    auto since = [](std::chrono::steady_clock::time_point a) {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
+    };
     cudaSetDevice(c->device);
     cudaStream_t s = c->stream;
     canon_enum_stats st{};
     const canon::rows::Params prm{(int)v, (int)b, (int)r, (int)k, (int)lambda};
-    DevBuf<uint64_t> lev, next, cand, offs, coffs, sums, aut, aut_out, rcache;
-    DevBuf<uint32_t> counts;
+    DevBuf<uint64_t> lev, next, cand, doffs, coffs, sums, aut, aut_out, rcache;
+    DevBuf<uint32_t> dcounts;
     DevBuf<uint8_t> can, status;
     DevBuf<unsigned> ticket, stop;
     DevBuf<canon::SplitPart> parts;
-    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    PinBuf hcand;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    cudaEventCreate(&e2);
     auto done = [&](int rc, const char *what, cudaError_t e) {
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        cudaEventDestroy(e2);
-        if (rc != CANON_OK) {
-            c->err = std::string("enumerate: ") + what + (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e)
-                                                                           : std::string());
-        }
+        if (rc != CANON_OK)
+            c->err = std::string("enumerate: ") + what +
+                     (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e) : std::string());
         return rc;
     };
-    cudaError_t e = ticket.ensure(2);
-    // level 1: row 0 is forced, r ones first
-    const uint64_t row0 = (r >= 64) ? ~0ull : ((1ull << r) - 1ull);
-    if (e == cudaSuccess)
-        e = lev.ensure(1);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(lev.p, &row0, sizeof(uint64_t), cudaMemcpyHostToDevice, s);
+    cudaError_t e = ticket.ensure(2);      // [0] work-stealing counter, [1] timeout flag
     if (e != cudaSuccess)
-        return done(CANON_ECUDA, "setup", e);
+        return done(CANON_ENOMEM, "setup", e);
+    // level 1: row 0 is forced, r ones first; the parents of a level live on the
+    // host (host generation) or in `lev` on the GPU (after a compaction)
+    std::vector<uint64_t> level(1, (r >= 64) ? ~0ull : ((1ull << r) - 1ull));
+    bool host_valid = true;
     uint64_t n_par = 1;
     uint32_t n = 1;
     while (n < v && n_par) {
         const uint32_t m = n + 1;
         const bool complete = m == v;
-        // 1-2: children per parent and their offsets
-        e = counts.ensure(n_par);
-        if (e == cudaSuccess)
-            e = offs.ensure(n_par + 1);
-        if (e == cudaSuccess)
-            e = rcache.ensure((size_t)n_par * ROW_CACHE);
-        if (e != cudaSuccess)
-            return done(CANON_ENOMEM, "level buffers", e);
-        cudaEventRecord(e0, s);
-        cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
-        rows_count_kernel<<<gen_grid((const void *)rows_count_kernel, c->num_sms, n_par), GEN_TPB, 0, s>>>(
-            prm, lev.p, (uint32_t)n_par, (int)n, counts.p, rcache.p, ticket.p);
-        e = exclusive_scan(counts.p, n_par, offs.p, sums, s);
+        const bool dev = n_par >= DEVICE_GEN_MIN;
+        // 1: children per parent and their offsets
+        auto tg = std::chrono::steady_clock::now();
+        std::vector<uint32_t> counts;
+        std::vector<uint64_t> offs;
         uint64_t n_cand = 0;
-        if (e == cudaSuccess)
-            e = read_u64(offs.p + n_par, &n_cand, s);
-        if (e != cudaSuccess)
-            return done(CANON_ECUDA, "count", e);
-        float ms = 0.f;
-        cudaEventRecord(e1, s);
-        cudaEventSynchronize(e1);
-        cudaEventElapsedTime(&ms, e0, e1);
-        st.gen_seconds += ms * 1e-3;
-        c->launches += 4;
-        // the canonical children of all slices, packed
+        if (!dev) {
+            if (!host_valid) {
+                level.resize((size_t)n_par * n);
+                e = cudaMemcpyAsync(level.data(), lev.p, level.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
+                if (e == cudaSuccess)
+                    e = cudaStreamSynchronize(s);
+                if (e != cudaSuccess)
+                    return done(CANON_ECUDA, "level to host", e);
+                host_valid = true;
+            }
+            counts.resize(n_par);
+            parallel_ranges(n_par, [&](uint64_t lo, uint64_t hi) {
+                for (uint64_t p = lo; p < hi; ++p)
+                    counts[p] = canon::rows::children<canon::rows::COUNT>(prm, level.data() + p * n, (int)n,
+                                                                         nullptr, 0);
+            });
+            offs.assign(n_par + 1, 0);
+            for (uint64_t p = 0; p < n_par; ++p)
+                offs[p + 1] = offs[p] + counts[p];
+            n_cand = offs[n_par];
+        } else {
+            e = dcounts.ensure(n_par);
+            if (e == cudaSuccess)
+                e = doffs.ensure(n_par + 1);
+            if (e == cudaSuccess)
+                e = rcache.ensure((size_t)n_par * ROW_CACHE);
+            if (e != cudaSuccess)
+                return done(CANON_ENOMEM, "level buffers", e);
+            cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
+            rows_count_kernel<<<gen_grid((const void *)rows_count_kernel, c->num_sms, n_par), GEN_TPB, 0, s>>>(
+                prm, lev.p, (uint32_t)n_par, (int)n, dcounts.p, rcache.p, ticket.p);
+            e = exclusive_scan(dcounts.p, n_par, doffs.p, sums, s);
+            if (e == cudaSuccess)
+                e = read_u64(doffs.p + n_par, &n_cand, s);
+            if (e != cudaSuccess)
+                return done(CANON_ECUDA, "count", e);
+            c->launches += 4;
+        }
+        st.gen_seconds += since(tg);
         e = next.ensure((size_t)(n_cand ? n_cand : 1) * m);
         if (e == cudaSuccess && complete)
             e = aut_out.ensure((size_t)(n_cand ? n_cand : 1) * 2);
@@ -328,28 +399,37 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
         uint64_t n_next = 0;
         uint64_t p0 = 0;
         while (p0 < n_par) {
-            // the largest slice of parents whose children fit SLICE_CAP (at least one parent)
-            uint64_t base = 0, p1 = n_par, end = n_cand;
-            e = read_u64(offs.p + p0, &base, s);
-            if (e == cudaSuccess && n_cand - base > SLICE_CAP) {
-                uint64_t lo = p0 + 1, hi = n_par;
-                while (lo < hi) {
-                    const uint64_t mid = (lo + hi + 1) / 2;
-                    uint64_t at = 0;
-                    e = read_u64(offs.p + mid, &at, s);
-                    if (e != cudaSuccess)
-                        break;
-                    if (at - base <= SLICE_CAP)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
+            // the largest slice of parents whose children fit SLICE_CAP (at least one)
+            uint64_t p1 = p0 + 1, base = 0, end = 0;
+            if (!dev) {
+                while (p1 < n_par && offs[p1 + 1] - offs[p0] <= SLICE_CAP)
+                    ++p1;
+                base = offs[p0];
+                end = offs[p1];
+            } else {
+                e = read_u64(doffs.p + p0, &base, s);
+                p1 = n_par;
+                end = n_cand;
+                if (e == cudaSuccess && n_cand - base > SLICE_CAP) {
+                    uint64_t lo = p0 + 1, hi = n_par;
+                    while (lo < hi) {
+                        const uint64_t mid = (lo + hi + 1) / 2;
+                        uint64_t at = 0;
+                        e = read_u64(doffs.p + mid, &at, s);
+                        if (e != cudaSuccess)
+                            break;
+                        if (at - base <= SLICE_CAP)
+                            lo = mid;
+                        else
+                            hi = mid - 1;
+                    }
+                    p1 = lo;
+                    if (e == cudaSuccess)
+                        e = read_u64(doffs.p + p1, &end, s);
                 }
-                p1 = lo;
-                if (e == cudaSuccess)
-                    e = read_u64(offs.p + p1, &end, s);
+                if (e != cudaSuccess)
+                    return done(CANON_ECUDA, "slice", e);
             }
-            if (e != cudaSuccess)
-                return done(CANON_ECUDA, "slice", e);
             const uint64_t ns = end - base;
             e = cand.ensure((size_t)(ns ? ns : 1) * m);
             if (e == cudaSuccess)
@@ -360,15 +440,33 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 e = coffs.ensure(ns + 1);
             if (e == cudaSuccess && complete)
                 e = aut.ensure((size_t)(ns ? ns : 1) * 2);
+            if (e == cudaSuccess && !dev)
+                e = hcand.ensure((size_t)(ns ? ns : 1) * m);
             if (e != cudaSuccess)
                 return done(CANON_ENOMEM, "slice buffers", e);
-            // 3: the children of parents [p0, p1)
+            // 2: the children of parents [p0, p1), in order
+            tg = std::chrono::steady_clock::now();
+            if (!dev) {
+                parallel_ranges(p1 - p0, [&](uint64_t lo, uint64_t hi) {
+                    for (uint64_t p = p0 + lo; p < p0 + hi; ++p)
+                        canon::rows::children<canon::rows::CHILD>(prm, level.data() + p * n, (int)n,
+                                                                  hcand.p + (offs[p] - base) * m, counts[p]);
+                });
+                e = cudaMemcpyAsync(cand.p, hcand.p, (size_t)ns * m * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
+            } else {
+                cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
+                rows_emit_kernel<<<gen_grid((const void *)rows_emit_kernel, c->num_sms, p1 - p0), GEN_TPB, 0, s>>>(
+                    prm, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, doffs.p, dcounts.p, rcache.p, cand.p, ticket.p);
+                e = cudaGetLastError();
+                if (e == cudaSuccess)
+                    e = cudaStreamSynchronize(s);
+                ++c->launches;
+            }
+            st.gen_seconds += since(tg);
+            if (e != cudaSuccess)
+                return done(CANON_ECUDA, "children", e);
+            // 3: the verdicts
             cudaEventRecord(e0, s);
-            cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
-            rows_emit_kernel<<<gen_grid((const void *)rows_emit_kernel, c->num_sms, p1 - p0), GEN_TPB, 0, s>>>(
-                prm, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, offs.p, counts.p, rcache.p, cand.p, ticket.p);
-            cudaEventRecord(e1, s);
-            // 4: the verdicts
             if (ns <= SPLIT_MAX) {
                 e = parts.ensure((size_t)(ns ? ns : 1) * m);
                 if (e == cudaSuccess)
@@ -384,8 +482,8 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                                                      cand.p, can.p, nullptr, complete ? aut.p : nullptr, status.p,
                                                      nullptr, c->cfg.max_trials, c->d_ticket, c->num_sms, s);
             }
-            cudaEventRecord(e2, s);
-            // 5: pack the canonical ones
+            cudaEventRecord(e1, s);
+            // 4: pack the canonical ones into the next level
             if (e == cudaSuccess)
                 e = exclusive_scan(can.p, ns, coffs.p, sums, s);
             if (e == cudaSuccess) {
@@ -406,10 +504,8 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 e = read_u64(coffs.p + ns, &n_can, s);
             if (e != cudaSuccess)
                 return done(CANON_ECUDA, "check", e);
-            float gen_ms = 0.f, chk_ms = 0.f;
-            cudaEventElapsedTime(&gen_ms, e0, e1);
-            cudaEventElapsedTime(&chk_ms, e1, e2);
-            st.gen_seconds += gen_ms * 1e-3;
+            float chk_ms = 0.f;
+            cudaEventElapsedTime(&chk_ms, e0, e1);
             st.kernel_ms += chk_ms;
             st.level_kernel_ms[m - 1] += chk_ms;
             c->last_ms = chk_ms;
@@ -424,6 +520,7 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
         st.level_checks[m - 1] += n_cand;
         ++st.levels;
         lev.swap(next);
+        host_valid = false;
         n_par = n_next;
         n = m;
     }
@@ -441,7 +538,7 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
             for (uint64_t i = 0; i < n_par; ++i)
                 cb(user, (const uint8_t *)(rows.data() + i * v), v, b, auts[2 * i], auts[2 * i + 1]);
     }
-    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    st.seconds = since(t0);
     if (stats)
         *stats = st;
     return done(CANON_OK, "", cudaSuccess);

@@ -275,7 +275,6 @@ class Context:
         if not self.h:
             raise CanonError(CANON_ENODEV, "canon_create failed (no GPU?)")
         self.aut_cap = aut_cap
-        self._kinds = []
 
     def close(self):
         if self.h:
@@ -304,7 +303,6 @@ class Context:
         bt = BibdBatch(n, v, b, flags, _ptr(rows, ctypes.c_uint64),
                        _ptr(nr, ctypes.c_uint8) if nr is not None else None)
         self._check(self.lib.canon_submit_bibd(self.h, ctypes.byref(bt)))
-        self._kinds += [("bibd", v, b)] * n
         return n
 
     def submit_ksys(self, data, np_, rounds, flags=0, nrows=None):
@@ -314,17 +312,29 @@ class Context:
         bt = KsysBatch(n, np_, rounds, flags, _ptr(data, ctypes.c_uint8),
                        _ptr(nr, ctypes.c_uint8) if nr is not None else None)
         self._check(self.lib.canon_submit_ksys(self.h, ctypes.byref(bt)))
-        self._kinds += [("ksys", np_, rounds)] * n
         return n
 
-    def sync(self, allow_timeout=False):
+    def sync(self, allow_timeout=False, raw=False):
+        """Runs canon_sync and copies the result arrays.  raw: |Aut| stays an (n, 2)
+        uint64 array (low, high words) and the automorphism arena is not copied, so
+        no per-item Python work is done."""
         r = Results()
         rc = self.lib.canon_sync(self.h, ctypes.byref(r))
         if rc != CANON_OK and not (allow_timeout and rc == CANON_ETIMEOUT):
             raise CanonError(rc, self.error())
         n = r.n
         out = {"n": n, "kernel_ms": r.kernel_ms}
-        if n:
+        if n and raw:
+            def view(p, count, dt):
+                return np.ctypeslib.as_array(p, shape=(count,)).view(dt).copy()
+            out["canonical"] = view(r.canonical, n, np.uint8)
+            out["status"] = view(r.status, n, np.uint8)
+            out["witness"] = view(r.witness, n * 16, np.uint8).reshape(n, 16)
+            out["aut"] = view(r.aut, 2 * n, np.uint64).reshape(n, 2)
+            out["reject_row"] = view(r.reject_row, n, np.uint8)
+            out["row_to_change"] = view(r.row_to_change, n, np.uint8)
+            out["trials"] = view(r.trials, n, np.uint64)
+        elif n:
             def arr(p, count, dt):
                 return np.ctypeslib.as_array(p, shape=(count,)).astype(dt, copy=True)
             out["canonical"] = arr(r.canonical, n, np.uint8).astype(bool)
@@ -340,7 +350,6 @@ class Context:
             out["len_aut"] = arr(r.len_aut, n, np.uint8)
             out["auts_raw"] = np.ctypeslib.as_array(r.auts, shape=(n * r.aut_cap * 64,)).reshape(
                 n, r.aut_cap, 64).copy()
-        self._kinds = []
         return out
 
     def canonize_bibd(self, rows, v, b):
