@@ -225,6 +225,8 @@ def run_gpu(args, rank, world, local, dist):
     d_st = ctx.alloc(n)
     ctx.generate_sts_device(n, V, SEED, True, d_rows)
     ctx.stream_sync()
+    # the autotuner picks the check variant for this shape on a sample (setup, untimed)
+    variant, tune_ms = ctx.tune_bibd(min(n, 1 << 16), V, B, flags, d_rows)
     l2_flush = ctx.alloc(512 << 20)
     zeros = np.zeros(512 << 20, np.uint8)
 
@@ -288,6 +290,8 @@ def run_gpu(args, rank, world, local, dist):
             "config": {"workload": WORKLOAD if n == N_ITEMS else "%d items of: %s" % (n, WORKLOAD),
                        "ordering": "plain", "flags": FLAGS_NAME if args.mode == "autcanon" else "COMPLETE|RAW",
                        "items_per_step": n, "canonical_fraction": float(can.mean()),
+                       "variant": ["one pass", "two passes", "split by first row"][variant],
+                       "tune_ms_65536": [round(x, 2) for x in tune_ms],
                        "l2": "flushed between steps (512 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": None if e2e_dt is None else {"value": world * n / e2e_dt, "unit": "checks/s",

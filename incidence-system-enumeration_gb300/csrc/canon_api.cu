@@ -242,6 +242,10 @@ canon_ctx *canon_create(const canon_cfg *cfg) {
 }
 
 void canon_destroy(canon_ctx *c) {
+    if (c) {
+        cudaFree(c->d_split_parts);
+        cudaFree(c->d_split_stop);
+    }
     if (!c)
         return;
     cudaSetDevice(c->device);
@@ -532,15 +536,61 @@ int canon_canonize_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint64
     return CANON_OK;
 }
 
+namespace {
+
+uint32_t tune_key(uint32_t v, uint32_t b, uint32_t flags) { return v | (b << 8) | (flags << 16); }
+
+// the split variant's scratch, grown to n matrices of v rows
+cudaError_t split_scratch(canon_ctx *c, size_t n, uint32_t v) {
+    const size_t need = n * v;
+    if (need <= c->split_cap && c->d_split_stop)
+        return cudaSuccess;
+    cudaFree(c->d_split_parts);
+    cudaFree(c->d_split_stop);
+    c->d_split_parts = nullptr;
+    c->d_split_stop = nullptr;
+    c->split_cap = 0;
+    cudaError_t e = cudaMalloc((void **)&c->d_split_parts, need * sizeof(canon::SplitPart));
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&c->d_split_stop, n * sizeof(unsigned) + 64);
+    if (e == cudaSuccess)
+        c->split_cap = need;
+    return e;
+}
+
+// one resident check in the given variant (-1: the default rule)
+cudaError_t run_variant(canon_ctx *c, int variant, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
+                        const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16, uint64_t *d_aut,
+                        uint8_t *d_status, uint64_t *d_trials, const uint64_t *orders, cudaStream_t s) {
+    if (variant == canon::VARIANT_SPLIT) {
+        cudaError_t e = split_scratch(c, n, v);
+        if (e != cudaSuccess)
+            return e;
+        c->launches += 2;
+        return canon::launch_bibd_check_split(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
+                                              c->d_split_parts, c->d_split_stop, c->cfg.max_trials, c->d_ticket,
+                                              c->num_sms, s);
+    }
+    const bool ref = flags & (CANON_SAVE_AUTS | CANON_REFERENCE_ORDER);
+    const bool two = !ref && (variant < 0 ? (flags & (CANON_AUT_CANON | CANON_FULL_AUT)) != 0
+                                          : variant == canon::VARIANT_TWO_PASS);
+    c->launches += two ? ((d_witness16 || d_trials) ? 2 : 1) : 1;
+    return canon::launch_bibd_check_uniform(n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut, d_status,
+                                            d_trials, c->cfg.max_trials, c->d_ticket, c->num_sms, s, orders,
+                                            variant);
+}
+
+}  // namespace
+
 int canon_check_bibd_device(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                             const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16, uint64_t *d_aut,
                             uint8_t *d_status, uint64_t *d_trials, void *stream) {
     if (!c || !d_rows || !d_canonical)
         return fail(c, CANON_EINVAL, "null argument");
-    if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x37u))
+    if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x77u))
         return fail(c, CANON_EINVAL,
                     "check: need 1 <= v <= 16, 1 <= b <= 63, flags in COMPLETE|RAW|FULL_AUT|AUT_CANON|"
-                    "REFERENCE_ORDER");
+                    "REFERENCE_ORDER|VERDICT_ONLY");
     cudaSetDevice(c->device);
     cudaStream_t s = stream ? (cudaStream_t)stream : c->stream;
     uint64_t *orders = nullptr;
@@ -565,15 +615,113 @@ int canon_check_bibd_device(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, ui
         orders = c->d_orders;
         c->launches += 3 * ((n + 65535) / 65536);
     }
-    cudaError_t e = canon::launch_bibd_check_uniform(n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut,
-                                                     d_status, d_trials, c->cfg.max_trials, c->d_ticket,
-                                                     c->num_sms, s, orders);
+    int variant = -1;
+    if (!orders) {
+        const auto it = c->tuned.find(tune_key(v, b, flags));
+        if (it != c->tuned.end())
+            variant = it->second;
+    }
+    const cudaError_t e = run_variant(c, variant, n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut,
+                                      d_status, d_trials, orders, s);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "check launch");
-    // the |Aut| route is two kernels (lex-max pass, witness pass)
-    const bool two = !(flags & (CANON_SAVE_AUTS | CANON_REFERENCE_ORDER)) && (flags & (CANON_AUT_CANON | CANON_FULL_AUT));
-    c->launches += two ? ((d_witness16 || d_trials) ? 2 : 1) : 1;
     cudaEventRecord(c->ev1, s);
+    return CANON_OK;
+}
+
+int canon_tune_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                    canon_tune_result *out) {
+    if (!c || !d_rows || !out || !n)
+        return fail(c, CANON_EINVAL, "tune: null argument or empty sample");
+    if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX || (flags & ~0x77u))
+        return fail(c, CANON_EINVAL, "tune: bad shape or flags");
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    const bool ref = flags & (CANON_SAVE_AUTS | CANON_REFERENCE_ORDER);
+    const bool verdict = flags & CANON_VERDICT_ONLY;
+    const bool want_aut = flags & (CANON_AUT_CANON | CANON_FULL_AUT);
+    bool applies[3] = {true, !ref, verdict && !ref && !want_aut};
+    // outputs of every variant, compared with the one-pass variant's on the host
+    struct Out {
+        uint8_t *can = nullptr, *wit = nullptr, *st = nullptr;
+        uint64_t *aut = nullptr;
+    } o[3];
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+        if (!applies[k])
+            continue;
+        e = cudaMalloc((void **)&o[k].can, n);
+        if (e == cudaSuccess)
+            e = cudaMalloc((void **)&o[k].st, n);
+        if (e == cudaSuccess)
+            e = cudaMalloc((void **)&o[k].aut, (size_t)n * 16);
+        if (e == cudaSuccess && !verdict)
+            e = cudaMalloc((void **)&o[k].wit, (size_t)n * 16);
+    }
+    std::vector<uint8_t> can0(n), st0(n), wit0(verdict ? 0 : (size_t)n * 16), can1(n), st1(n),
+        wit1(verdict ? 0 : (size_t)n * 16);
+    std::vector<uint64_t> aut0((size_t)n * 2), aut1((size_t)n * 2);
+    float ms[3] = {-1.f, -1.f, -1.f};
+    int best = -1;
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+        if (!applies[k])
+            continue;
+        // one untimed run, then two timed ones
+        e = run_variant(c, k, n, v, b, flags, d_rows, o[k].can, o[k].wit, o[k].aut, o[k].st, nullptr, nullptr, s);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(s);
+        float t = 0.f;
+        for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+            cudaEventRecord(c->ev0, s);
+            e = run_variant(c, k, n, v, b, flags, d_rows, o[k].can, o[k].wit, o[k].aut, o[k].st, nullptr, nullptr,
+                            s);
+            cudaEventRecord(c->ev1, s);
+            if (e == cudaSuccess)
+                e = cudaEventSynchronize(c->ev1);
+            float dt = 0.f;
+            cudaEventElapsedTime(&dt, c->ev0, c->ev1);
+            t += dt;
+        }
+        if (e != cudaSuccess)
+            break;
+        ms[k] = t / 2.f;
+        // identical outputs, or the variant is not kept
+        std::vector<uint8_t> &cn = k ? can1 : can0, &sn = k ? st1 : st0, &wn = k ? wit1 : wit0;
+        std::vector<uint64_t> &an = k ? aut1 : aut0;
+        e = cudaMemcpy(cn.data(), o[k].can, n, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(sn.data(), o[k].st, n, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(an.data(), o[k].aut, (size_t)n * 16, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && !verdict)
+            e = cudaMemcpy(wn.data(), o[k].wit, (size_t)n * 16, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            break;
+        bool same = true;
+        for (uint32_t i = 0; k && same && i < n; ++i) {
+            same = can1[i] == can0[i] && st1[i] == st0[i];
+            if (same && (can0[i] || want_aut))
+                same = aut1[2 * i] == aut0[2 * i] && aut1[2 * i + 1] == aut0[2 * i + 1];
+            if (same && !verdict && !can0[i])
+                same = std::memcmp(&wit1[(size_t)i * 16], &wit0[(size_t)i * 16], v) == 0;
+        }
+        if (!same)
+            ms[k] = -2.f;
+        else if (best < 0 || ms[k] < ms[best])
+            best = k;
+    }
+    for (int k = 0; k < 3; ++k) {
+        cudaFree(o[k].can);
+        cudaFree(o[k].st);
+        cudaFree(o[k].aut);
+        cudaFree(o[k].wit);
+    }
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "tune");
+    c->tuned[tune_key(v, b, flags)] = best;
+    out->variant = best;
+    for (int k = 0; k < 3; ++k)
+        out->ms[k] = ms[k];
     return CANON_OK;
 }
 

@@ -411,11 +411,13 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
                                       const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16,
                                       uint64_t *d_aut, uint8_t *d_status, uint64_t *d_trials,
                                       uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s,
-                                      const uint64_t *d_orders) {
+                                      const uint64_t *d_orders, int variant) {
     if (!n)
         return cudaSuccess;
     const int need = (int)((n + TPB - 1) / TPB);
-    if (!(flags & (F_SAVE_AUTS | F_REFERENCE_ORDER)) && (flags & (F_AUT_CANON | F_FULL_AUT))) {
+    const bool ref_order = flags & (F_SAVE_AUTS | F_REFERENCE_ORDER);
+    const bool two = !ref_order && (variant < 0 ? (flags & (F_AUT_CANON | F_FULL_AUT)) != 0 : variant == 1);
+    if (two) {
         // |Aut| wanted for every matrix: two passes, the lex-max search for all,
         // the reference-order witness for the rejected ones.  (Without it the
         // single pass below rejects most non-canonical matrices in a few trials

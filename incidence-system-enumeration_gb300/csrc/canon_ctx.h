@@ -1,5 +1,6 @@
 // canon_ctx.h -- the context behind the C ABI's opaque canon_ctx handle.
 #pragma once
+#include <map>
 #include <string>
 #include <vector>
 
@@ -34,6 +35,12 @@ struct canon_ctx {
     size_t scratch_bytes = 0;
     uint64_t *d_orders = nullptr;
     size_t d_orders_bytes = 0;
+    // autotuned check variant per (v, b, flags) (canon_tune_bibd), and the split
+    // variant's scratch
+    std::map<uint32_t, int> tuned;
+    canon::SplitPart *d_split_parts = nullptr;
+    unsigned *d_split_stop = nullptr;
+    size_t split_cap = 0;              // matrices x rows the scratch holds
     std::string err;
     float last_ms = 0.f;
     uint64_t launches = 0;

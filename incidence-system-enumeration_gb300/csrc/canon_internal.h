@@ -59,7 +59,11 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
                                       const uint64_t *d_rows, uint8_t *d_canonical,
                                       uint8_t *d_witness16, uint64_t *d_aut, uint8_t *d_status,
                                       uint64_t *d_trials, uint64_t max_trials, unsigned *d_ticket,
-                                      int num_sms, cudaStream_t s, const uint64_t *d_orders = nullptr);
+                                      int num_sms, cudaStream_t s, const uint64_t *d_orders = nullptr,
+                                      int variant = -1);
+// check variants with identical outputs (canon_tune_bibd): one pass, two passes,
+// the search split by first row (verdict only)
+enum : int { VARIANT_SINGLE = 0, VARIANT_TWO_PASS = 1, VARIANT_SPLIT = 2 };
 // one share of a lex-max search split by first row (bibd_split_kernel)
 struct SplitPart {
     uint64_t leaves;

@@ -58,6 +58,7 @@ HEADER_SYMBOLS = [
     "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys", "canon_mlp_features",
     "canon_label_first_rows", "canon_mlp_forward", "canon_mlp_grad", "canon_mlp_train",
     "canon_design_properties", "canon_report_bibd", "canon_ksys_cycles", "canon_report_ksys",
+    "canon_tune_bibd",
 ]
 MLP_PARAMS = 128 * 64 + 128 + 128 * 128 + 128 + 128 + 1
 
@@ -104,6 +105,13 @@ class EnumStats(ctypes.Structure):
 
 DESIGN_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint32,
                              ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64)
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("variant", ctypes.c_int), ("ms", ctypes.c_float * 3)]
+
+
+VARIANT_SINGLE, VARIANT_TWO_PASS, VARIANT_SPLIT = 0, 1, 2
 
 
 class MlpWeights(ctypes.Structure):
@@ -176,6 +184,7 @@ def load_library(path=LIB_PATH):
     L.canon_mlp_train.argtypes = [vp, u64, vp, vp, u32, u32, ctypes.c_float, fp, fp]
     L.canon_set_ordering.argtypes = [vp, ctypes.POINTER(MlpWeights)]
     u8p, sz = ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t
+    L.canon_tune_bibd.argtypes = [vp, u32, u32, u32, u32, vp, ctypes.POINTER(TuneResult)]
     L.canon_design_properties.argtypes = [vp, u32, u32, u32, u64p, u8p, u8p]
     L.canon_report_bibd.argtypes = [u32, u32, u32, u32, u32, u32, u64p, u8p, u8p, u64, ctypes.c_double,
                                     ctypes.c_char_p, sz]
@@ -400,6 +409,13 @@ class Context:
         st = EnumStats()
         self._check(self.lib.canon_enumerate_bibd(self.h, v, b, r, k, lam, c, None, ctypes.byref(st)))
         return found, st
+
+    def tune_bibd(self, n, v, b, flags, d_rows):
+        """Autotunes the check variant for (v, b, flags) on n device-resident matrices;
+        returns (variant kept, [ms per variant: -1 not applicable, -2 outputs differed])."""
+        r = TuneResult()
+        self._check(self.lib.canon_tune_bibd(self.h, n, v, b, flags, d_rows, ctypes.byref(r)))
+        return r.variant, [float(x) for x in r.ms]
 
     def design_properties(self, designs):
         """(simple, transitive) flags of complete designs (v x b 0/1 matrices)."""

@@ -175,13 +175,36 @@ int canon_canonize_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint
 /* Same check as canon_submit_bibd + canon_sync for device pointers, all items
  * with v rows; launched on `stream` (a cudaStream_t, NULL = the context's).
  * Output arrays are device pointers (any may be NULL except canonical).
- * flags: CANON_COMPLETE, CANON_RAW, CANON_FULL_AUT, CANON_AUT_CANON, CANON_REFERENCE_ORDER. */
+ * flags: CANON_COMPLETE, CANON_RAW, CANON_FULL_AUT, CANON_AUT_CANON, CANON_REFERENCE_ORDER,
+ * CANON_VERDICT_ONLY.  A variant kept by canon_tune_bibd for (v, b, flags) is used. */
 int canon_check_bibd_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                             const uint64_t *d_rows, uint8_t *d_canonical, uint8_t *d_witness16,
                             uint64_t *d_aut, uint8_t *d_status, uint64_t *d_trials, void *stream);
 /* Seeded STS(v) batch on the device (Stinson hill-climbing + uniform row and
  * column permutations); if canon_odd, odd items are replaced by their
  * canonical form.  rows: device pointer [n*v]. */
+/* ---- autotuning per design shape ----
+ * Times the check variants that give identical outputs for (v, b, flags) on n
+ * device-resident matrices, verifies them against the one-pass variant and keeps
+ * the fastest for later canon_check_bibd_device calls with the same (v, b, flags)
+ * on this context (without a learned order):
+ *   CANON_VARIANT_SINGLE   one pass: short reference-order search, lex-max search
+ *                          when it does not decide;
+ *   CANON_VARIANT_TWO_PASS lex-max pass for all, witness pass for the rejected
+ *                          (not with CANON_SAVE_AUTS / CANON_REFERENCE_ORDER);
+ *   CANON_VARIANT_SPLIT    the lex-max search split over one thread per (matrix,
+ *                          first row) (CANON_VERDICT_ONLY without |Aut| flags).
+ * ms[i]: the variant's device time, -1 when it does not apply, -2 when its
+ * outputs differed (never chosen). */
+#define CANON_VARIANT_SINGLE   0
+#define CANON_VARIANT_TWO_PASS 1
+#define CANON_VARIANT_SPLIT    2
+typedef struct {
+    int   variant;      /* the variant kept */
+    float ms[3];
+} canon_tune_result;
+int canon_tune_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                    canon_tune_result *out);
 int canon_generate_sts_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint64_t seed, int canon_odd,
                               uint64_t *d_rows, void *stream);
 /* Device memory helpers so callers without a CUDA toolchain can hold batches in HBM. */

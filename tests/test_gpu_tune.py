@@ -1,0 +1,62 @@
+"""canon_tune_bibd: the autotuner times the check variants that give identical
+outputs for a design shape, keeps the fastest, and later checks of that shape
+use it with unchanged outputs (compared with the untuned path and the oracle)."""
+import numpy as np
+import pytest
+
+import cases
+import ise_gb300 as G
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def sample(n, seed):
+    """STS(15) rows: random relabellings and canonical forms, alternating."""
+    sts = cases.load_sts15()
+    rows = np.zeros((n, 15), np.uint64)
+    for i in range(n):
+        rows[i] = oracle.sts_random_rows(15, seed, i) if i % 2 == 0 else G.pack_rows(sts[i % len(sts)][0])
+    return rows
+
+
+def run(ctx, rows, flags):
+    n, v = rows.shape
+    d_rows = ctx.alloc(rows.nbytes)
+    ctx.h2d(d_rows, rows)
+    d_can, d_aut, d_st, d_wit = ctx.alloc(n), ctx.alloc(16 * n), ctx.alloc(n), ctx.alloc(16 * n)
+    ctx.check_bibd_device(n, v, 35, flags, d_rows, d_can, d_wit, d_aut, d_st)
+    ctx.stream_sync()
+    out = dict(canonical=ctx.d2h(np.zeros(n, np.uint8), d_can), status=ctx.d2h(np.zeros(n, np.uint8), d_st),
+               aut=ctx.d2h(np.zeros(2 * n, np.uint64), d_aut).reshape(n, 2),
+               witness=ctx.d2h(np.zeros(16 * n, np.uint8), d_wit).reshape(n, 16))
+    return out, d_rows
+
+
+@pytest.mark.parametrize("flags", [G.COMPLETE | G.RAW | G.AUT_CANON, G.COMPLETE | G.RAW,
+                                   G.COMPLETE | G.RAW | G.VERDICT_ONLY])
+def test_tuned_variant_keeps_outputs(flags):
+    rows = sample(96, 99)
+    n = len(rows)
+    plain_ctx = G.Context(max_items=1024)
+    ref, _ = run(plain_ctx, rows, flags)
+    plain_ctx.close()
+    ctx = G.Context(max_items=1024)
+    d_rows = ctx.alloc(rows.nbytes)
+    ctx.h2d(d_rows, rows)
+    variant, ms = ctx.tune_bibd(n, 15, 35, flags, d_rows)
+    assert ms[0] > 0 and ms[1] > 0                      # one pass and two passes both apply
+    assert (ms[2] > 0) == bool(flags & G.VERDICT_ONLY)   # the split search only for verdicts
+    assert -2.0 not in ms                                # every variant matched the one-pass outputs
+    assert variant == min((k for k in range(3) if ms[k] > 0), key=lambda k: ms[k])
+    got, _ = run(ctx, rows, flags)
+    ctx.close()
+    assert np.array_equal(got["canonical"], ref["canonical"]) and not got["status"].any()
+    for i in range(n):
+        M = oracle.bibd_normalize(oracle.rows_to_matrix(rows[i], 35))
+        o = oracle.bibd_test(M, oracle.SAVE_ROW_PERM | oracle.SAVE_ROW_TO_CHANGE)
+        assert bool(got["canonical"][i]) == o["canonical"]
+        if o["canonical"]:
+            assert int(got["aut"][i][0]) == o["aut"]
+        elif not flags & G.VERDICT_ONLY:
+            assert bytes(got["witness"][i][:15]) == o["witness"]
