@@ -377,16 +377,18 @@ int canon_sync(canon_ctx *c, canon_results *r) {
         } else if (c->n_bitems) {
             // items that all want |Aut| without the reference order take the two-pass check
             bool two_pass = true;
-            uint32_t max_b = 0;
+            uint32_t max_b = 0, max_v = 0;
             for (uint32_t i = 0; i < c->n_bitems; ++i) {
                 const uint8_t f = c->h_bitems[i].flags;
                 two_pass = two_pass && (f & (canon::F_AUT_CANON | canon::F_FULL_AUT)) &&
                            !(f & (canon::F_SAVE_AUTS | canon::F_REFERENCE_ORDER));
                 if (c->h_bitems[i].ncols > max_b)
                     max_b = c->h_bitems[i].ncols;
+                if (c->h_bitems[i].nrows > max_v)
+                    max_v = c->h_bitems[i].nrows;
             }
             e = two_pass ? canon::launch_bibd_check_two_pass(c->d_bitems, c->n_bitems, c->d_words, c->d_out,
-                                                             c->cfg.max_trials, c->d_ticket, c->num_sms, s, max_b)
+                                                             c->cfg.max_trials, c->d_ticket, c->num_sms, s, max_b, max_v)
                          : canon::launch_bibd_check(c->d_bitems, c->n_bitems, c->d_words, c->d_out,
                                                     c->cfg.max_trials, c->d_ticket, c->num_sms, s);
             if (e != cudaSuccess)

@@ -80,17 +80,19 @@ __global__ void __launch_bounds__(TPB) bibd_uniform_kernel(uint32_t n_items, uin
 // sized by BCAP) and fewer registers.  Pass 2 (bibd_witness_kernel): the
 // reference-order search, only for the matrices found non-canonical, gives the
 // first rejecting permutation.
-template <int BCAP>
+// BCAP / VCAP bound the columns / rows of the launch: the smaller the per-thread
+// state, the more blocks fit an SM (v <= 15, b <= 35: 348 B, 10 blocks of 64).
+template <int BCAP, int VCAP>
 __global__ void __launch_bounds__(TPB) bibd_max_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
                                                        const uint64_t *__restrict__ rows, uint8_t *canonical,
                                                        uint64_t *aut, uint8_t *status, uint64_t max_nodes,
                                                        unsigned *ticket, const uint64_t *__restrict__ orders) {
-    __shared__ uint64_t s_rows[VMAX * TPB];
-    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
-    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint64_t s_rows[VCAP * TPB];
+    __shared__ uint64_t s_lvl[(VCAP + 1) * TPB];
+    __shared__ uint16_t s_vd[VCAP * TPB];
     __shared__ uint16_t s_cm[BCAP * TPB];
     const unsigned tid = threadIdx.x;
-    Smem sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
     for (;;) {
         const unsigned it = atomicAdd(ticket, 1u);
         if (it >= n_items)
@@ -152,16 +154,16 @@ __global__ void __launch_bounds__(TPB) bibd_witness_kernel(uint32_t n_items, uin
 
 // The two passes over work items of any shape (the batched path); BCAP bounds the
 // columns of every item of the launch, as in bibd_max_kernel.
-template <unsigned BCAP>
+template <unsigned BCAP, unsigned VCAP>
 __global__ void __launch_bounds__(TPB) bibd_items_max_kernel(const Item *__restrict__ items, uint32_t n_items,
                                                              const uint64_t *__restrict__ words, Outputs out,
                                                              uint64_t max_nodes, unsigned *ticket) {
-    __shared__ uint64_t s_rows[VMAX * TPB];
-    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
-    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint64_t s_rows[VCAP * TPB];
+    __shared__ uint64_t s_lvl[(VCAP + 1) * TPB];
+    __shared__ uint16_t s_vd[VCAP * TPB];
     __shared__ uint16_t s_cm[BCAP * TPB];
     const unsigned tid = threadIdx.x;
-    Smem sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
     for (;;) {
         const unsigned it = atomicAdd(ticket, 1u);
         if (it >= n_items)
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(TPB) bibd_items_max_kernel(const Item *__restr
         const unsigned n = item.nrows, b = item.ncols, o_i = item.out_idx;
         MaxOut mo{false, false, 0, 0, 0};
         uint8_t st = 0;
-        if (item.kind != KIND_BIBD || n < 1 || n > VMAX || b < 1 || b > BMAX || b > BCAP ||
+        if (item.kind != KIND_BIBD || n < 1 || n > VCAP || b < 1 || b > BMAX || b > BCAP ||
             !load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW)) {
             st = ST_BADINPUT;
         } else {
@@ -303,10 +305,10 @@ __global__ void __launch_bounds__(TPB) bibd_split_kernel(uint32_t n_items, uint3
                                                          unsigned *stop, uint64_t max_nodes, unsigned *ticket) {
     __shared__ uint64_t s_rows[VMAX * TPB];
     __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
-    __shared__ uint32_t s_vd[VMAX * TPB];
+    __shared__ uint16_t s_vd[VMAX * TPB];
     __shared__ uint16_t s_cm[64 * TPB];
     const unsigned tid = threadIdx.x;
-    Smem sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
     const uint64_t total = (uint64_t)n_items * v;
     for (;;) {
         const unsigned it = atomicAdd(ticket, 1u);
@@ -383,20 +385,24 @@ cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint6
 
 cudaError_t launch_bibd_check_two_pass(const Item *d_items, uint32_t n_items, const uint64_t *d_words, Outputs out,
                                        uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s,
-                                       uint32_t max_b) {
+                                       uint32_t max_b, uint32_t max_v) {
     if (!n_items)
         return cudaSuccess;
     cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
     const int need = (int)((n_items + TPB - 1) / TPB);
-    const bool narrow = max_b <= 40;
-    int grid = narrow ? blocks_for((const void *)bibd_items_max_kernel<40>, num_sms)
-                      : blocks_for((const void *)bibd_items_max_kernel<64>, num_sms);
+    const int shape = (max_v <= 15 && max_b <= 35) ? 0 : (max_b <= 40 ? 1 : 2);
+    const void *kfn = shape == 0 ? (const void *)bibd_items_max_kernel<35, 15>
+                      : shape == 1 ? (const void *)bibd_items_max_kernel<40, 16>
+                                   : (const void *)bibd_items_max_kernel<64, 16>;
+    int grid = blocks_for(kfn, num_sms);
     if (grid > need)
         grid = need;
-    if (narrow)
-        bibd_items_max_kernel<40><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+    if (shape == 0)
+        bibd_items_max_kernel<35, 15><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+    else if (shape == 1)
+        bibd_items_max_kernel<40, 16><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
     else
-        bibd_items_max_kernel<64><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+        bibd_items_max_kernel<64, 16><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
@@ -423,16 +429,22 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
         // single pass below rejects most non-canonical matrices in a few trials
         // of the reference order and runs the lex-max search only for the rest.)
         cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
-        int grid = b <= 40 ? blocks_for((const void *)bibd_max_kernel<40>, num_sms)
-                           : blocks_for((const void *)bibd_max_kernel<64>, num_sms);
+        // the smallest instance that holds the shape
+        const void *kfn = (v <= 15 && b <= 35) ? (const void *)bibd_max_kernel<35, 15>
+                          : (b <= 40)          ? (const void *)bibd_max_kernel<40, 16>
+                                               : (const void *)bibd_max_kernel<64, 16>;
+        int grid = blocks_for(kfn, num_sms);
         if (grid > need)
             grid = need;
-        if (b <= 40)
-            bibd_max_kernel<40><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status, max_trials,
-                                                     tk, d_orders);
+        if (v <= 15 && b <= 35)
+            bibd_max_kernel<35, 15><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
+                                                         max_trials, tk, d_orders);
+        else if (b <= 40)
+            bibd_max_kernel<40, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
+                                                         max_trials, tk, d_orders);
         else
-            bibd_max_kernel<64><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status, max_trials,
-                                                     tk, d_orders);
+            bibd_max_kernel<64, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
+                                                         max_trials, tk, d_orders);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;
@@ -590,7 +602,7 @@ cudaError_t launch_bibd_check_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32
     // route is the one canon_sync takes for the same flags
     const bool two_pass = (flags & (F_AUT_CANON | F_FULL_AUT)) && !(flags & (F_SAVE_AUTS | F_REFERENCE_ORDER));
     if (two_pass)
-        return launch_bibd_check_two_pass(items, n, d_rows, out, max_trials, counter, sms, s, b);
+        return launch_bibd_check_two_pass(items, n, d_rows, out, max_trials, counter, sms, s, b, v);
     return launch_bibd_check(items, n, d_rows, out, max_trials, counter, sms, s);
 }
 

@@ -177,13 +177,19 @@ __device__ __forceinline__ uint64_t merge_orbits(uint64_t perm, uint64_t orb, un
     return orb;
 }
 
-struct Smem {
+template <typename VD>
+struct SmemT {
     uint64_t *rows;  // rows[r * TPB]: row r as a bit set of columns
     uint64_t *lvl;   // lvl[r * TPB]: orbit-start masks of level r (also scratch)
     uint8_t *pc;     // pc[j * TPB]: permColumn
     uint16_t *cm;    // cm[c * TPB]: column c as a bit set of rows
-    uint32_t *vd;    // vd[r * TPB]: verdicts at level r, bits 0-15 "greater" (reject), 16-31 "equal"
+    VD *vd;          // vd[r * TPB]: search(): verdicts at level r, bits 0-15 "greater"
+                     // (reject), 16-31 "equal"; max_search(): the rows still to visit
 };
+// the reference-order search needs 32-bit verdict words; the lex-max search alone
+// (its own kernels) keeps 16-bit row sets, 32 B less shared memory per thread
+using Smem = SmemT<uint32_t>;
+using SmemMax = SmemT<uint16_t>;
 
 #define R_(r) sm.rows[(r) * TPB]
 #define L_(r) sm.lvl[(r) * TPB]
@@ -204,7 +210,8 @@ struct CheckOut {
 // pattern read from row 0 down.  Equal in content to GenerateBinaryColumnOrbits()
 // applied to rows 0..n-1 (MatrixCanonChecker.cpp:186-263), which swaps the first 0
 // and the last 1 inside every orbit until each row is 1s-first.
-__device__ void normalize_columns(Smem sm, unsigned n, unsigned b) {
+template <typename S>
+__device__ void normalize_columns(S sm, unsigned n, unsigned b) {
     // codes (16 bit) are kept four to a word in the lvl scratch area
     for (unsigned c = 0; c < b; ++c) {
         unsigned code = 0;
@@ -239,7 +246,8 @@ __device__ void normalize_columns(Smem sm, unsigned n, unsigned b) {
 
 // Orbit-start masks of every level and the column-major copy of the matrix;
 // returns false if a row is not 1s-first inside the orbits of the rows above it.
-__device__ bool build_levels(Smem sm, unsigned n, unsigned b) {
+template <typename S>
+__device__ bool build_levels(S sm, unsigned n, unsigned b) {
     const uint64_t cols = (1ull << b) - 1ull;
     uint64_t m = 1ull;
     bool ok = true;
@@ -588,7 +596,8 @@ struct MaxOut {
 // lv: inside every orbit of level lv that the bound's row lv splits, the columns
 // holding a 1 in row `cand` move to the front.  CM_() holds the row masks of the
 // columns in arranged order (the column masks permuted by permColumn).
-__device__ __forceinline__ void refine_arranged(Smem sm, unsigned lv, unsigned cand, unsigned b) {
+template <typename S>
+__device__ __forceinline__ void refine_arranged(S sm, unsigned lv, unsigned cand, unsigned b) {
     const uint64_t m = L_(lv) | (1ull << b);
     uint64_t split = L_(lv + 1) & ~L_(lv);
     while (split) {
@@ -624,7 +633,8 @@ __device__ __forceinline__ void refine_arranged(Smem sm, unsigned lv, unsigned c
 // combine as |Aut| = (sum of orbit0) x (that product).
 // stop: a flag that another thread of a split search raises once it has shown M
 // not to be canonical; it is read every 64 nodes and ends this share early.
-__device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o,
+template <typename S>
+__device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o,
                            uint64_t order0 = ID16, bool prune = true, bool stop_on_improve = false,
                            unsigned root_mask = 0xFFFFu, const volatile unsigned *stop = nullptr) {
     const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
@@ -752,7 +762,7 @@ __device__ void max_search(Smem sm, unsigned n, unsigned b, uint64_t max_nodes, 
                 L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
                 valid = i + 1;
             }
-            VD_(i) = (i == 0) ? (tied & root_mask) : tied;     // children still to visit
+            VD_(i) = (i == 0) ? (tied & root_mask) : tied;     // children still to visit (16 bits)
         }
         // next child of the node at level i
         unsigned rem = VD_(i);
@@ -827,7 +837,8 @@ __device__ __forceinline__ void reset_out(CheckOut &o) {
     o.len_aut = 0;
 }
 
-__device__ __forceinline__ bool load_rows(Smem sm, const uint64_t *src, unsigned n, unsigned b, unsigned flags) {
+template <typename S>
+__device__ __forceinline__ bool load_rows(S sm, const uint64_t *src, unsigned n, unsigned b, unsigned flags) {
     for (unsigned r = 0; r < n; ++r)
         R_(r) = src[r];
     if (flags & F_RAW)

@@ -54,7 +54,7 @@ cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint6
 // want |Aut| (CANON_AUT_CANON or CANON_FULL_AUT) without the reference order; d_ticket: two words
 cudaError_t launch_bibd_check_two_pass(const Item *d_items, uint32_t n_items, const uint64_t *d_words,
                                        Outputs out, uint64_t max_trials, unsigned *d_ticket, int num_sms,
-                                       cudaStream_t s, uint32_t max_b = 63);
+                                       cudaStream_t s, uint32_t max_b = 63, uint32_t max_v = 16);
 cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
                                       const uint64_t *d_rows, uint8_t *d_canonical,
                                       uint8_t *d_witness16, uint64_t *d_aut, uint8_t *d_status,
