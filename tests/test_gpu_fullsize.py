@@ -1,0 +1,60 @@
+"""Config 2 at its full size (1,048,576 STS(15) from the bench seed) through
+size-independent properties: the canonical-form half of the batch is exactly
+the canonical form of the other generation's items, every such form is reported
+canonical with the |Aut| that the check gives the original matrix, canonizing
+the originals reproduces the forms, and every |Aut| is the order of one of the
+80 STS(15) isomorphism classes."""
+import numpy as np
+import pytest
+
+import cases
+import ise_gb300 as G
+
+pytestmark = pytest.mark.gpu
+
+N = 1 << 20
+SEED = 20241203          # the bench's seed
+V, B = 15, 35
+
+
+def check(ctx, d_rows, flags):
+    d_can, d_aut, d_st = ctx.alloc(N), ctx.alloc(16 * N), ctx.alloc(N)
+    ctx.check_bibd_device(N, V, B, flags, d_rows, d_can, None, d_aut, d_st)
+    ctx.stream_sync()
+    can = ctx.d2h(np.zeros(N, np.uint8), d_can)
+    aut = ctx.d2h(np.zeros(2 * N, np.uint64), d_aut).reshape(N, 2)
+    st = ctx.d2h(np.zeros(N, np.uint8), d_st)
+    for p in (d_can, d_aut, d_st):
+        ctx.free(p)
+    return can, aut, st
+
+
+def test_config2_full_size_properties():
+    ctx = G.Context(max_items=N)
+    try:
+        d_a, d_b = ctx.alloc(N * V * 8), ctx.alloc(N * V * 8)
+        ctx.generate_sts_device(N, V, SEED, False, d_a)      # random relabellings only
+        ctx.generate_sts_device(N, V, SEED, True, d_b)       # odd items: their canonical form
+        ctx.stream_sync()
+        A = ctx.d2h(np.zeros(N * V, np.uint64), d_a).reshape(N, V)
+        Bm = ctx.d2h(np.zeros(N * V, np.uint64), d_b).reshape(N, V)
+        assert np.array_equal(A[0::2], Bm[0::2])
+        flags = G.COMPLETE | G.RAW | G.AUT_CANON
+        can_a, aut_a, st_a = check(ctx, d_a, flags)
+        can_b, aut_b, st_b = check(ctx, d_b, flags)
+        assert not st_a.any() and not st_b.any()
+        assert can_b[1::2].all()
+        assert np.array_equal(aut_b[1::2], aut_a[1::2])
+        assert np.array_equal(can_b[0::2], can_a[0::2]) and np.array_equal(aut_b[0::2], aut_a[0::2])
+        orders = {a for _, a in cases.load_sts15()}
+        assert set(int(x) for x in np.unique(aut_a[:, 0])) <= orders and not aut_a[:, 1].any()
+        # random relabellings are almost never already canonical
+        assert can_a[0::2].mean() < 1e-3
+        # canonizing the originals of the odd half reproduces the forms, with the same |Aut|
+        forms, aut_c = ctx.canonize_bibd(A[1::2], V, B)
+        assert np.array_equal(np.asarray(forms).reshape(-1, V), Bm[1::2])
+        assert np.array_equal(np.array(aut_c, dtype=np.uint64), aut_a[1::2, 0])
+        ctx.free(d_a)
+        ctx.free(d_b)
+    finally:
+        ctx.close()
