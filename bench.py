@@ -462,7 +462,7 @@ def run_mix(args):
         for _ in range(args.steps):
             t0 = time.perf_counter()
             submit()
-            r = ctx.sync()
+            r = ctx.sync(raw=True)
             walls.append(time.perf_counter() - t0)
             kms.append(r["kernel_ms"])
     assert r["n"] == n and not r["status"].any()
@@ -473,7 +473,7 @@ def run_mix(args):
             "config": {"workload": "%d partial matrices: 40%% STS(15) 5-15 rows, 30%% BIBD(8,14,7,4,3) 4-8, "
                                    "20%% BIBD(11,11,5,5,2) 4-11, 10%% K10 3-9 rounds; prefixes of randomly "
                                    "relabelled designs, seed %d" % (n, SEED + 3),
-                       "canonical_fraction": float(r["canonical"].mean())},
+                       "canonical_fraction": float(r["canonical"].astype(np.float64).mean())},
             "e2e": {"value": n * args.steps / sum(walls), "unit": "checks/s",
                     "h2d_bytes_per_step": int(sum(b[3].nbytes for b in batches) + 16 * n),
                     "d2h_bytes_per_step": 51 * n},

@@ -623,8 +623,8 @@ __device__ __forceinline__ void refine_arranged(S sm, unsigned lv, unsigned cand
 
 // order0: the order in which the rows are tried as the first row (nibble-packed;
 // ID16 = increasing, the plain order).  Only the search order changes with it;
-// a reordered first level turns the automorphism pruning off (it needs the
-// identity path first).  stop_on_improve: return as soon as M is known not to be
+// with pruning, row 0 (the identity path) still comes first while M may be
+// canonical, and the other first rows follow order0.  stop_on_improve: return as soon as M is known not to be
 // canonical (leaves, first_rows and R_() are then incomplete).  root_mask: the
 // rows that may come first (a search split over several threads by first row).
 // With pruning and M canonical, orbit0 counts the rows of root_mask found in the
@@ -641,7 +641,6 @@ __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, Max
     const uint64_t cols = (1ull << b) - 1ull;
     const uint64_t sentinel = 1ull << b;
     const uint64_t nmask1 = (n >= 16) ? NIB1 : (NIB1 & ((1ull << (4 * n)) - 1ull));
-    prune = prune && order0 == ID16;
     o.improved = false;
     o.timeout = false;
     o.leaves = 0;
@@ -791,7 +790,7 @@ __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, Max
             continue;
         }
         unsigned x = __ffs(rem) - 1;
-        if (i == 0 && order0 != ID16) {
+        if (i == 0 && order0 != ID16 && !(pr && (rem & 1u))) {
             for (unsigned q = 0; q < n; ++q) {
                 const unsigned c = pg(order0, q);
                 if ((rem >> c) & 1u) {

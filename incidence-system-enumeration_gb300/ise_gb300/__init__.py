@@ -343,6 +343,7 @@ class Context:
             out["reject_row"] = view(r.reject_row, n, np.uint8)
             out["row_to_change"] = view(r.row_to_change, n, np.uint8)
             out["trials"] = view(r.trials, n, np.uint64)
+            out["player_index"] = view(r.player_index, n, np.int32)
         elif n:
             def arr(p, count, dt):
                 return np.ctypeslib.as_array(p, shape=(count,)).astype(dt, copy=True)
