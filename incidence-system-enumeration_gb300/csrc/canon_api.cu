@@ -544,7 +544,7 @@ uint32_t tune_key(uint32_t v, uint32_t b, uint32_t flags) { return v | (b << 8) 
 
 // the split variant's scratch, grown to n matrices of v rows
 cudaError_t split_scratch(canon_ctx *c, size_t n, uint32_t v) {
-    const size_t need = n * v;
+    const size_t need = n * v * (canon::split_levels(n, v) == 2 ? v : 1);
     if (need <= c->split_cap && c->d_split_stop)
         return cudaSuccess;
     cudaFree(c->d_split_parts);
@@ -554,7 +554,7 @@ cudaError_t split_scratch(canon_ctx *c, size_t n, uint32_t v) {
     c->split_cap = 0;
     cudaError_t e = cudaMalloc((void **)&c->d_split_parts, need * sizeof(canon::SplitPart));
     if (e == cudaSuccess)
-        e = cudaMalloc((void **)&c->d_split_stop, n * sizeof(unsigned) + 64);
+        e = cudaMalloc((void **)&c->d_split_stop, need * sizeof(unsigned) + 64);   // need >= n
     if (e == cudaSuccess)
         c->split_cap = need;
     return e;

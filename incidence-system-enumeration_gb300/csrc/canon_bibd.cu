@@ -293,34 +293,42 @@ __global__ void __launch_bounds__(TPB) bibd_label_kernel(uint32_t n_items, uint3
     }
 }
 
-// The verdict of a small batch with the lex-max search split by first row: one
-// thread per (matrix, first row), so a level of few matrices still fills the GPU
-// and a check's latency is that of its largest subtree, not of the whole search.
-// Thread j searches the subtrees that start with row j (row 0: the identity path,
-// which gives the orbit lengths below level 0); the first of a matrix's threads
-// to improve on M raises its stop flag.  bibd_split_combine_kernel then forms the
-// verdict and |Aut| = (rows in the orbit of row 0) x (row 0's product below).
+// The verdict of a small batch with the lex-max search split by its first rows:
+// one thread per (matrix, first row) -- or, with levels = 2, per (matrix, first
+// row, second row) -- so a level of few matrices still fills the GPU and a
+// check's latency is that of its largest subtree, not of the whole search.
+// Thread (0[, 1]) takes the identity path and gives the orbit lengths below; the
+// others stop each subtree at its first automorphism; the first thread of a
+// matrix to improve on M raises its stop flag.  bibd_split_combine_kernel forms
+// the verdict and |Aut| = |orbit of row 0| (x |orbit of row 1 under the
+// stabilizer of row 0|) x the identity thread's product.
 __global__ void __launch_bounds__(TPB) bibd_split_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
-                                                         const uint64_t *__restrict__ rows, SplitPart *parts,
-                                                         unsigned *stop, uint64_t max_nodes, unsigned *ticket) {
+                                                         uint32_t levels, const uint64_t *__restrict__ rows,
+                                                         SplitPart *parts, unsigned *stop, uint64_t max_nodes,
+                                                         unsigned *ticket) {
     __shared__ uint64_t s_rows[VMAX * TPB];
     __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
     __shared__ uint16_t s_vd[VMAX * TPB];
     __shared__ uint16_t s_cm[64 * TPB];
     const unsigned tid = threadIdx.x;
     SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
-    const uint64_t total = (uint64_t)n_items * v;
+    const unsigned per = levels == 2 ? v * v : v;
+    const uint64_t total = (uint64_t)n_items * per;
     for (;;) {
         const unsigned it = atomicAdd(ticket, 1u);
         if (it >= total)
             break;
-        const unsigned item = it / v, j = it - item * v;
-        MaxOut mo{false, false, 0, 0, 0, 0};
+        const unsigned item = it / per, r = it - item * per;
+        const unsigned j = levels == 2 ? r / v : r, k = levels == 2 ? r - (r / v) * v : 0u;
+        const unsigned mask1 = levels == 2 ? (1u << k) : 0xFFFFu;
+        MaxOut mo{false, false, 0, 0, 0, 0, 0};
         uint8_t st = 0;
-        if (!load_rows(sm, rows + (size_t)item * v, v, b, flags & F_RAW)) {
+        if (levels == 2 && j == k) {
+            // no path starts with the same row twice
+        } else if (!load_rows(sm, rows + (size_t)item * v, v, b, flags & F_RAW)) {
             st = ST_BADINPUT;
         } else if (!((volatile unsigned *)stop)[item]) {
-            max_search(sm, v, b, max_nodes, mo, ID16, true, true, 1u << j, stop + item);
+            max_search(sm, v, b, max_nodes, mo, ID16, true, true, 1u << j, stop + item, mask1);
             if (mo.timeout)
                 st = ST_TIMEOUT;
             if (mo.improved)
@@ -329,22 +337,40 @@ __global__ void __launch_bounds__(TPB) bibd_split_kernel(uint32_t n_items, uint3
         SplitPart p;
         p.leaves = mo.leaves;
         p.orbit0 = (uint8_t)mo.orbit0;
+        p.orbit1 = (uint8_t)mo.orbit1;
         p.improved = mo.improved ? 1 : 0;
         p.status = st;
         parts[it] = p;
     }
 }
 
-__global__ void bibd_split_combine_kernel(uint32_t n_items, uint32_t v, const SplitPart *parts,
+__global__ void bibd_split_combine_kernel(uint32_t n_items, uint32_t v, uint32_t levels, const SplitPart *parts,
                                           const unsigned *stop, uint8_t *canonical, uint64_t *aut,
                                           uint8_t *status) {
+    const unsigned per = levels == 2 ? v * v : v;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += gridDim.x * blockDim.x) {
-        const SplitPart *p = parts + (size_t)i * v;
+        const SplitPart *p = parts + (size_t)i * per;
         uint8_t st = 0;
-        unsigned total0 = 0;
-        for (uint32_t j = 0; j < v; ++j) {
-            st |= p[j].status;
-            total0 += p[j].orbit0;
+        for (uint32_t q = 0; q < per; ++q)
+            st |= p[q].status;
+        uint64_t order = 0;
+        if (levels == 2) {
+            // rows 1.. that some thread (j, k) mapped row 0 to, rows 2.. mapped to row 1
+            uint64_t o0 = 1, o1 = 1;
+            for (uint32_t j = 1; j < v; ++j) {
+                bool any = false;
+                for (uint32_t k = 0; k < v; ++k)
+                    any = any || p[j * v + k].orbit0;
+                o0 += any;
+            }
+            for (uint32_t k = 2; k < v; ++k)
+                o1 += p[k].orbit1;
+            order = o0 * o1 * p[1].leaves;
+        } else {
+            unsigned total0 = 0;
+            for (uint32_t j = 0; j < v; ++j)
+                total0 += p[j].orbit0;
+            order = (uint64_t)total0 * (p[0].leaves / (p[0].orbit0 ? p[0].orbit0 : 1));
         }
         const bool improved = stop[i] != 0;
         if (improved)
@@ -352,7 +378,7 @@ __global__ void bibd_split_combine_kernel(uint32_t n_items, uint32_t v, const Sp
         const bool can = !st && !improved;
         canonical[i] = can ? 1 : 0;
         if (aut) {
-            aut[2 * (size_t)i] = can ? (uint64_t)total0 * (p[0].leaves / (p[0].orbit0 ? p[0].orbit0 : 1)) : 0;
+            aut[2 * (size_t)i] = can ? order : 0;
             aut[2 * (size_t)i + 1] = 0;
         }
         if (status)
@@ -486,16 +512,18 @@ cudaError_t launch_bibd_check_split(uint32_t n, uint32_t v, uint32_t b, uint32_t
                                     cudaStream_t s) {
     if (!n)
         return cudaSuccess;
+    // two levels while the threads stay few enough (the parts hold n * v * v)
+    const uint32_t levels = split_levels(n, v);
     cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
     cudaMemsetAsync(d_stop, 0, (size_t)n * sizeof(unsigned), s);
-    const uint64_t work = (uint64_t)n * v;
+    const uint64_t work = (uint64_t)n * (levels == 2 ? v * v : v);
     int grid = blocks_for((const void *)bibd_split_kernel, num_sms);
     const int need = (int)((work + TPB - 1) / TPB);
     if (grid > need)
         grid = need;
-    bibd_split_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_parts, d_stop, max_trials, tk);
+    bibd_split_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, levels, d_rows, d_parts, d_stop, max_trials, tk);
     const int g2 = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
-    bibd_split_combine_kernel<<<g2, 256, 0, s>>>(n, v, d_parts, d_stop, d_canonical, d_aut, d_status);
+    bibd_split_combine_kernel<<<g2, 256, 0, s>>>(n, v, levels, d_parts, d_stop, d_canonical, d_aut, d_status);
     return cudaGetLastError();
 }
 

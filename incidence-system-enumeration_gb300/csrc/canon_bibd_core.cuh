@@ -590,6 +590,7 @@ struct MaxOut {
     uint64_t nodes;
     unsigned first_rows;  // rows that start a labeling reaching the canonical form
     unsigned orbit0;      // pruned search of a canonical M: the first rows found in the orbit of row 0
+    unsigned orbit1;      // ... and the second rows (under row 0) found in the orbit of row 1
 };
 
 // The arranged column masks for level lv+1 after row `cand` was taken at level
@@ -630,13 +631,16 @@ __device__ __forceinline__ void refine_arranged(S sm, unsigned lv, unsigned cand
 // With pruning and M canonical, orbit0 counts the rows of root_mask found in the
 // orbit of row 0, and the thread whose root_mask holds row 0 alone has
 // leaves = the product of the orbit lengths below level 0; split searches then
-// combine as |Aut| = (sum of orbit0) x (that product).
+// combine as |Aut| = (sum of orbit0) x (that product).  root_mask1 restricts the
+// second rows the same way; orbit1 counts those found in the orbit of row 1
+// under the automorphisms that fix row 0.
 // stop: a flag that another thread of a split search raises once it has shown M
 // not to be canonical; it is read every 64 nodes and ends this share early.
 template <typename S>
 __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o,
                            uint64_t order0 = ID16, bool prune = true, bool stop_on_improve = false,
-                           unsigned root_mask = 0xFFFFu, const volatile unsigned *stop = nullptr) {
+                           unsigned root_mask = 0xFFFFu, const volatile unsigned *stop = nullptr,
+                           unsigned root_mask1 = 0xFFFFu) {
     const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     const uint64_t cols = (1ull << b) - 1ull;
     const uint64_t sentinel = 1ull << b;
@@ -647,6 +651,7 @@ __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, Max
     o.nodes = 0;
     o.first_rows = 0;
     o.orbit0 = 0;
+    o.orbit1 = 0;
     unsigned valid = n;        // rows 0..valid-1 of the bound (and levels 0..valid) are set
     unsigned used = 0;
     uint64_t perm = 0;
@@ -761,7 +766,8 @@ __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, Max
                 L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
                 valid = i + 1;
             }
-            VD_(i) = (i == 0) ? (tied & root_mask) : tied;     // children still to visit (16 bits)
+            // children still to visit (16 bits)
+            VD_(i) = (i == 0) ? (tied & root_mask) : (i == 1 ? (tied & root_mask1) : tied);
         }
         // next child of the node at level i
         unsigned rem = VD_(i);
@@ -779,6 +785,9 @@ __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, Max
                 if (i == 0)
                     for (unsigned q = 0; q < n; ++q)
                         o.orbit0 += ((root_mask >> q) & 1u) && pg(orb, q) == 0;
+                if (i == 1)
+                    for (unsigned q = 1; q < n; ++q)
+                        o.orbit1 += ((root_mask1 >> q) & 1u) && pg(orb, q) == 1;
             }
             if (i == 0)
                 break;

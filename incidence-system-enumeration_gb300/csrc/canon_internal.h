@@ -67,11 +67,15 @@ enum : int { VARIANT_SINGLE = 0, VARIANT_TWO_PASS = 1, VARIANT_SPLIT = 2 };
 // one share of a lex-max search split by first row (bibd_split_kernel)
 struct SplitPart {
     uint64_t leaves;
-    uint8_t orbit0, improved, status, pad[5];
+    uint8_t orbit0, improved, status, orbit1, pad[4];
 };
+// levels of the split search for n matrices of v rows: 2 (threads per matrix and
+// first two rows) while n * v * v <= 2^18 and v >= 3, else 1
+inline uint32_t split_levels(uint64_t n, uint32_t v) { return (v >= 3 && n * v * v <= (1ull << 18)) ? 2u : 1u; }
 // verdict (and |Aut| of the canonical) of n matrices with v rows, one thread per
-// (matrix, first row); d_parts: n*v parts, d_stop: n words of scratch.  Outputs
-// other than the flag, |Aut| and status are not produced.
+// (matrix, first row[, second row]); d_parts: n*v*v parts (n*v when one level),
+// d_stop: n words of scratch.  Outputs other than the flag, |Aut| and status are
+// not produced.
 cudaError_t launch_bibd_check_split(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
                                     uint8_t *d_canonical, uint64_t *d_aut, uint8_t *d_status, SplitPart *d_parts,
                                     unsigned *d_stop, uint64_t max_trials, unsigned *d_ticket, int num_sms,

@@ -468,7 +468,7 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
             // 3: the verdicts
             cudaEventRecord(e0, s);
             if (ns <= SPLIT_MAX) {
-                e = parts.ensure((size_t)(ns ? ns : 1) * m);
+                e = parts.ensure((size_t)(ns ? ns : 1) * m * (canon::split_levels(ns, m) == 2 ? m : 1));
                 if (e == cudaSuccess)
                     e = stop.ensure(ns ? ns : 1);
                 if (e == cudaSuccess)

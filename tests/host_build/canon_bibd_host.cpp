@@ -66,3 +66,20 @@ extern "C" int emu_maxsearch_root(const uint64_t *rows, unsigned n, unsigned b, 
     *leaves = mo.leaves; *orbit0 = mo.orbit0; *improved = mo.improved;
     return mo.timeout ? -2 : 0;
 }
+
+// a share of a search split by the first two rows
+extern "C" int emu_maxsearch_root2(const uint64_t *rows, unsigned n, unsigned b, unsigned root_mask,
+                                   unsigned root_mask1, uint64_t *leaves, unsigned *orbit0, unsigned *orbit1,
+                                   uint8_t *improved) {
+    static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
+    static uint32_t s_vd[VMAX * TPB];
+    static uint16_t s_cm[64 * TPB];
+    static uint8_t s_pc[64 * TPB];
+    Smem sm{s_rows, s_lvl, s_pc, s_cm, s_vd};
+    if (!load_rows(sm, rows, n, b, F_RAW))
+        return -1;
+    MaxOut mo;
+    max_search(sm, n, b, 1ull << 30, mo, ID16, true, true, root_mask, nullptr, root_mask1);
+    *leaves = mo.leaves; *orbit0 = mo.orbit0; *orbit1 = mo.orbit1; *improved = mo.improved;
+    return mo.timeout ? -2 : 0;
+}

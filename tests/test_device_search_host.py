@@ -188,6 +188,56 @@ def _split_result(L, rows, n, b):
     return improved, (0 if improved else total0 * deep)
 
 
+def _split2_result(L, rows, n, b):
+    """The search split into one thread per (first row, second row), combined as
+    the two-level split kernel does."""
+    u64 = ctypes.c_uint64
+    rows = np.ascontiguousarray(rows, np.uint64)
+    improved, in_orbit0, in_orbit1, deep = False, set(), 0, None
+    for j in range(n):
+        for k in range(n):
+            leaves, o0, o1, imp = u64(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint8()
+            assert L.emu_maxsearch_root2(rows.ctypes.data_as(ctypes.POINTER(u64)), n, b, 1 << j, 1 << k,
+                                         ctypes.byref(leaves), ctypes.byref(o0), ctypes.byref(o1),
+                                         ctypes.byref(imp)) == 0
+            improved |= bool(imp.value)
+            if j != 0 and o0.value:
+                in_orbit0.add(j)
+            if j == 0 and k >= 2:
+                in_orbit1 += o1.value
+            if (j, k) == (0, 1):
+                deep = leaves.value
+    return improved, (0 if improved else (1 + len(in_orbit0)) * (1 + in_orbit1) * deep)
+
+
+def test_search_split_by_first_two_rows_combines_to_the_whole(host):
+    """One thread per (first row, second row): |Aut| = |orbit of row 0| x |orbit of
+    row 1 under the stabilizer of row 0| x the identity thread's product below."""
+    import ise_gb300 as G
+    rng = np.random.default_rng(12)
+    todo = []
+    for M, _ in cases.load_sts15()[::7]:
+        todo.append((G.pack_rows(M), 35))
+        P = cases.permute_normalize(M, rng)
+        for k in (4, 8, 12):
+            todo.append((G.pack_rows(oracle.bibd_normalize(P[:k])), 35))
+    for params in [(8, 14, 7, 4, 3), (13, 26, 6, 3, 1), (9, 12, 4, 3, 1)]:
+        for M, _ in cases.bibd_designs(*params):
+            todo.append((G.pack_rows(M), params[1]))
+            P = cases.permute_normalize(M, rng)
+            for k in range(3, params[0] + 1, 3):
+                todo.append((G.pack_rows(oracle.bibd_normalize(P[:k])), params[1]))
+    for i in range(6):
+        todo.append((oracle.sts_random_rows(15, 78, i), 35))
+    for rows, b in todo:
+        n = len(rows)
+        full = maxsearch(host, rows, n, b, True)
+        imp, aut = _split2_result(host, rows, n, b)
+        assert imp == full["improved"]
+        if not imp:
+            assert aut == full["aut"], (n, aut, full["aut"])
+
+
 def test_search_split_by_first_row_combines_to_the_whole(host):
     """One thread per first row (the enumerator's small-batch check): the verdict is
     the OR of the threads', |Aut| = (rows found in the orbit of row 0) x (the
