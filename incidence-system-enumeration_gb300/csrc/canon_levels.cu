@@ -46,7 +46,7 @@ constexpr int GEN_TPB = 128;
 constexpr uint64_t DEVICE_GEN_MIN = 1ull << 17;
 // slices up to this size are checked with the search split by first row (one
 // thread per matrix and first row): small levels are latency bound
-constexpr uint64_t SPLIT_MAX = 1ull << 14;
+constexpr uint64_t SPLIT_MAX = 1ull << 16;
 
 template <typename T>
 struct DevBuf {
