@@ -9,6 +9,8 @@
 // canonical ones form level n+1.  Orderly generation makes the result independent of the
 // visiting order: every prefix of a canonical matrix is canonical, so the set of
 // canonical complete matrices is the same as the depth-first search finds.
+#include <sched.h>
+
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -72,15 +74,27 @@ struct KsysGen {
     }
 };
 
+// the host cores this process may run on (its CPU affinity), not every core of
+// the machine: a container or a job slot often holds fewer
+unsigned host_threads() {
+    cpu_set_t set;
+    CPU_ZERO(&set);
+    if (sched_getaffinity(0, sizeof(set), &set) == 0) {
+        const int c = CPU_COUNT(&set);
+        if (c > 0)
+            return (unsigned)c;
+    }
+    const unsigned n = std::thread::hardware_concurrency();
+    return n ? n : 1;
+}
+
 // children of every parent of a level, generated on all host cores; the
 // concatenation keeps the parents' order, so the result does not depend on the
 // number of threads
 template <typename Gen, typename T>
 void level_children(const Gen &proto, const std::vector<T> &level, size_t stride, int n, std::vector<T> &out) {
     const size_t parents = level.size() / stride;
-    unsigned nt = std::thread::hardware_concurrency();
-    if (nt < 1)
-        nt = 1;
+    unsigned nt = host_threads();
     if (nt > 32)
         nt = 32;
     if (parents < 64)

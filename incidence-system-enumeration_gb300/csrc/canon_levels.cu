@@ -23,6 +23,8 @@
 // generation makes the result independent of the visiting order: every prefix
 // of a canonical matrix is canonical, so the canonical complete matrices are
 // exactly those the depth-first search finds.
+#include <sched.h>
+
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -282,12 +284,24 @@ struct PinBuf {
     ~PinBuf() { cudaFreeHost(p); }
 };
 
+// the host cores this process may run on (its CPU affinity), not every core of
+// the machine: a container or a job slot often holds fewer
+unsigned host_threads() {
+    cpu_set_t set;
+    CPU_ZERO(&set);
+    if (sched_getaffinity(0, sizeof(set), &set) == 0) {
+        const int c = CPU_COUNT(&set);
+        if (c > 0)
+            return (unsigned)c;
+    }
+    const unsigned n = std::thread::hardware_concurrency();
+    return n ? n : 1;
+}
+
 // fn(lo, hi) over [0, n) on all host cores, in contiguous ranges
 template <typename F>
 void parallel_ranges(uint64_t n, F fn) {
-    unsigned nt = std::thread::hardware_concurrency();
-    if (nt < 1)
-        nt = 1;
+    unsigned nt = host_threads();
     if (nt > 64)
         nt = 64;
     if (n < 256)
