@@ -70,8 +70,8 @@ struct SplitPart {
     uint8_t orbit0, improved, status, orbit1, pad[4];
 };
 // levels of the split search for n matrices of v rows: 2 (threads per matrix and
-// first two rows) while n * v * v <= 2^18 and v >= 3, else 1
-inline uint32_t split_levels(uint64_t n, uint32_t v) { return (v >= 3 && n * v * v <= (1ull << 18)) ? 2u : 1u; }
+// first two rows) while n * v * v <= 2^20 and v >= 3, else 1
+inline uint32_t split_levels(uint64_t n, uint32_t v) { return (v >= 3 && n * v * v <= (1ull << 20)) ? 2u : 1u; }
 // verdict (and |Aut| of the canonical) of n matrices with v rows, one thread per
 // (matrix, first row[, second row]); d_parts: n*v*v parts (n*v when one level),
 // d_stop: n words of scratch.  Outputs other than the flag, |Aut| and status are
