@@ -60,8 +60,9 @@ struct DevBuf {
             return cudaSuccess;
         cudaFree(p);
         p = nullptr;
+        // at least double, so a growing enumeration reallocates (and synchronises) rarely
+        const size_t want = (n > 2 * cap ? n : 2 * cap) + 1024;
         cap = 0;
-        const size_t want = n + n / 4 + 1024;
         const cudaError_t e = cudaMalloc(&p, want * sizeof(T));
         if (e == cudaSuccess)
             cap = want;
@@ -271,8 +272,9 @@ struct PinBuf {
             return cudaSuccess;
         cudaFreeHost(p);
         p = nullptr;
+        // at least double: pinning memory is slow
+        const size_t want = (n > 2 * cap ? n : 2 * cap) + 1024;
         cap = 0;
-        const size_t want = n + n / 4 + 1024;
         const cudaError_t e = cudaHostAlloc((void **)&p, want * sizeof(uint64_t), cudaHostAllocDefault);
         if (e == cudaSuccess)
             cap = want;
