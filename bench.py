@@ -25,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -41,11 +42,18 @@ WORKLOAD = ("1,048,576 STS(15) 15x35 bit-packed matrices, seed %d, odd items can
             "outputs canonical flag + first rejecting permutation + |Aut|" % SEED)
 IN_BYTES = V * 8          # packed rows read per check
 OUT_BYTES = 1 + 16 + 16   # flag + witness + |Aut| written per check
-# DRAM bytes per check of the check kernel: dram__bytes_read.sum + dram__bytes_write.sum of one ncu
-# capture of 131,072 checks (15,918,592 B + 0 B; profiles/bibd_uniform_kernel_sts15_131k.md),
-# scaled by the checks of a launch (traffic grows with the number of matrices read).
+# DRAM bytes per check of the lex-max pass: dram__bytes_read.sum + dram__bytes_write.sum of one ncu
+# capture of 131,072 checks (15,918,592 B + 0 B; profiles/bibd_max_kernel_sts15_131k.md), scaled by
+# the checks of a launch (traffic grows with the number of matrices read).
 TRAFFIC_PER_CHECK = 15918592.0 / 131072
+# Integer work of the lex-max search (the check's roofline): a node compares the best
+# arrangement of every candidate row with the bound, one bit-sliced step per column of
+# the matrix: the column's row mask ANDed with the tied rows, a 6-plane carry chain
+# (AND + XOR per plane) and the final XOR -- 12 lane operations per column and node.
+INT_OPS_PER_NODE_COLUMN = 12
 MEASURED_PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
+CPU_NOTE = ("the oracle: a C restatement of the reference's checker (TestCanonicity + CanonizeMatrix), "
+            "not the reference binary, which does not build on this platform")
 
 
 def peaks():
@@ -63,10 +71,9 @@ class ClockSampler:
     def __init__(self, gpu):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "ise_gb300_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
-        os.makedirs(os.path.dirname(self.path), exist_ok=True)
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -88,6 +95,12 @@ class ClockSampler:
                 self.proc.kill()
             self.f.close()
 
+    def remove(self):
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+
     def summary(self):
         out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         try:
@@ -108,6 +121,7 @@ class ClockSampler:
         if sm:
             out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                    "samples": len(sm)}
+        self.remove()
         return out
 
 
@@ -207,7 +221,7 @@ def run_reference(args, rank, world, dist):
         "config": {"workload": WORKLOAD, "ordering": "plain", "l2": "n/a (host CPU)"},
         "cpu_baseline": {"value": value, "unit": "checks/s", "cores": threads, "kind": "port",
                          "sample": "first %d items of the workload per step (%d checks/step)"
-                                   % (len(rows), len(rows))},
+                                   % (len(rows), len(rows)), "note": CPU_NOTE},
         "e2e": {"value": value, "unit": "checks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -256,7 +270,8 @@ def run_gpu(args, rank, world, local, dist):
     value = world * n * args.steps / t_total
     ms_step = 1e3 * t_total / args.steps
     hbm, src = peaks()
-    achieved = (IN_BYTES + OUT_BYTES) * n / (sum(times) / len(times) / 1e3) / 1e9
+    roofline, roofline_hbm = integer_roofline(ctx, args, n, flags, variant, d_rows, d_can, d_aut, d_st, flush_l2,
+                                              hbm, src, times)
 
     # end to end through the batch API with host buffers
     host_rows = ctx.d2h(np.zeros(n * V, np.uint64), d_rows)
@@ -279,7 +294,8 @@ def run_gpu(args, rank, world, local, dist):
         rows_s = host_rows.reshape(n, V)[:sample]
         rate, done, dt = cpu_check_rate(rows_s, threads, 20)
         cpu = {"value": rate, "unit": "checks/s", "cores": threads, "kind": "port",
-               "sample": "first %d items of the same batch (%d checked in %.1f s)" % (sample, done, dt)}
+               "sample": "first %d items of the same batch (%d checked in %.1f s)" % (sample, done, dt),
+               "note": CPU_NOTE}
 
     if rank == 0:
         line = {
@@ -296,10 +312,8 @@ def run_gpu(args, rank, world, local, dist):
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "e2e": None if e2e_dt is None else {"value": world * n / e2e_dt, "unit": "checks/s",
                                                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": TRAFFIC_PER_CHECK * n,
-                         "note": "peak %s; the check is an integer search (ALU/issue bound), HBM "
-                                 "traffic is %d B per check" % (src, IN_BYTES + OUT_BYTES)},
+            "roofline": roofline,
+            "roofline_hbm": roofline_hbm,
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "clocks": clk.summary(),
@@ -308,6 +322,47 @@ def run_gpu(args, rank, world, local, dist):
     for p in (d_rows, d_can, d_wit, d_aut, d_st, l2_flush):
         ctx.free(p)
     ctx.close()
+
+
+def integer_roofline(ctx, args, n, flags, variant, d_rows, d_can, d_aut, d_st, flush_l2, hbm, src, times):
+    """The integer roofline of the dominant kernel (the lex-max pass of the two-pass
+    check, or the one-pass kernel): algorithmic integer operations per launch --
+    lex-max nodes (counted exactly on the device for this batch) x columns x 12 --
+    over that kernel's own CUDA-event time, against the integer lane-operation rate
+    this GPU sustains (canon_measure_int_peak).  HBM is reported beside it."""
+    import ise_gb300 as G
+    d_nodes = ctx.alloc(8 * n)
+    ctx.lexmax_nodes_bibd(n, V, B, flags, d_rows, d_nodes)
+    nodes = ctx.d2h(np.zeros(n, np.uint64), d_nodes)
+    ctx.free(d_nodes)
+    ops = float(nodes.sum()) * B * INT_OPS_PER_NODE_COLUMN
+    if variant == G.VARIANT_TWO_PASS:
+        # the first pass alone: without witness and trials outputs only it is launched
+        ms = []
+        for _ in range(2):
+            flush_l2()
+            ctx.check_bibd_device(n, V, B, flags, d_rows, d_can, None, d_aut, d_st)
+            ctx.stream_sync()
+            ms.append(ctx.last_kernel_ms())
+        kname = "bibd_max_kernel<35, 15> (lex-max pass)"
+    else:
+        ms = list(times)
+        kname = "the one-pass check kernel"
+    k_s = sum(ms) / len(ms) / 1e3
+    peak = ctx.measure_int_peak()
+    roof = {"bound": "int", "achieved": ops / k_s / 1e12, "peak": peak / 1e12, "unit": "Tops/s",
+            "frac": ops / k_s / peak, "traffic": TRAFFIC_PER_CHECK * n,
+            "kernel": kname, "kernel_ms": 1e3 * k_s,
+            "ops_per_launch": ops, "nodes_per_check_mean": float(nodes.mean()),
+            "ops_model": "lex-max nodes x %d columns x %d lane ops (bit-sliced count per column and node)"
+                         % (B, INT_OPS_PER_NODE_COLUMN),
+            "peak_source": "measured on this GPU: independent 32-bit XOR/ADD/shift chains (canon_measure_int_peak)"}
+    achieved_hbm = (IN_BYTES + OUT_BYTES) * n / k_s / 1e9
+    roof_hbm = {"bound": "hbm", "achieved": achieved_hbm, "peak": hbm, "unit": "GB/s",
+                "frac": achieved_hbm / hbm, "peak_source": src,
+                "note": "secondary: %d algorithmic bytes per check (rows in, flag + witness + |Aut| out)"
+                        % (IN_BYTES + OUT_BYTES)}
+    return roof, roof_hbm
 
 
 ENUM_WORKLOADS = {
@@ -368,116 +423,56 @@ def run_enum(args):
     ctx.close()
 
 
-MIX_SHAPES = [  # (share, kind, (v, b, r, k, lambda) or np, min filled rows, max filled rows)
-    (0.40, "bibd", (15, 35, 7, 3, 1), 5, 15),
-    (0.30, "bibd", (8, 14, 7, 4, 3), 4, 8),
-    (0.20, "bibd", (11, 11, 5, 5, 2), 4, 11),
-    (0.10, "ksys", 10, 3, 9),
-]
-
-
-def _permute_bits(words, perm):
-    """Column permutation of packed rows: new column c = old column perm[c]."""
-    bits = (words[..., None] >> perm.astype(np.uint64)) & np.uint64(1)
-    return (bits << np.arange(perm.shape[-1], dtype=np.uint64)).sum(axis=-1, dtype=np.uint64)
-
-
-def build_mix(ctx, n_total, seed):
-    """Seeded stand-in for the uneven batch of config 3: partial matrices that are
-    prefixes of randomly relabelled designs (so every one is a valid partial design)."""
-    import ise_gb300 as G
-    rng = np.random.default_rng(seed)
-    batches = []
-    for share, kind, params, lo, hi in MIX_SHAPES:
-        cnt = int(round(share * n_total))
-        nr = rng.integers(lo, hi + 1, size=cnt).astype(np.uint8)
-        if kind == "bibd" and params[0] == 15:
-            d = ctx.alloc(cnt * 15 * 8)
-            ctx.generate_sts_device(cnt, 15, seed + 1, False, d)
-            rows = ctx.d2h(np.zeros(cnt * 15, np.uint64), d).reshape(cnt, 15)
-            ctx.free(d)
-            batches.append(("bibd", 15, 35, rows, nr))
-        elif kind == "bibd":
-            v, b = params[0], params[1]
-            designs, _ = ctx.enumerate_bibd(*params)
-            base = np.stack([G.pack_rows(M) for M, _ in designs])
-            pick = rng.integers(len(base), size=cnt)
-            rp = np.argsort(rng.random((cnt, v)), axis=1)
-            rows = np.take_along_axis(base[pick], rp, axis=1)
-            cp = np.argsort(rng.random((cnt, b)), axis=1)
-            rows = _permute_bits(rows, cp[:, None, :].repeat(v, axis=1))
-            batches.append(("bibd", v, b, rows, nr))
-        else:
-            found, _ = ctx.enumerate_ksys(params)
-            base = np.stack([R for R, _ in found])                       # 396 x 9 x 10
-            pick = rng.integers(len(base), size=cnt)
-            R = base[pick].astype(np.int64)
-            # relabel so that a random round becomes round 0 = (0 1)(2 3)...
-            d = rng.integers(9, size=cnt)
-            src = R[np.arange(cnt), d]                                   # cnt x 10 players in pair order
-            gperm = np.argsort(rng.random((cnt, 5)), axis=1)
-            flip = rng.integers(2, size=(cnt, 5))
-            lab = np.zeros((cnt, 10), np.int64)
-            for g in range(5):
-                a_ = src[np.arange(cnt), 2 * gperm[:, g]]
-                b_ = src[np.arange(cnt), 2 * gperm[:, g] + 1]
-                x_ = np.where(flip[:, g] == 1, b_, a_)
-                y_ = np.where(flip[:, g] == 1, a_, b_)
-                lab[np.arange(cnt), x_] = 2 * g
-                lab[np.arange(cnt), y_] = 2 * g + 1
-            X = np.take_along_axis(lab[:, None, :].repeat(9, axis=1), R, axis=2)   # relabelled rounds
-            pa, pb = X[..., 0::2], X[..., 1::2]
-            lo_, hi_ = np.minimum(pa, pb), np.maximum(pa, pb)
-            order = np.argsort(lo_, axis=2)
-            lo_ = np.take_along_axis(lo_, order, axis=2)
-            hi_ = np.take_along_axis(hi_, order, axis=2)
-            rounds = np.stack([lo_, hi_], axis=3).reshape(cnt, 9, 10)
-            rorder = np.argsort(rounds[:, :, 1], axis=1)
-            rounds = np.take_along_axis(rounds, rorder[:, :, None], axis=1).astype(np.uint8)
-            batches.append(("ksys", 10, 9, rounds, nr))
-    return batches
-
-
 def run_mix(args):
-    """Config 3: one persistent launch over the uneven 2M mix."""
+    """Config 3: one persistent launch over the uneven 2M mix of partial matrices, each
+    made by seeded random backtracking of its filled rows (ise_gb300.workloads)."""
     import ise_gb300 as G
-    n_total = args.items if args.items != N_ITEMS else 2_097_152
-    ctx = G.Context(max_items=n_total + 16, max_words=16 * n_total, aut_cap=1)
-    batches = build_mix(ctx, n_total, SEED + 3)
-    n = sum(len(b[4]) for b in batches)
-
-    def submit():
-        for kind, v, b, rows, nr in batches:
-            if kind == "bibd":
-                ctx.submit_bibd(rows, v, b, G.RAW, nr)
-            else:
-                ctx.submit_ksys(rows, v, b, 0, nr)
-
+    from ise_gb300 import workloads
+    n_total = args.items if args.items != N_ITEMS else workloads.MIX_ITEMS
+    t0 = time.perf_counter()
+    batches = workloads.config3_mix(n_total, SEED + 3)
+    gen_s = time.perf_counter() - t0
+    n = sum(len(bt["nrows"]) for bt in batches)
+    ctx = G.Context(max_items=n + 16, max_words=16 * n, aut_cap=1)
     for _ in range(args.warmup):
-        submit()
-        ctx.sync()
+        workloads.submit_mix(ctx, batches)
+        ctx.sync(raw=True)
     l0 = ctx.kernel_launches()
     kms, walls = [], []
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            submit()
+            workloads.submit_mix(ctx, batches)
             r = ctx.sync(raw=True)
             walls.append(time.perf_counter() - t0)
             kms.append(r["kernel_ms"])
-    assert r["n"] == n and not r["status"].any()
+    launches = ctx.kernel_launches() - l0
+    if r["n"] != n or r["status"].any():
+        raise SystemExit("bench: mix reported %d bad status items" % int((r["status"] != 0).sum()))
+    kinds, off = [], 0
+    for bt in batches:
+        cnt = len(bt["nrows"])
+        can = r["canonical"][off:off + cnt].astype(np.float64)
+        kinds.append({"shape": bt["name"], "items": cnt, "rows_filled": [int(bt["nrows"].min()),
+                                                                          int(bt["nrows"].max())],
+                      "canonical_fraction": float(can.mean()),
+                      "from_complete_design": int(bt["from_complete"])})
+        off += cnt
+    h2d = workloads.mix_input_bytes(batches) + 16 * n
+    d2h = 51 * n
     line = {"metric": "exact canonicity checks/sec (config 3 uneven mix, one persistent launch)",
             "value": n * args.steps / (sum(kms) / 1e3), "unit": "checks/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sum(kms) / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u64 bit rows / u8", "data": "synthetic",
-            "config": {"workload": "%d partial matrices: 40%% STS(15) 5-15 rows, 30%% BIBD(8,14,7,4,3) 4-8, "
-                                   "20%% BIBD(11,11,5,5,2) 4-11, 10%% K10 3-9 rounds; prefixes of randomly "
-                                   "relabelled designs, seed %d" % (n, SEED + 3),
-                       "canonical_fraction": float(r["canonical"].astype(np.float64).mean())},
+            "config": {"workload": "%d partial matrices by seeded random backtracking of their filled rows "
+                                   "(seed %d): 40%% STS(15) 5-15 rows, 30%% BIBD(8,14,7,4,3) 4-8, "
+                                   "20%% BIBD(11,11,5,5,2) 4-11, 10%% K10 3-9 rounds" % (n, SEED + 3),
+                       "kinds": kinds,
+                       "canonical_fraction": float(r["canonical"].astype(np.float64).mean()),
+                       "generation_s": gen_s},
             "e2e": {"value": n * args.steps / sum(walls), "unit": "checks/s",
-                    "h2d_bytes_per_step": int(sum(b[3].nbytes for b in batches) + 16 * n),
-                    "d2h_bytes_per_step": 51 * n},
-            "gpu_launches": ctx.kernel_launches() - l0, "clocks": clk.summary()}
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -527,12 +522,20 @@ def run_learned(args):
         for b in bufs:
             ctx.free(b)
     identical = all(np.array_equal(a, b) for a, b in zip(res["plain"][1], res["learned"][1]))
-    # lex-max nodes in both orders and the top-1 hit rate of the network
-    d_lab = ctx.alloc(2 * n_eval)
+    canon_mask = res["plain"][1][0].astype(bool)
+    # lex-max nodes of the check's search (the first pass) in both orders, split by verdict
     d_nodes = ctx.alloc(8 * n_eval)
+    node_stats = {}
+    for name, prm in (("plain", None), ("learned", params)):
+        ctx.set_ordering(prm)
+        ctx.lexmax_nodes_bibd(n_eval, V, B, flags, d_rows, d_nodes)
+        nd = ctx.d2h(np.zeros(n_eval, np.uint64), d_nodes).astype(np.float64)
+        node_stats[name] = {"mean": float(nd.mean()), "canonical_mean": float(nd[canon_mask].mean()),
+                            "noncanonical_mean": float(nd[~canon_mask].mean())}
     ctx.set_ordering(None)
-    ctx.label_first_rows(n_eval, V, B, G.RAW, d_rows, d_lab, d_nodes)
-    nodes_plain = ctx.d2h(np.zeros(n_eval, np.uint64), d_nodes).astype(np.float64)
+    # the first rows that reach the canonical form, and the top-1 hit rate of the network
+    d_lab = ctx.alloc(2 * n_eval)
+    ctx.label_first_rows(n_eval, V, B, G.RAW, d_rows, d_lab)
     lab = ctx.d2h(np.zeros(n_eval, np.uint16), d_lab)
     d_feat = ctx.alloc(65536 * V * 64 * 2)
     d_log = ctx.alloc(65536 * V * 4)
@@ -552,7 +555,8 @@ def run_learned(args):
             "plain_checks_per_s": res["plain"][0], "learned_over_plain": res["learned"][0] / res["plain"][0],
             "outputs_identical": identical, "train_loss_per_epoch": [float(x) for x in losses],
             "train_seconds": train_s, "top1_hit_rate": top1,
-            "lexmax_nodes_plain_mean": float(nodes_plain.mean())}
+            "lexmax_nodes": node_stats,
+            "lexmax_nodes_learned_over_plain": node_stats["learned"]["mean"] / node_stats["plain"]["mean"]}
     print(json.dumps(line), flush=True)
     ctx.close()
 

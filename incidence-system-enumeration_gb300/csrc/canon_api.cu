@@ -727,6 +727,69 @@ int canon_tune_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t f
     return CANON_OK;
 }
 
+int canon_lexmax_nodes_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
+                            const uint64_t *d_rows, uint64_t *d_nodes) {
+    if (!c || !d_rows || !d_nodes)
+        return fail(c, CANON_EINVAL, "null argument");
+    if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX)
+        return fail(c, CANON_EINVAL, "nodes: need 1 <= v <= 16, 1 <= b <= 63");
+    cudaSetDevice(c->device);
+    const uint64_t *orders = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (c->order_on) {
+        // the learned first-row order, as canon_check_bibd_device applies it
+        const size_t need = (size_t)n * 8 + 256;
+        if (!c->d_orders_bytes || c->d_orders_bytes < need) {
+            if (c->d_orders)
+                cudaFree(c->d_orders);
+            c->d_orders = nullptr;
+            c->d_orders_bytes = 0;
+            e = cudaMalloc((void **)&c->d_orders, need);
+            if (e == cudaSuccess)
+                c->d_orders_bytes = need;
+        }
+        if (e == cudaSuccess)
+            e = compute_orders(c, n, v, b, d_rows, c->d_orders, c->stream);
+        orders = c->d_orders;
+    }
+    if (e == cudaSuccess)
+        e = canon::launch_bibd_lexmax_nodes(n, v, b, flags, d_rows, d_nodes, c->cfg.max_trials, c->d_ticket,
+                                            c->num_sms, c->stream, orders);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(c->stream);
+    ++c->launches;
+    return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "nodes");
+}
+
+int canon_measure_int_peak(canon_ctx *c, double *lane_ops_per_s) {
+    if (!c || !lane_ops_per_s)
+        return fail(c, CANON_EINVAL, "null argument");
+    cudaSetDevice(c->device);
+    uint32_t *sink = nullptr;
+    cudaError_t e = cudaMalloc((void **)&sink, 16);
+    uint64_t ops = 0;
+    float best = 0.f;
+    // one untimed launch, then the fastest of five
+    for (int rep = 0; rep < 6 && e == cudaSuccess; ++rep) {
+        cudaEventRecord(c->ev0, c->stream);
+        e = canon::launch_int_peak(1u << 16, c->num_sms, sink, c->stream, &ops);
+        cudaEventRecord(c->ev1, c->stream);
+        if (e == cudaSuccess)
+            e = cudaEventSynchronize(c->ev1);
+        float ms = 0.f;
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        if (e == cudaSuccess && rep > 0 && ms > 0.f && (best == 0.f || ms < best))
+            best = ms;
+        ++c->launches;
+    }
+    cudaFree(sink);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "int peak");
+    *lane_ops_per_s = best > 0.f ? (double)ops / (best * 1e-3) : 0.0;
+    return CANON_OK;
+}
+
 int canon_generate_sts_device(canon_ctx *c, uint32_t n, uint32_t v, uint64_t seed, int canon_odd, uint64_t *d_rows,
                               void *stream) {
     if (!c || !d_rows)
@@ -907,9 +970,11 @@ static cudaError_t mlp_grad_pass(canon_ctx *c, long n, const void *d_x, const fl
     float *dh2 = reinterpret_cast<float *>(base + (size_t)n * 8 + act * 4);
     float *dh1 = dh2 + act;
     cudaStream_t s = c->stream;
-    cudaMemsetAsync(c->d_grad, 0, canon::mlp::N_PARAMS * 4, s);
-    cudaMemsetAsync(c->d_loss, 0, 4, s);
-    e = mlp_forward_installed(c, n, d_x, logit, h1, h2, s);
+    e = cudaMemsetAsync(c->d_grad, 0, canon::mlp::N_PARAMS * 4, s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(c->d_loss, 0, 4, s);
+    if (e == cudaSuccess)
+        e = mlp_forward_installed(c, n, d_x, logit, h1, h2, s);
     if (e == cudaSuccess)
         e = canon::mlp::backward(n, logit, d_labels, h1, h2, c->d_w3, c->d_w2t, dy, dh2, dh1, c->d_loss, c->num_sms, s);
     if (e == cudaSuccess)
@@ -946,8 +1011,11 @@ int canon_mlp_train(canon_ctx *c, uint64_t n, const void *d_x, const float *d_la
     cudaError_t e = upload_params(c, params);
     if (e != cudaSuccess)
         return cuda_fail(c, e, "train upload");
-    cudaMemsetAsync(c->d_adam_m, 0, canon::mlp::N_PARAMS * 4, c->stream);
-    cudaMemsetAsync(c->d_adam_v, 0, canon::mlp::N_PARAMS * 4, c->stream);
+    e = cudaMemsetAsync(c->d_adam_m, 0, canon::mlp::N_PARAMS * 4, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(c->d_adam_v, 0, canon::mlp::N_PARAMS * 4, c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "train reset");
     int step = 0;
     for (uint32_t ep = 0; ep < epochs; ++ep) {
         double lsum = 0.0;

@@ -14,6 +14,7 @@
 // takes the next one.
 #include <mutex>
 
+#include "../../include/canon_gb300.h"
 #include "canon_bibd_core.cuh"
 
 namespace canon {
@@ -86,7 +87,8 @@ template <int BCAP, int VCAP>
 __global__ void __launch_bounds__(TPB) bibd_max_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
                                                        const uint64_t *__restrict__ rows, uint8_t *canonical,
                                                        uint64_t *aut, uint8_t *status, uint64_t max_nodes,
-                                                       unsigned *ticket, const uint64_t *__restrict__ orders) {
+                                                       unsigned *ticket, const uint64_t *__restrict__ orders,
+                                                       uint64_t *nodes_out) {
     __shared__ uint64_t s_rows[VCAP * TPB];
     __shared__ uint64_t s_lvl[(VCAP + 1) * TPB];
     __shared__ uint16_t s_vd[VCAP * TPB];
@@ -107,7 +109,8 @@ __global__ void __launch_bounds__(TPB) bibd_max_kernel(uint32_t n_items, uint32_
                 st = ST_TIMEOUT;
         }
         const bool can = !st && !mo.improved;
-        canonical[it] = can ? 1 : 0;
+        if (canonical)
+            canonical[it] = can ? 1 : 0;
         if (status)
             status[it] = st;
         if (aut) {
@@ -115,7 +118,34 @@ __global__ void __launch_bounds__(TPB) bibd_max_kernel(uint32_t n_items, uint32_
             aut[2 * (size_t)it] = has ? mo.leaves : 0;
             aut[2 * (size_t)it + 1] = 0;
         }
+        if (nodes_out)
+            nodes_out[it] = mo.nodes;
     }
+}
+
+// Throughput of the integer pipes on this GPU: every thread runs eight independent
+// chains of 32-bit XOR / ADD / shift-add steps (LOP3 and IADD3 class operations)
+// for `iters` rounds; a round is 24 operations per thread.  The result is stored
+// only when it matches a value the caller never passes, so the work is not removed.
+__global__ void __launch_bounds__(256) int_peak_kernel(uint32_t iters, uint32_t seed, uint32_t never,
+                                                       uint32_t *sink) {
+    uint32_t a0 = seed ^ threadIdx.x, a1 = a0 * 3u, a2 = a0 * 5u, a3 = a0 * 7u;
+    uint32_t a4 = a0 * 11u, a5 = a0 * 13u, a6 = a0 * 17u, a7 = a0 * 19u;
+    const uint32_t k = seed | 1u;
+#pragma unroll 4
+    for (uint32_t i = 0; i < iters; ++i) {
+        a0 = ((a0 ^ k) + a1) ^ (a0 >> 1);
+        a1 = ((a1 ^ k) + a2) ^ (a1 >> 1);
+        a2 = ((a2 ^ k) + a3) ^ (a2 >> 1);
+        a3 = ((a3 ^ k) + a4) ^ (a3 >> 1);
+        a4 = ((a4 ^ k) + a5) ^ (a4 >> 1);
+        a5 = ((a5 ^ k) + a6) ^ (a5 >> 1);
+        a6 = ((a6 ^ k) + a7) ^ (a6 >> 1);
+        a7 = ((a7 ^ k) + a0) ^ (a7 >> 1);
+    }
+    const uint32_t r = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
+    if (r == never)
+        sink[0] = r;
 }
 
 // Pass 2: the first rejecting permutation (reference order) of the matrices that
@@ -386,13 +416,26 @@ __global__ void bibd_split_combine_kernel(uint32_t n_items, uint32_t v, uint32_t
     }
 }
 
-int blocks_for(const void *kernel, int num_sms) {
+// Persistent grid: resident blocks per SM x SMs, at most `need` blocks.  A failed
+// occupancy query is returned instead of launching a guessed size.
+cudaError_t grid_for(const void *kernel, int num_sms, int need, int *grid) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TPB, 0);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TPB, 0);
+    if (e != cudaSuccess)
+        return e;
     if (per_sm < 1)
         per_sm = 1;
-    return per_sm * (num_sms > 0 ? num_sms : 1);
+    const int g = per_sm * (num_sms > 0 ? num_sms : 1);
+    *grid = g < need ? g : need;
+    return cudaSuccess;
 }
+
+#define CANON_TRY(x)                          \
+    do {                                      \
+        const cudaError_t e_ = (x);           \
+        if (e_ != cudaSuccess)                \
+            return e_;                        \
+    } while (0)
 
 }  // namespace
 
@@ -400,11 +443,10 @@ cudaError_t launch_bibd_check(const Item *d_items, uint32_t n_items, const uint6
                               uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
     if (!n_items)
         return cudaSuccess;
-    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
-    int grid = blocks_for((const void *)bibd_items_kernel, num_sms);
+    CANON_TRY(cudaMemsetAsync(tk, 0, sizeof(unsigned), s));
     const int need = (int)((n_items + TPB - 1) / TPB);
-    if (grid > need)
-        grid = need;
+    int grid = 0;
+    CANON_TRY(grid_for((const void *)bibd_items_kernel, num_sms, need, &grid));
     bibd_items_kernel<<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
     return cudaGetLastError();
 }
@@ -414,15 +456,14 @@ cudaError_t launch_bibd_check_two_pass(const Item *d_items, uint32_t n_items, co
                                        uint32_t max_b, uint32_t max_v) {
     if (!n_items)
         return cudaSuccess;
-    cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
+    CANON_TRY(cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s));
     const int need = (int)((n_items + TPB - 1) / TPB);
     const int shape = (max_v <= 15 && max_b <= 35) ? 0 : (max_b <= 40 ? 1 : 2);
     const void *kfn = shape == 0 ? (const void *)bibd_items_max_kernel<35, 15>
                       : shape == 1 ? (const void *)bibd_items_max_kernel<40, 16>
                                    : (const void *)bibd_items_max_kernel<64, 16>;
-    int grid = blocks_for(kfn, num_sms);
-    if (grid > need)
-        grid = need;
+    int grid = 0;
+    CANON_TRY(grid_for(kfn, num_sms, need, &grid));
     if (shape == 0)
         bibd_items_max_kernel<35, 15><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
     else if (shape == 1)
@@ -432,9 +473,8 @@ cudaError_t launch_bibd_check_two_pass(const Item *d_items, uint32_t n_items, co
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    int g2 = blocks_for((const void *)bibd_items_witness_kernel, num_sms);
-    if (g2 > need)
-        g2 = need;
+    int g2 = 0;
+    CANON_TRY(grid_for((const void *)bibd_items_witness_kernel, num_sms, need, &g2));
     bibd_items_witness_kernel<<<g2, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk + 1);
     return cudaGetLastError();
 }
@@ -454,41 +494,69 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
         // the reference-order witness for the rejected ones.  (Without it the
         // single pass below rejects most non-canonical matrices in a few trials
         // of the reference order and runs the lex-max search only for the rest.)
-        cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
+        CANON_TRY(cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s));
         // the smallest instance that holds the shape
         const void *kfn = (v <= 15 && b <= 35) ? (const void *)bibd_max_kernel<35, 15>
                           : (b <= 40)          ? (const void *)bibd_max_kernel<40, 16>
                                                : (const void *)bibd_max_kernel<64, 16>;
-        int grid = blocks_for(kfn, num_sms);
-        if (grid > need)
-            grid = need;
+        int grid = 0;
+        CANON_TRY(grid_for(kfn, num_sms, need, &grid));
         if (v <= 15 && b <= 35)
             bibd_max_kernel<35, 15><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
-                                                         max_trials, tk, d_orders);
+                                                         max_trials, tk, d_orders, nullptr);
         else if (b <= 40)
             bibd_max_kernel<40, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
-                                                         max_trials, tk, d_orders);
+                                                         max_trials, tk, d_orders, nullptr);
         else
             bibd_max_kernel<64, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
-                                                         max_trials, tk, d_orders);
+                                                         max_trials, tk, d_orders, nullptr);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;
         if (d_witness16 || d_trials) {
-            int g2 = blocks_for((const void *)bibd_witness_kernel, num_sms);
-            if (g2 > need)
-                g2 = need;
+            int g2 = 0;
+            CANON_TRY(grid_for((const void *)bibd_witness_kernel, num_sms, need, &g2));
             bibd_witness_kernel<<<g2, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_witness16, d_status,
                                                    d_trials, max_trials, tk + 1);
         }
         return cudaGetLastError();
     }
-    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
-    int grid = blocks_for((const void *)bibd_uniform_kernel, num_sms);
-    if (grid > need)
-        grid = need;
+    CANON_TRY(cudaMemsetAsync(tk, 0, sizeof(unsigned), s));
+    int grid = 0;
+    CANON_TRY(grid_for((const void *)bibd_uniform_kernel, num_sms, need, &grid));
     bibd_uniform_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut, d_status,
                                              d_trials, max_trials, tk, d_orders);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bibd_lexmax_nodes(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                                     uint64_t *d_nodes, uint64_t max_nodes, unsigned *tk, int num_sms,
+                                     cudaStream_t s, const uint64_t *d_orders) {
+    if (!n)
+        return cudaSuccess;
+    CANON_TRY(cudaMemsetAsync(tk, 0, sizeof(unsigned), s));
+    const int need = (int)((n + TPB - 1) / TPB);
+    int grid = 0;
+    if (v <= 15 && b <= 35) {
+        CANON_TRY(grid_for((const void *)bibd_max_kernel<35, 15>, num_sms, need, &grid));
+        bibd_max_kernel<35, 15><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, nullptr, nullptr, nullptr, max_nodes,
+                                                     tk, d_orders, d_nodes);
+    } else if (b <= 40) {
+        CANON_TRY(grid_for((const void *)bibd_max_kernel<40, 16>, num_sms, need, &grid));
+        bibd_max_kernel<40, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, nullptr, nullptr, nullptr, max_nodes,
+                                                     tk, d_orders, d_nodes);
+    } else {
+        CANON_TRY(grid_for((const void *)bibd_max_kernel<64, 16>, num_sms, need, &grid));
+        bibd_max_kernel<64, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, nullptr, nullptr, nullptr, max_nodes,
+                                                     tk, d_orders, d_nodes);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_int_peak(uint32_t iters, int num_sms, uint32_t *d_sink, cudaStream_t s, uint64_t *ops) {
+    const int grid = 8 * (num_sms > 0 ? num_sms : 1);
+    int_peak_kernel<<<grid, 256, 0, s>>>(iters, 0x9E3779B9u, 0xFFFFFFFFu, d_sink);
+    *ops = (uint64_t)grid * 256u * iters * 32u;
     return cudaGetLastError();
 }
 
@@ -497,11 +565,10 @@ cudaError_t launch_bibd_labels(uint32_t n, uint32_t v, uint32_t b, uint32_t flag
                                uint64_t max_nodes, unsigned *tk, int num_sms, cudaStream_t s) {
     if (!n)
         return cudaSuccess;
-    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
-    int grid = blocks_for((const void *)bibd_label_kernel, num_sms);
+    CANON_TRY(cudaMemsetAsync(tk, 0, sizeof(unsigned), s));
     const int need = (int)((n + TPB - 1) / TPB);
-    if (grid > need)
-        grid = need;
+    int grid = 0;
+    CANON_TRY(grid_for((const void *)bibd_label_kernel, num_sms, need, &grid));
     bibd_label_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_first_rows, d_nodes, d_orders, max_nodes, tk);
     return cudaGetLastError();
 }
@@ -514,14 +581,14 @@ cudaError_t launch_bibd_check_split(uint32_t n, uint32_t v, uint32_t b, uint32_t
         return cudaSuccess;
     // two levels while the threads stay few enough (the parts hold n * v * v)
     const uint32_t levels = split_levels(n, v);
-    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
-    cudaMemsetAsync(d_stop, 0, (size_t)n * sizeof(unsigned), s);
+    CANON_TRY(cudaMemsetAsync(tk, 0, sizeof(unsigned), s));
+    CANON_TRY(cudaMemsetAsync(d_stop, 0, (size_t)n * sizeof(unsigned), s));
     const uint64_t work = (uint64_t)n * (levels == 2 ? v * v : v);
-    int grid = blocks_for((const void *)bibd_split_kernel, num_sms);
     const int need = (int)((work + TPB - 1) / TPB);
-    if (grid > need)
-        grid = need;
+    int grid = 0;
+    CANON_TRY(grid_for((const void *)bibd_split_kernel, num_sms, need, &grid));
     bibd_split_kernel<<<grid, TPB, 0, s>>>(n, v, b, flags, levels, d_rows, d_parts, d_stop, max_trials, tk);
+    CANON_TRY(cudaGetLastError());
     const int g2 = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
     bibd_split_combine_kernel<<<g2, 256, 0, s>>>(n, v, levels, d_parts, d_stop, d_canonical, d_aut, d_status);
     return cudaGetLastError();
@@ -532,12 +599,11 @@ cudaError_t launch_bibd_canonize(uint32_t n, uint32_t v, uint32_t b, uint64_t *d
                                  uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
     if (!n || first_item >= n || !stride_items)
         return cudaSuccess;
-    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
-    int grid = blocks_for((const void *)bibd_canonize_kernel, num_sms);
+    CANON_TRY(cudaMemsetAsync(tk, 0, sizeof(unsigned), s));
     const uint32_t cnt = (n - first_item + stride_items - 1) / stride_items;
     const int need = (int)((cnt + TPB - 1) / TPB);
-    if (grid > need)
-        grid = need;
+    int grid = 0;
+    CANON_TRY(grid_for((const void *)bibd_canonize_kernel, num_sms, need, &grid));
     bibd_canonize_kernel<<<grid, TPB, 0, s>>>(n, v, b, d_rows, d_aut, d_status, stride_items, first_item,
                                               max_trials, tk);
     return cudaGetLastError();
@@ -551,7 +617,7 @@ cudaError_t launch_bibd_canonize(uint32_t n, uint32_t v, uint32_t b, uint64_t *d
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr uint32_t NOALLOC_MAX_ITEMS = 65536;                       // CANON_NOALLOC_MAX_ITEMS
+constexpr uint32_t NOALLOC_MAX_ITEMS = CANON_NOALLOC_MAX_ITEMS;     // 65,536 work descriptors
 constexpr size_t NOALLOC_COUNTER_OFF = (size_t)NOALLOC_MAX_ITEMS * sizeof(Item);
 constexpr size_t NOALLOC_SCRATCH_BYTES = NOALLOC_COUNTER_OFF + 256;   // 1 MiB + 256 B
 

@@ -83,6 +83,13 @@ cudaError_t launch_bibd_check_split(uint32_t n, uint32_t v, uint32_t b, uint32_t
 cudaError_t launch_bibd_labels(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
                                uint16_t *d_first_rows, uint64_t *d_nodes, const uint64_t *d_orders,
                                uint64_t max_nodes, unsigned *d_ticket, int num_sms, cudaStream_t s);
+// per-matrix node counts of the lex-max pass of the resident check (the search of
+// bibd_max_kernel, same tree): the work measure of the check's integer roofline
+cudaError_t launch_bibd_lexmax_nodes(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
+                                     uint64_t *d_nodes, uint64_t max_nodes, unsigned *d_ticket, int num_sms,
+                                     cudaStream_t s, const uint64_t *d_orders = nullptr);
+// integer-pipe throughput probe: *ops = 32-bit lane operations of the launch
+cudaError_t launch_int_peak(uint32_t iters, int num_sms, uint32_t *d_sink, cudaStream_t s, uint64_t *ops);
 // order of the rows as first-row candidates by decreasing score (scores: n x v floats)
 cudaError_t launch_order_by_score(uint32_t n, uint32_t v, const float *d_scores, uint64_t *d_orders,
                                   cudaStream_t s);

@@ -83,9 +83,13 @@ cudaError_t launch_mixed_check(const Item *d_bitems, uint32_t nb, const Item *d_
                                uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
     if (!nb && !nk)
         return cudaSuccess;
-    cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
+    cudaError_t e = cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
+    if (e != cudaSuccess)
+        return e;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mixed_kernel, MTPB, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mixed_kernel, MTPB, 0);
+    if (e != cudaSuccess)
+        return e;
     if (per_sm < 1)
         per_sm = 1;
     int grid = per_sm * (num_sms > 0 ? num_sms : 1);
@@ -137,9 +141,13 @@ cudaError_t launch_ksys_check(const Item *d_items, uint32_t n_items, const uint8
                               unsigned *tk, int num_sms, cudaStream_t s) {
     if (!n_items)
         return cudaSuccess;
-    cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
+    cudaError_t e = cudaMemsetAsync(tk, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess)
+        return e;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksys_kernel, ksys::KTPB, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksys_kernel, ksys::KTPB, 0);
+    if (e != cudaSuccess)
+        return e;
     if (per_sm < 1)
         per_sm = 1;
     int grid = per_sm * (num_sms > 0 ? num_sms : 1);

@@ -1,5 +1,5 @@
 // canon_ksys_core.cuh -- device search of the k-system checker (group size 2).
-// Included by canon_ksys.cu and canon_mixed.cu.
+// Included by canon_ksys.cu (the k-system kernel and the mixed persistent kernel).
 #pragma once
 #include "canon_internal.h"
 #include "canon_nibble.cuh"

@@ -60,12 +60,21 @@ struct DevBuf {
             return cudaSuccess;
         cudaFree(p);
         p = nullptr;
-        // at least double, so a growing enumeration reallocates (and synchronises) rarely
-        const size_t want = (n > 2 * cap ? n : 2 * cap) + 1024;
+        // at least double, so a growing enumeration reallocates (and synchronises) rarely;
+        // if that much does not fit, exactly what is needed (plus a little)
+        size_t want = (n > 2 * cap ? n : 2 * cap) + 1024;
         cap = 0;
-        const cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e == cudaErrorMemoryAllocation && want > n + 1024) {
+            (void)cudaGetLastError();   // clear the failed request before the retry
+            p = nullptr;
+            want = n + 1024;
+            e = cudaMalloc(&p, want * sizeof(T));
+        }
         if (e == cudaSuccess)
             cap = want;
+        else
+            p = nullptr;
         return e;
     }
     void swap(DevBuf &o) {
@@ -239,7 +248,9 @@ cudaError_t exclusive_scan(const T *in, uint64_t n, uint64_t *out, DevBuf<uint64
         scan_sums_kernel<<<1, SCAN_TPB, 0, s>>>(sums.p, ntiles);
         tile_scan_kernel<T><<<ntiles, SCAN_TPB, 0, s>>>(in, n, sums.p, ntiles, out);
     } else {
-        cudaMemsetAsync(out, 0, sizeof(uint64_t), s);
+        e = cudaMemsetAsync(out, 0, sizeof(uint64_t), s);
+        if (e != cudaSuccess)
+            return e;
     }
     return cudaGetLastError();
 }
@@ -251,16 +262,20 @@ cudaError_t read_u64(const uint64_t *d, uint64_t *h, cudaStream_t s) {
     return e;
 }
 
-int gen_grid(const void *kernel, int num_sms, uint64_t work) {
+// persistent grid of a generator kernel; a failed occupancy query is returned
+cudaError_t gen_grid(const void *kernel, int num_sms, uint64_t work, int *grid) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, GEN_TPB, 0);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, GEN_TPB, 0);
+    if (e != cudaSuccess)
+        return e;
     if (per_sm < 1)
         per_sm = 1;
     uint64_t g = (uint64_t)per_sm * (num_sms > 0 ? num_sms : 1);
     const uint64_t need = (work + GEN_TPB - 1) / GEN_TPB;
     if (g > need)
         g = need;
-    return (int)(g ? g : 1);
+    *grid = (int)(g ? g : 1);
+    return cudaSuccess;
 }
 
 // pinned host memory that grows (contents not kept)
@@ -272,12 +287,20 @@ struct PinBuf {
             return cudaSuccess;
         cudaFreeHost(p);
         p = nullptr;
-        // at least double: pinning memory is slow
-        const size_t want = (n > 2 * cap ? n : 2 * cap) + 1024;
+        // at least double: pinning memory is slow; exactly what is needed if that fails
+        size_t want = (n > 2 * cap ? n : 2 * cap) + 1024;
         cap = 0;
-        const cudaError_t e = cudaHostAlloc((void **)&p, want * sizeof(uint64_t), cudaHostAllocDefault);
+        cudaError_t e = cudaHostAlloc((void **)&p, want * sizeof(uint64_t), cudaHostAllocDefault);
+        if (e == cudaErrorMemoryAllocation && want > n + 1024) {
+            (void)cudaGetLastError();
+            p = nullptr;
+            want = n + 1024;
+            e = cudaHostAlloc((void **)&p, want * sizeof(uint64_t), cudaHostAllocDefault);
+        }
         if (e == cudaSuccess)
             cap = want;
+        else
+            p = nullptr;
         return e;
     }
     PinBuf() = default;
@@ -396,10 +419,17 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 e = rcache.ensure((size_t)n_par * ROW_CACHE);
             if (e != cudaSuccess)
                 return done(CANON_ENOMEM, "level buffers", e);
-            cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
-            rows_count_kernel<<<gen_grid((const void *)rows_count_kernel, c->num_sms, n_par), GEN_TPB, 0, s>>>(
-                prm, lev.p, (uint32_t)n_par, (int)n, dcounts.p, rcache.p, ticket.p);
-            e = exclusive_scan(dcounts.p, n_par, doffs.p, sums, s);
+            int grid = 0;
+            e = cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
+            if (e == cudaSuccess)
+                e = gen_grid((const void *)rows_count_kernel, c->num_sms, n_par, &grid);
+            if (e != cudaSuccess)
+                return done(CANON_ECUDA, "count", e);
+            rows_count_kernel<<<grid, GEN_TPB, 0, s>>>(prm, lev.p, (uint32_t)n_par, (int)n, dcounts.p, rcache.p,
+                                                       ticket.p);
+            e = cudaGetLastError();
+            if (e == cudaSuccess)
+                e = exclusive_scan(dcounts.p, n_par, doffs.p, sums, s);
             if (e == cudaSuccess)
                 e = read_u64(doffs.p + n_par, &n_cand, s);
             if (e != cudaSuccess)
@@ -470,9 +500,14 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 });
                 e = cudaMemcpyAsync(cand.p, hcand.p, (size_t)ns * m * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
             } else {
-                cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
-                rows_emit_kernel<<<gen_grid((const void *)rows_emit_kernel, c->num_sms, p1 - p0), GEN_TPB, 0, s>>>(
-                    prm, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, doffs.p, dcounts.p, rcache.p, cand.p, ticket.p);
+                int grid = 0;
+                e = cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s);
+                if (e == cudaSuccess)
+                    e = gen_grid((const void *)rows_emit_kernel, c->num_sms, p1 - p0, &grid);
+                if (e != cudaSuccess)
+                    return done(CANON_ECUDA, "children", e);
+                rows_emit_kernel<<<grid, GEN_TPB, 0, s>>>(prm, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, doffs.p,
+                                                          dcounts.p, rcache.p, cand.p, ticket.p);
                 e = cudaGetLastError();
                 if (e == cudaSuccess)
                     e = cudaStreamSynchronize(s);
@@ -502,8 +537,9 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
             // 4: pack the canonical ones into the next level
             if (e == cudaSuccess)
                 e = exclusive_scan(can.p, ns, coffs.p, sums, s);
+            if (e == cudaSuccess)
+                e = cudaMemsetAsync(ticket.p + 1, 0, sizeof(unsigned), s);
             if (e == cudaSuccess) {
-                cudaMemsetAsync(ticket.p + 1, 0, sizeof(unsigned), s);
                 const int grid = (int)((ns + 255) / 256 < 4096 ? (ns + 255) / 256 : 4096);
                 compact_kernel<<<grid ? grid : 1, 256, 0, s>>>(ns, (int)m, cand.p, can.p, status.p,
                                                                complete ? aut.p : nullptr, coffs.p,

@@ -2,6 +2,13 @@
 #pragma once
 #include <cstdint>
 
+#ifndef __CUDACC__
+// host-only translation units (g++) include the host-and-device helpers too
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#endif
+
 namespace canon {
 
 constexpr uint64_t NIB_ID16 = 0xFEDCBA9876543210ull;   // identity permutation of 0..15

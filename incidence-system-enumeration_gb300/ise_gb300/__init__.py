@@ -58,7 +58,8 @@ HEADER_SYMBOLS = [
     "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys", "canon_mlp_features",
     "canon_label_first_rows", "canon_mlp_forward", "canon_mlp_grad", "canon_mlp_train",
     "canon_design_properties", "canon_report_bibd", "canon_ksys_cycles", "canon_report_ksys",
-    "canon_tune_bibd",
+    "canon_tune_bibd", "canon_generate_partial_bibd", "canon_generate_partial_ksys", "canon_lexmax_nodes_bibd",
+    "canon_measure_int_peak",
 ]
 MLP_PARAMS = 128 * 64 + 128 + 128 * 128 + 128 + 128 + 1
 
@@ -193,6 +194,11 @@ def load_library(path=LIB_PATH):
     L.canon_ksys_cycles.restype = sz
     L.canon_report_ksys.argtypes = [u32, u32, u32, u8p, u64p, ctypes.c_char_p, sz]
     L.canon_report_ksys.restype = sz
+    L.canon_generate_partial_bibd.argtypes = [u32, u32, u32, u32, u32, u32, u64, u32, u32, u64p, u8p,
+                                              ctypes.POINTER(ctypes.c_uint32)]
+    L.canon_generate_partial_ksys.argtypes = [u32, u32, u64, u32, u32, u8p, u8p]
+    L.canon_lexmax_nodes_bibd.argtypes = [vp, u32, u32, u32, u32, vp, vp]
+    L.canon_measure_int_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     _lib = L
     return L
 
@@ -260,6 +266,35 @@ def report_ksys(matrices, auts, lib=None):
     n, rounds, np_ = X.shape
     return _text(lambda buf, cap: L.canon_report_ksys(np_, rounds, n, _ptr(X, ctypes.c_uint8),
                                                       _ptr(a, ctypes.c_uint64), buf, cap))
+
+
+def generate_partial_bibd(params, n, seed, min_rows, max_rows, lib=None):
+    """n seeded partial BIBD(v,b,r,k,lambda) matrices by random backtracking of their
+    rows (canon_generate_partial_bibd): (rows n x v uint64, nrows n uint8, number of
+    items taken from a complete design)."""
+    L = lib or load_library()
+    v, b, r, k, lam = params
+    rows = np.zeros((n, v), np.uint64)
+    nrows = np.zeros(n, np.uint8)
+    fc = ctypes.c_uint32(0)
+    rc = L.canon_generate_partial_bibd(v, b, r, k, lam, n, seed, min_rows, max_rows, _ptr(rows, ctypes.c_uint64),
+                                       _ptr(nrows, ctypes.c_uint8), ctypes.byref(fc))
+    if rc != CANON_OK:
+        raise CanonError(rc, "generate_partial_bibd")
+    return rows, nrows, int(fc.value)
+
+
+def generate_partial_ksys(np_, n, seed, min_rounds, max_rounds, lib=None):
+    """n seeded partial 1-factorizations of K_np, round by round with random
+    backtracking (canon_generate_partial_ksys): (data n x (np-1) x np uint8, nrows)."""
+    L = lib or load_library()
+    data = np.zeros((n, np_ - 1, np_), np.uint8)
+    nrows = np.zeros(n, np.uint8)
+    rc = L.canon_generate_partial_ksys(np_, n, seed, min_rounds, max_rounds, _ptr(data, ctypes.c_uint8),
+                                       _ptr(nrows, ctypes.c_uint8))
+    if rc != CANON_OK:
+        raise CanonError(rc, "generate_partial_ksys")
+    return data, nrows
 
 
 def pack_rows(M):
@@ -410,6 +445,16 @@ class Context:
         st = EnumStats()
         self._check(self.lib.canon_enumerate_bibd(self.h, v, b, r, k, lam, c, None, ctypes.byref(st)))
         return found, st
+
+    def lexmax_nodes_bibd(self, n, v, b, flags, d_rows, d_nodes):
+        """Lex-max nodes per matrix of the resident check's first pass (device array)."""
+        self._check(self.lib.canon_lexmax_nodes_bibd(self.h, n, v, b, flags, d_rows, d_nodes))
+
+    def measure_int_peak(self):
+        """32-bit integer lane operations per second of this GPU (canon_measure_int_peak)."""
+        x = ctypes.c_double(0)
+        self._check(self.lib.canon_measure_int_peak(self.h, ctypes.byref(x)))
+        return x.value
 
     def tune_bibd(self, n, v, b, flags, d_rows):
         """Autotunes the check variant for (v, b, flags) on n device-resident matrices;

@@ -207,6 +207,17 @@ int canon_tune_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t
                     canon_tune_result *out);
 int canon_generate_sts_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint64_t seed, int canon_odd,
                               uint64_t *d_rows, void *stream);
+/* ---- measurement ----
+ * Lex-max nodes visited per matrix by the search of the resident check's first pass
+ * (its verdict and |Aut|), for n device-resident matrices: the work measure of the
+ * check's integer roofline.  With a learned order installed (canon_set_ordering) the
+ * search runs in that order, as canon_check_bibd_device runs it.  d_nodes: n device
+ * words. */
+int canon_lexmax_nodes_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
+                            const uint64_t *d_rows, uint64_t *d_nodes);
+/* 32-bit integer lane operations per second that this GPU sustains on independent
+ * XOR / ADD / shift chains (the peak of the check's integer roofline). */
+int canon_measure_int_peak(canon_ctx *ctx, double *lane_ops_per_s);
 /* Device memory helpers so callers without a CUDA toolchain can hold batches in HBM. */
 void *canon_device_alloc(canon_ctx *ctx, size_t bytes);
 int   canon_device_free(canon_ctx *ctx, void *p);
@@ -250,6 +261,33 @@ int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uin
  * group size 2 with the check at every level (k-Factorization/TripleSys/Source/
  * TripleSys.cpp:80-775, check at checkCurrentResult.cpp:91).  np even, <= 12. */
 int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *user, canon_enum_stats *stats);
+
+/* ---- seeded inputs of an uneven batched check ----
+ * n partial BIBD(v, b, r, k, lambda) incidence matrices made by random backtracking of
+ * their rows, as an orderly enumerator meets them (the row constraints of
+ * C_InSysEnumerator's row solutions, Source/Enumerator.cpp:726-975, with MakeRow,
+ * Source/MatrixCanonChecker.cpp:14-93, drawn at random): item i has nrows[i] rows,
+ * uniform in [min_rows, max_rows]; each row has weight r, lambda columns in common
+ * with every earlier row, no column above k ones and no column left unable to reach
+ * k ones with the rows below.  A level without an admissible row drops the row above
+ * and draws it again, so dead ends that no complete design extends are included.
+ * A Steiner triple system (k = 3, lambda = 1) with v-1 or v rows filled is a complete
+ * design (v-1 admissible rows determine the last), which row-by-row backtracking
+ * reaches only rarely: such items, and any whose search budget runs out, are the
+ * first rows of a complete random STS(v) (Stinson's hill-climbing, uniform row and
+ * column permutation); *n_from_complete (optional) counts them.
+ * rows: n*v words (unfilled rows 0), bit c = column c.  Item i uses its own random
+ * stream (seed, i); the work is spread over the host cores.  CANON_ETIMEOUT if an
+ * item's search budget ran out (its nrows is then 0).  Host only. */
+int canon_generate_partial_bibd(uint32_t v, uint32_t b, uint32_t r, uint32_t k, uint32_t lambda, uint32_t n,
+                                uint64_t seed, uint32_t min_rows, uint32_t max_rows, uint64_t *rows,
+                                uint8_t *nrows, uint32_t *n_from_complete);
+/* n partial 1-factorizations of K_np (np even, <= 12), the same way round by round:
+ * round 0 is (0 1)(2 3)..., every further round a random perfect matching of pairs not
+ * used before, in result() form (pairs ascending, ordered by first player), the
+ * rounds ordered by the partner of player 0.  data: n*(np-1)*np bytes, item i's round d at (i*(np-1) + d)*np. */
+int canon_generate_partial_ksys(uint32_t np, uint32_t n, uint64_t seed, uint32_t min_rounds, uint32_t max_rounds,
+                                uint8_t *data, uint8_t *nrows);
 
 /* ---- result tables (the reference's text output of a finished run) ----
  * Per complete design: simple[i] = no two equal columns (no replicated blocks) and
@@ -332,18 +370,21 @@ typedef struct {
 #define CANON_NOALLOC_MAX_ITEMS 65536u
 
 /* The batched TestCanonicity() check of canon_submit_bibd + canon_sync for
- * device-resident matrices, for callers that cannot call cudaMalloc: code that
- * runs while a CUDA graph is being captured, inside a host application whose
- * device memory belongs to another allocator or pool, or on a latency path
- * where the implicit synchronisation of cudaMalloc/cudaFree is not acceptable.
- * It needs no context and allocates nothing: its scratch (one 16-byte work
- * descriptor per matrix and a work counter) is a static device array of
- * 1 MiB + 256 bytes that every GPU loading this library holds until the
- * process exits.  Hence at most CANON_NOALLOC_MAX_ITEMS matrices per call;
+ * device-resident matrices, for callers that cannot call cudaMalloc: a host
+ * application whose device memory belongs to another allocator or pool (a
+ * framework's caching allocator, a fixed arena sized at start-up), or a latency
+ * path where the implicit device synchronisation of cudaMalloc/cudaFree is not
+ * acceptable.  It needs no context and allocates nothing: its scratch (one
+ * 16-byte work descriptor per matrix and a work counter) is a static device
+ * array of 1 MiB + 256 bytes that every GPU loading this library holds until
+ * the process exits.  Hence at most CANON_NOALLOC_MAX_ITEMS matrices per call;
  * larger batches are refused with CANON_ESIZE.  Rows and per-matrix filled-row
  * counts (d_nrows, NULL = all v) are device pointers laid out as in
  * canon_bibd_batch; `out` holds device pointers.  Launched on `stream`
  * (a cudaStream_t, NULL = the default stream) and not waited for.
+ * Unlike canon_submit_bibd, which refuses a whole batch with CANON_EINVAL when a
+ * filled-row count is 0 or above v, the counts are only read on the GPU here: such
+ * a matrix gets status CANON_ST_BADINPUT (canonical 0) and the others are checked.
  * The first call on a device looks up the scratch's device address (once per
  * device, with that device current), so make that first call before any stream
  * capture.  All calls share the one scratch array: calls whose work overlaps on

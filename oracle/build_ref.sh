@@ -2,9 +2,10 @@
 # Builds oracle/_ref/libref_grouporder.so from the reference's GroupOrder.h as it
 # lies in the reference tree (read-only; nothing is copied).  Two shim headers
 # stand in for MSVC-only system headers; __declspec is defined away.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   (default: $ISE_REFERENCE_ROOT, else /root/reference, where this build found it)
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${ISE_REFERENCE_ROOT:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/k-Factorization/Utils/Include/GroupOrder.h" ]; then

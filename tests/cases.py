@@ -114,3 +114,25 @@ def table_rows(designs, simple, transitive):
         r[3] += bool(t)
         r[4] += bool(s and t)
     return [rows[a] for a in sorted(rows)]
+
+
+def oracle_sts_check(rows, b=35):
+    """Oracle outputs of a complete STS check with |Aut| of rejected matrices from
+    their canonical form (COMPLETE|RAW|AUT_CANON): (canonical, witness, aut)."""
+    M = oracle.bibd_normalize(oracle.rows_to_matrix(rows, b))
+    o = oracle.bibd_test(M, oracle.SAVE_ROW_PERM | oracle.SAVE_ROW_TO_CHANGE)
+    aut = o["aut"]
+    if not o["canonical"]:
+        _, aut, _ = oracle.bibd_canonize(M)
+    return o["canonical"], o["witness"], aut, o["row_to_change"]
+
+
+def compare_sts_sample(rows, can, wit, aut, idx, v=15, b=35):
+    """Every item of `idx` against the oracle (host threads)."""
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        for i, (oc, ow, oa, _) in zip(idx, ex.map(lambda i: oracle_sts_check(rows[i], b), idx)):
+            assert bool(can[i]) == oc, i
+            assert int(aut[i][0]) == oa and int(aut[i][1]) == 0, (i, aut[i], oa)
+            if not oc:
+                assert bytes(wit[i][:v]) == ow, i

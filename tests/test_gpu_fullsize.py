@@ -17,16 +17,36 @@ SEED = 20241203          # the bench's seed
 V, B = 15, 35
 
 
-def check(ctx, d_rows, flags):
+def check(ctx, d_rows, flags, witness=False):
     d_can, d_aut, d_st = ctx.alloc(N), ctx.alloc(16 * N), ctx.alloc(N)
-    ctx.check_bibd_device(N, V, B, flags, d_rows, d_can, None, d_aut, d_st)
+    d_wit = ctx.alloc(16 * N) if witness else None
+    ctx.check_bibd_device(N, V, B, flags, d_rows, d_can, d_wit, d_aut, d_st)
     ctx.stream_sync()
     can = ctx.d2h(np.zeros(N, np.uint8), d_can)
     aut = ctx.d2h(np.zeros(2 * N, np.uint64), d_aut).reshape(N, 2)
     st = ctx.d2h(np.zeros(N, np.uint8), d_st)
-    for p in (d_can, d_aut, d_st):
+    wit = ctx.d2h(np.zeros(16 * N, np.uint8), d_wit).reshape(N, 16) if witness else None
+    for p in (d_can, d_aut, d_st) + ((d_wit,) if witness else ()):
         ctx.free(p)
-    return can, aut, st
+    return (can, aut, st, wit) if witness else (can, aut, st)
+
+
+def test_config2_full_size_sample_matches_oracle():
+    """The bench's 1,048,576-matrix batch as the bench checks it (verdict, first
+    rejecting permutation, |Aut| via the canonical form); every 512th item against
+    the oracle."""
+    ctx = G.Context(max_items=N)
+    try:
+        d_rows = ctx.alloc(N * V * 8)
+        ctx.generate_sts_device(N, V, SEED, True, d_rows)
+        ctx.stream_sync()
+        rows = ctx.d2h(np.zeros(N * V, np.uint64), d_rows).reshape(N, V)
+        can, aut, st, wit = check(ctx, d_rows, G.COMPLETE | G.RAW | G.AUT_CANON, witness=True)
+        ctx.free(d_rows)
+    finally:
+        ctx.close()
+    assert not st.any()
+    cases.compare_sts_sample(rows, can, wit, aut, range(0, N, 512))
 
 
 def test_config2_full_size_properties():

@@ -153,3 +153,50 @@ def test_first_row_labels_start_a_canonical_labeling(ctx):
         # the first rows of the labelings reaching the canonical form are one orbit of
         # Aut(M) on the rows: at least one row, and their number divides |Aut|
         assert k >= 1 and aut % k == 0, (i, k, aut)
+
+
+def test_config4_eval_batch_learned_order_matches_oracle():
+    """Config 4's evaluation batch at full size (1,048,576 fresh STS(15), the bench's
+    seed + 1) under a trained learned order: every output equals the plain order's
+    on every item, and every 512th item equals the oracle."""
+    n, V, B, seed = 1 << 20, 15, 35, 20241203
+    ctx = G.Context(max_items=16, aut_cap=1)
+    try:
+        # a short training run on the training seed's batch (labels from the exact search)
+        n_train = 1 << 14
+        d_tr = ctx.alloc(n_train * V * 8)
+        ctx.generate_sts_device(n_train, V, seed, True, d_tr)
+        d_lab = ctx.alloc(2 * n_train)
+        ctx.label_first_rows(n_train, V, B, G.RAW, d_tr, d_lab)
+        lab = ctx.d2h(np.zeros(n_train, np.uint16), d_lab)
+        labels = ((lab[:, None] >> np.arange(V, dtype=np.uint16)) & 1).astype(np.float32).reshape(-1)
+        d_feat = ctx.alloc(n_train * V * 64 * 2)
+        ctx.mlp_features(n_train, V, B, d_tr, d_feat)
+        d_y = to_device(ctx, labels)
+        params, _ = ctx.mlp_train(n_train * V, d_feat, d_y, G.init_mlp_params(seed), epochs=1, batch=8192, lr=1e-3)
+        for p_ in (d_tr, d_lab, d_feat, d_y):
+            ctx.free(p_)
+        d_rows = ctx.alloc(n * V * 8)
+        ctx.generate_sts_device(n, V, seed + 1, True, d_rows)
+        ctx.stream_sync()
+        rows = ctx.d2h(np.zeros(n * V, np.uint64), d_rows).reshape(n, V)
+        flags = G.COMPLETE | G.RAW | G.AUT_CANON
+        outs = {}
+        for name, prm in (("plain", None), ("learned", params)):
+            ctx.set_ordering(prm)
+            d = [ctx.alloc(n), ctx.alloc(16 * n), ctx.alloc(16 * n), ctx.alloc(n)]
+            ctx.check_bibd_device(n, V, B, flags, d_rows, *d)
+            ctx.stream_sync()
+            outs[name] = [ctx.d2h(np.zeros(n * k, np.uint8), p_) for p_, k in zip(d, (1, 16, 16, 1))]
+            for p_ in d:
+                ctx.free(p_)
+        ctx.set_ordering(None)
+        ctx.free(d_rows)
+    finally:
+        ctx.close()
+    for a, b in zip(outs["plain"], outs["learned"]):
+        assert np.array_equal(a, b)
+    can, wit, aut, st = outs["learned"]
+    assert not st.any()
+    import cases
+    cases.compare_sts_sample(rows, can, wit.reshape(n, 16), aut.view(np.uint64).reshape(n, 2), range(0, n, 512))

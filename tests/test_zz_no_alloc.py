@@ -1,10 +1,11 @@
 """canon_check_bibd_noalloc: the check for callers that cannot allocate device
-memory (stream capture, a host whose device memory belongs to another
-allocator, latency paths that cannot take cudaMalloc's synchronisation).
+memory (a host whose device memory belongs to another allocator or a fixed
+arena, latency paths that cannot take cudaMalloc's device synchronisation).
 It is called through the C ABI and must give exactly what the batched entry
 point (canon_submit_bibd + canon_sync) gives, on two calls in a row, which also
-shows that the shared static scratch is reset between calls.  Collected last so
-that a run stopping at the first failure has run everything else already."""
+shows that the shared static scratch is reset between calls; the free device
+memory must not change across a call.  Collected last so that a run stopping at
+the first failure has run everything else already."""
 import ctypes
 
 import numpy as np
@@ -40,8 +41,9 @@ def batch(seed):
     return rows, nrows
 
 
-def run_noalloc(ctx, rows, nrows, flags, aut_cap=16):
-    n = len(nrows)
+def run_noalloc(ctx, rows, nrows, flags, aut_cap=16, pass_nrows=True):
+    import torch
+    n = len(rows)
     lib = G.load_library()
     d_rows = ctx.alloc(rows.nbytes)
     d_nrows = ctx.alloc(n)
@@ -51,15 +53,22 @@ def run_noalloc(ctx, rows, nrows, flags, aut_cap=16):
     ptrs["auts"] = ctx.alloc(n * aut_cap * 64)
     try:
         out = G.DeviceOutputs(**{k: ptrs[k] for k in ptrs}, aut_cap=aut_cap)
-        rc = lib.canon_check_bibd_noalloc(n, 15, 35, flags, d_rows, d_nrows, ctypes.byref(out), 1 << 24, None)
-        assert rc == G.CANON_OK
+        free = []
+        # the same call twice: the first may load the kernels' code (lazy module
+        # loading); around the second the free device memory must not change
+        for _ in range(2):
+            torch.cuda.synchronize()
+            free.append(torch.cuda.mem_get_info()[0])
+            rc = lib.canon_check_bibd_noalloc(n, 15, 35, flags, d_rows, d_nrows if pass_nrows else None,
+                                              ctypes.byref(out), 1 << 24, None)
+            assert rc == G.CANON_OK
+            # launched on the default stream, which the context's (non-blocking) stream does not wait for
+            torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free[1], "the call changed the free device memory"
     except Exception:
         for p in list(ptrs.values()) + [d_rows, d_nrows]:
             ctx.free(p)
         raise
-    # launched on the default stream, which the context's (non-blocking) stream does not wait for
-    import torch
-    torch.cuda.synchronize()
     res = {}
     for name, size, dt in FIELDS:
         host = np.zeros(n * size, np.uint8)
@@ -99,6 +108,31 @@ def test_noalloc_matches_batched_entry_point_twice(flags):
                 for i in range(n):
                     k, ln = min(int(ref["n_auts"][i]), 16), int(ref["len_aut"][i])
                     assert np.array_equal(got["auts"][i][:k, :ln], ref["auts_raw"][i][:k, :ln]), (call, i)
+    finally:
+        ctx.close()
+
+
+def test_noalloc_flags_bad_row_counts_per_matrix_and_takes_null_counts():
+    """A filled-row count of 0 or above v marks that matrix CANON_ST_BADINPUT and
+    leaves the others checked; without counts every matrix has all v rows."""
+    ctx = G.Context(max_items=1024, aut_cap=16, max_trials=1 << 24)
+    try:
+        rows, nrows = batch(2024)
+        full = rows[nrows == 15]
+        bad = nrows.copy()
+        bad[1], bad[4] = 0, 16
+        got = run_noalloc(ctx, rows, bad, 0)
+        assert got["status"][1] == G.ST_BADINPUT and got["status"][4] == G.ST_BADINPUT
+        assert got["canonical"][1] == 0 and got["canonical"][4] == 0
+        keep = np.ones(len(bad), bool)
+        keep[[1, 4]] = False
+        ref = run_batched(ctx, rows[keep], nrows[keep], 0)
+        assert np.array_equal(got["canonical"][keep], ref["canonical"].astype(np.uint8))
+        assert np.array_equal(got["witness"].reshape(-1, 16)[keep], ref["witness"])
+        got = run_noalloc(ctx, full, np.full(len(full), 15, np.uint8), G.COMPLETE, pass_nrows=False)
+        ref = run_batched(ctx, full, None, G.COMPLETE)
+        assert np.array_equal(got["canonical"], ref["canonical"].astype(np.uint8))
+        assert np.array_equal(got["witness"].reshape(-1, 16), ref["witness"])
     finally:
         ctx.close()
 
