@@ -306,7 +306,7 @@ def run_gpu(args, rank, world, local, dist):
             "config": {"workload": WORKLOAD if n == N_ITEMS else "%d items of: %s" % (n, WORKLOAD),
                        "ordering": "plain", "flags": FLAGS_NAME if args.mode == "autcanon" else "COMPLETE|RAW",
                        "items_per_step": n, "canonical_fraction": float(can.mean()),
-                       "variant": ["one pass", "two passes", "split by first row"][variant],
+                       "variant": G.VARIANT_NAMES[variant],
                        "tune_ms_65536": [round(x, 2) for x in tune_ms],
                        "l2": "flushed between steps (512 MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -336,7 +336,7 @@ def integer_roofline(ctx, args, n, flags, variant, d_rows, d_can, d_aut, d_st, f
     nodes = ctx.d2h(np.zeros(n, np.uint64), d_nodes)
     ctx.free(d_nodes)
     ops = float(nodes.sum()) * B * INT_OPS_PER_NODE_COLUMN
-    if variant == G.VARIANT_TWO_PASS:
+    if variant in (G.VARIANT_TWO_PASS, G.VARIANT_CONVERGED):
         # the first pass alone: without witness and trials outputs only it is launched
         ms = []
         for _ in range(2):
@@ -344,7 +344,8 @@ def integer_roofline(ctx, args, n, flags, variant, d_rows, d_can, d_aut, d_st, f
             ctx.check_bibd_device(n, V, B, flags, d_rows, d_can, None, d_aut, d_st)
             ctx.stream_sync()
             ms.append(ctx.last_kernel_ms())
-        kname = "bibd_max_kernel<35, 15> (lex-max pass)"
+        kname = ("bibd_conv_kernel<35, 15> (lex-max pass, converged layout)" if variant == G.VARIANT_CONVERGED
+                 else "bibd_max_kernel<35, 15> (lex-max pass)")
     else:
         ms = list(times)
         kname = "the one-pass check kernel"

@@ -15,7 +15,7 @@
 #include <mutex>
 
 #include "../../include/canon_gb300.h"
-#include "canon_bibd_core.cuh"
+#include "canon_bibd_conv.cuh"
 
 namespace canon {
 
@@ -146,6 +146,92 @@ __global__ void __launch_bounds__(256) int_peak_kernel(uint32_t iters, uint32_t 
     const uint32_t r = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
     if (r == never)
         sink[0] = r;
+}
+
+// Pass 1 in the converged layout (canon_bibd_conv.cuh): the same search, verdict,
+// |Aut| and node count as bibd_max_kernel, with every iteration of the loop split
+// into control steps (divergent, short) and one node step per thread -- the column
+// arrangement for the chosen child and the evaluation of the new node, one pass over
+// the b columns with the same trip count in every lane.  A thread that finishes its
+// matrix takes the next one inside the control steps, so the lanes keep evaluating
+// nodes together until the batch runs out.
+template <int BCAP, int VCAP>
+__global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
+                                                        const uint64_t *__restrict__ rows, uint8_t *canonical,
+                                                        uint64_t *aut, uint8_t *status, uint64_t max_nodes,
+                                                        unsigned *ticket, const uint64_t *__restrict__ orders,
+                                                        uint64_t *nodes_out) {
+    __shared__ uint64_t s_rows[VCAP * TPB];
+    __shared__ uint64_t s_lvl[(VCAP + 1) * TPB];
+    __shared__ uint16_t s_vd[VCAP * TPB];
+    __shared__ uint16_t s_cm[BCAP * TPB];
+    const unsigned tid = threadIdx.x;
+    SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    const bool want_aut = flags & (F_AUT_CANON | F_FULL_AUT);
+    ConvState st{};
+    uint32_t it = 0;
+    bool have = false, done = false;
+    // outputs of the matrix this thread has finished (status: 0, ST_BADINPUT, ST_TIMEOUT)
+    auto finish = [&](uint8_t stat) {
+        const bool can = !stat && !st.improved;
+        if (canonical)
+            canonical[it] = can ? 1 : 0;
+        if (status)
+            status[it] = stat;
+        if (aut) {
+            aut[2 * (size_t)it] = (!stat && (can || want_aut)) ? conv_leaves(st) : 0;
+            aut[2 * (size_t)it + 1] = 0;
+        }
+        if (nodes_out)
+            nodes_out[it] = st.nodes;
+        have = false;
+    };
+    for (;;) {
+        // control steps until this thread has a node to evaluate, or no work is left
+        int ref_lv = -1;
+        unsigned ref_x = 0;
+        bool eval = false;
+        while (!done && !eval) {
+            if (!have) {
+                it = atomicAdd(ticket, 1u);
+                if (it >= n_items) {
+                    done = true;
+                    break;
+                }
+                conv_start(st, v, orders ? orders[it] : ID16);
+                have = true;
+                if (!load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW)) {
+                    finish(ST_BADINPUT);
+                    continue;
+                }
+                eval = true;        // the root: no arrangement step
+                break;
+            }
+            if (conv_next(sm, st, ref_lv, ref_x)) {
+                eval = true;
+                break;
+            }
+            finish(0);
+        }
+        if (__all_sync(0xFFFFFFFFu, done))
+            break;
+        if (!eval)
+            continue;
+        // the node step: every lane with a node runs the same b-column passes
+        if (ref_lv >= 0)
+            refine_uniform(sm, (unsigned)ref_lv, ref_x, b);
+        if (++st.nodes > max_nodes) {
+            st.timeout = true;
+            finish(ST_TIMEOUT);
+            continue;
+        }
+        unsigned tied = st.allrows & ~st.used;
+        uint64_t arr = 0;
+        const bool hb = st.i < st.valid;
+        const int state = eval_node_uniform(sm, st.i, b, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        if (!conv_after_eval(sm, st, state, tied, arr, b))
+            finish(0);
+    }
 }
 
 // Pass 2: the first rejecting permutation (reference order) of the matrices that
@@ -488,7 +574,9 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
         return cudaSuccess;
     const int need = (int)((n + TPB - 1) / TPB);
     const bool ref_order = flags & (F_SAVE_AUTS | F_REFERENCE_ORDER);
-    const bool two = !ref_order && (variant < 0 ? (flags & (F_AUT_CANON | F_FULL_AUT)) != 0 : variant == 1);
+    const bool two = !ref_order && (variant < 0 ? (flags & (F_AUT_CANON | F_FULL_AUT)) != 0
+                                                : (variant == VARIANT_TWO_PASS || variant == VARIANT_CONVERGED));
+    const bool conv = variant == VARIANT_CONVERGED;
     if (two) {
         // |Aut| wanted for every matrix: two passes, the lex-max search for all,
         // the reference-order witness for the rejected ones.  (Without it the
@@ -496,20 +584,34 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
         // of the reference order and runs the lex-max search only for the rest.)
         CANON_TRY(cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s));
         // the smallest instance that holds the shape
-        const void *kfn = (v <= 15 && b <= 35) ? (const void *)bibd_max_kernel<35, 15>
-                          : (b <= 40)          ? (const void *)bibd_max_kernel<40, 16>
-                                               : (const void *)bibd_max_kernel<64, 16>;
+        const int shape = (v <= 15 && b <= 35) ? 0 : (b <= 40 ? 1 : 2);
+        const void *kfn = conv ? (shape == 0   ? (const void *)bibd_conv_kernel<35, 15>
+                                  : shape == 1 ? (const void *)bibd_conv_kernel<40, 16>
+                                               : (const void *)bibd_conv_kernel<64, 16>)
+                               : (shape == 0   ? (const void *)bibd_max_kernel<35, 15>
+                                  : shape == 1 ? (const void *)bibd_max_kernel<40, 16>
+                                               : (const void *)bibd_max_kernel<64, 16>);
         int grid = 0;
         CANON_TRY(grid_for(kfn, num_sms, need, &grid));
-        if (v <= 15 && b <= 35)
-            bibd_max_kernel<35, 15><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
-                                                         max_trials, tk, d_orders, nullptr);
-        else if (b <= 40)
-            bibd_max_kernel<40, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
-                                                         max_trials, tk, d_orders, nullptr);
-        else
-            bibd_max_kernel<64, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status,
-                                                         max_trials, tk, d_orders, nullptr);
+#define CANON_PASS1(K, BC, VC)                                                                                  \
+    K<BC, VC><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status, max_trials, tk, d_orders, \
+                                   nullptr)
+        if (conv) {
+            if (shape == 0)
+                CANON_PASS1(bibd_conv_kernel, 35, 15);
+            else if (shape == 1)
+                CANON_PASS1(bibd_conv_kernel, 40, 16);
+            else
+                CANON_PASS1(bibd_conv_kernel, 64, 16);
+        } else {
+            if (shape == 0)
+                CANON_PASS1(bibd_max_kernel, 35, 15);
+            else if (shape == 1)
+                CANON_PASS1(bibd_max_kernel, 40, 16);
+            else
+                CANON_PASS1(bibd_max_kernel, 64, 16);
+        }
+#undef CANON_PASS1
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;

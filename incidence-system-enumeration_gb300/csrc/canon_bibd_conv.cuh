@@ -1,0 +1,226 @@
+// canon_bibd_conv.cuh -- the lex-max search of canon_bibd_core.cuh (max_search()) laid
+// out so that the threads of a warp stay converged.
+//
+// Each thread owns one matrix, as in bibd_max_kernel, but the search is a state
+// machine whose steps are of two kinds:
+//   control -- choosing the next child, backtracking, leaves, automorphism orbits,
+//              finishing a matrix and taking the next: short, divergent code;
+//   node    -- arranging the columns for the chosen child and evaluating the new
+//              node: one pass over all b columns of the matrix with the same trip
+//              count in every thread, whatever the thread's level and orbits.
+// Every iteration of the kernel's loop runs the control steps until each thread has
+// one node to evaluate, then all threads evaluate their node together.  In
+// max_search() the loops over orbits and over the columns of an orbit have
+// data-dependent lengths, so the 32 threads of a warp rarely run the same
+// instruction (5.5 of 32 lanes active on STS(15)); here the heavy part runs with
+// every active lane.
+//
+// The search tree, the node count, the verdict and |Aut| are those of max_search()
+// with automorphism pruning (prune = true, stop_on_improve = false, all first rows):
+//   - node evaluation: the greatest arranged row over the unused rows, orbit by
+//     orbit, bit-sliced over the rows (the comparison of checkColOrbit(),
+//     Source/CanonicityChecker.cpp:191-223), compared with the bound as it is built;
+//   - column arrangement: inside every orbit of the parent's level the columns with
+//     a 1 in the chosen row go first (a one-pass partition; only the set of columns
+//     of an orbit matters to later levels, not their order inside it);
+//   - the last level's arrangement is skipped: a leaf is never evaluated.
+#pragma once
+#include "canon_bibd_core.cuh"
+
+namespace canon {
+namespace bibd {
+namespace {
+
+// the greatest arranged row over `tied` at level lv, compared with `bound`:
+// 0 equal so far, 1 greater, 2 smaller (have_bound false: never compared, 0)
+template <typename S>
+__device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned &tied, uint64_t &arr,
+                                                 bool have_bound, uint64_t bound) {
+    const uint64_t lvl = L_(lv);
+    // bit p: column p closes an orbit (the next column starts one, or p is the last)
+    const uint64_t ends = (lvl >> 1) | (1ull << (b - 1));
+    unsigned t0 = tied;
+    uint64_t a = 0;
+    int state = 0;
+    unsigned p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
+    unsigned s = 0;
+    for (unsigned p = 0; p < b; ++p) {
+        unsigned carry = (unsigned)CM_(p) & t0, t;
+        t = p0 & carry; p0 ^= carry; carry = t;
+        t = p1 & carry; p1 ^= carry; carry = t;
+        t = p2 & carry; p2 ^= carry; carry = t;
+        t = p3 & carry; p3 ^= carry; carry = t;
+        t = p4 & carry; p4 ^= carry; carry = t;
+        p5 ^= carry;
+        if ((ends >> p) & 1u) {
+            unsigned cstar = 0;
+            t = t0 & p5; if (t) { t0 = t; cstar |= 32u; }
+            t = t0 & p4; if (t) { t0 = t; cstar |= 16u; }
+            t = t0 & p3; if (t) { t0 = t; cstar |= 8u; }
+            t = t0 & p2; if (t) { t0 = t; cstar |= 4u; }
+            t = t0 & p1; if (t) { t0 = t; cstar |= 2u; }
+            t = t0 & p0; if (t) { t0 = t; cstar |= 1u; }
+            a |= ((1ull << cstar) - 1ull) << s;
+            if (state == 0 && have_bound) {
+                const uint64_t rng = ((2ull << p) - 1ull) & ~((1ull << s) - 1ull);
+                const unsigned cb = __popcll(bound & rng);
+                state = cstar > cb ? 1 : (cstar < cb ? 2 : 0);
+            }
+            p0 = p1 = p2 = p3 = p4 = p5 = 0;
+            s = p + 1;
+        }
+    }
+    tied = t0;
+    arr = a;
+    return state;
+}
+
+// the columns of level lv+1 after row x was taken at level lv: inside every orbit of
+// level lv, the columns with a 1 in row x first (one pass, a write pointer per orbit)
+template <typename S>
+__device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, unsigned b) {
+    const uint64_t starts = L_(lv);
+    unsigned w = 0;
+    for (unsigned p = 0; p < b; ++p) {
+        if ((starts >> p) & 1u)
+            w = p;
+        const uint16_t c = CM_(p);
+        if ((c >> x) & 1u) {
+            CM_(p) = CM_(w);
+            CM_(w) = c;
+            ++w;
+        }
+    }
+}
+
+// the per-thread state of one lex-max search (max_search()'s locals)
+struct ConvState {
+    uint64_t perm, orb, order, leaves, nodes, order0;
+    unsigned n, valid, used, id_top, i, allrows;
+    uint64_t nmask1;
+    bool improved, timeout;
+};
+
+__device__ __forceinline__ void conv_start(ConvState &st, unsigned n, uint64_t order0) {
+    st.n = n;
+    st.allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
+    st.nmask1 = (n >= 16) ? NIB1 : (NIB1 & ((1ull << (4 * n)) - 1ull));
+    st.valid = n;
+    st.used = 0;
+    st.perm = 0;
+    st.orb = ID16;
+    st.order = 1;
+    st.id_top = 0;
+    st.i = 0;
+    st.leaves = 0;
+    st.nodes = 0;
+    st.order0 = order0;
+    st.improved = false;
+    st.timeout = false;
+}
+
+// Control steps from "choose the next child of the node at level st.i" until a node
+// is due for evaluation (returns true with ref_lv / ref_x set: ref_lv < 0 for none)
+// or the search is over (returns false).
+template <typename S>
+__device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsigned &ref_x) {
+    const unsigned n = st.n;
+    for (;;) {
+        const bool pr = !st.improved;
+        unsigned i = st.i;
+        unsigned rem = VD_(i);
+        if (pr && st.id_top >= i) {
+            // at an identity node only orbit leaders are branched on
+            while (rem && pg(st.orb, __ffs(rem) - 1) != (unsigned)(__ffs(rem) - 1))
+                rem &= rem - 1;
+        }
+        if (!rem) {
+            if (pr && st.id_top >= i) {
+                unsigned len = 0;
+                for (unsigned q = i; q < n; ++q)
+                    len += pg(st.orb, q) == i;
+                st.order *= len;
+            }
+            if (i == 0)
+                return false;
+            --i;
+            st.used &= ~(1u << pg(st.perm, i));
+            if (st.id_top > i)
+                st.id_top = i;
+            st.i = i;
+            continue;
+        }
+        unsigned x = __ffs(rem) - 1;
+        if (i == 0 && st.order0 != ID16 && !(pr && (rem & 1u))) {
+            for (unsigned q = 0; q < n; ++q) {
+                const unsigned c = pg(st.order0, q);
+                if ((rem >> c) & 1u) {
+                    x = c;
+                    break;
+                }
+            }
+        }
+        VD_(i) = (uint16_t)(rem & ~(1u << x));
+        st.perm = ps(st.perm, i, x);
+        st.used |= 1u << x;
+        if (st.id_top == i && x == i)
+            st.id_top = i + 1;
+        if (i + 1 < n) {
+            ref_lv = (int)i;
+            ref_x = x;
+            st.i = i + 1;
+            return true;
+        }
+        // a leaf
+        if (pr && st.id_top < n) {
+            // an automorphism moving row id_top: merge its orbits and go back to the
+            // identity node it branched from
+            st.orb = merge_orbits(st.perm, st.orb, n, st.id_top, st.nmask1);
+            st.i = st.id_top;
+            st.used = (1u << st.i) - 1u;
+            continue;
+        }
+        ++st.leaves;
+        st.used &= ~(1u << pg(st.perm, i));
+        if (st.id_top > i)
+            st.id_top = i;
+        st.i = i;
+    }
+}
+
+// After the node at level st.i was evaluated: prune, or raise the bound and keep
+// the children.  Returns false when the search is over (only at the root).
+template <typename S>
+__device__ __forceinline__ bool conv_after_eval(S sm, ConvState &st, int state, unsigned tied, uint64_t arr,
+                                                unsigned b) {
+    const unsigned i = st.i;
+    if (state == 2) {
+        // smaller than the bound: every extension is smaller too
+        if (i == 0)
+            return false;
+        st.i = i - 1;
+        st.used &= ~(1u << pg(st.perm, i - 1));
+        if (st.id_top > i - 1)
+            st.id_top = i - 1;
+        return true;
+    }
+    if (state == 1 || i >= st.valid) {
+        if (state == 1) {
+            st.improved = true;
+            st.leaves = 0;
+        }
+        const uint64_t cols = (1ull << b) - 1ull;
+        R_(i) = arr;
+        L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
+        st.valid = i + 1;
+    }
+    VD_(i) = (uint16_t)tied;
+    return true;
+}
+
+// |Aut| (the number of labelings reaching the canonical form) once the search is over
+__device__ __forceinline__ uint64_t conv_leaves(const ConvState &st) { return st.improved ? st.leaves : st.order; }
+
+}  // namespace
+}  // namespace bibd
+}  // namespace canon

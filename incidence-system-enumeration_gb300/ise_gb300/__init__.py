@@ -109,10 +109,11 @@ DESIGN_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint
 
 
 class TuneResult(ctypes.Structure):
-    _fields_ = [("variant", ctypes.c_int), ("ms", ctypes.c_float * 3)]
+    _fields_ = [("variant", ctypes.c_int), ("ms", ctypes.c_float * 4)]
 
 
-VARIANT_SINGLE, VARIANT_TWO_PASS, VARIANT_SPLIT = 0, 1, 2
+VARIANT_SINGLE, VARIANT_TWO_PASS, VARIANT_SPLIT, VARIANT_CONVERGED = 0, 1, 2, 3
+VARIANT_NAMES = ["one pass", "two passes", "split by first row", "two passes, converged lex-max pass"]
 
 
 class MlpWeights(ctypes.Structure):

@@ -193,15 +193,19 @@ int canon_check_bibd_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, 
  *   CANON_VARIANT_TWO_PASS lex-max pass for all, witness pass for the rejected
  *                          (not with CANON_SAVE_AUTS / CANON_REFERENCE_ORDER);
  *   CANON_VARIANT_SPLIT    the lex-max search split over one thread per (matrix,
- *                          first row) (CANON_VERDICT_ONLY without |Aut| flags).
+ *                          first row) (CANON_VERDICT_ONLY without |Aut| flags);
+ *   CANON_VARIANT_CONVERGED two passes, the lex-max pass laid out so that the
+ *                          threads of a warp evaluate their nodes together (one
+ *                          pass over all columns per node and thread).
  * ms[i]: the variant's device time, -1 when it does not apply, -2 when its
  * outputs differed (never chosen). */
-#define CANON_VARIANT_SINGLE   0
-#define CANON_VARIANT_TWO_PASS 1
-#define CANON_VARIANT_SPLIT    2
+#define CANON_VARIANT_SINGLE    0
+#define CANON_VARIANT_TWO_PASS  1
+#define CANON_VARIANT_SPLIT     2
+#define CANON_VARIANT_CONVERGED 3
 typedef struct {
     int   variant;      /* the variant kept */
-    float ms[3];
+    float ms[4];
 } canon_tune_result;
 int canon_tune_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
                     canon_tune_result *out);

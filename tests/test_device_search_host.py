@@ -11,6 +11,8 @@ import cases
 import conftest
 import oracle
 
+import ise_gb300 as G
+
 SRC = os.path.join(conftest.REPO, "tests", "host_build", "canon_bibd_host.cpp")
 OUT = os.path.join(conftest.REPO, "tests", "host_build", "_build", "libcanon_bibd_host.so")
 CUDA_INC = "/usr/local/cuda/include"
@@ -265,3 +267,45 @@ def test_search_split_by_first_row_combines_to_the_whole(host):
         assert imp == full["improved"]
         if not imp:
             assert aut == full["aut"]
+
+
+def _conv_vs_max(L, rows, n, b, order0=0xFEDCBA9876543210):
+    u64 = ctypes.c_uint64
+    res = []
+    for fn in (L.emu_conv_search, L.emu_maxsearch_order):
+        leaves, nodes, imp = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint8()
+        rc = fn(rows.ctypes.data_as(ctypes.POINTER(u64)), n, b, ctypes.c_uint64(order0), ctypes.byref(leaves),
+                ctypes.byref(nodes), ctypes.byref(imp))
+        assert rc == 0
+        res.append((leaves.value, nodes.value, imp.value))
+    return res
+
+
+def test_converged_layout_walks_the_same_tree(host):
+    """The converged search (canon_bibd_conv.cuh) visits exactly the nodes of
+    max_search() and gives the same verdict and |Aut|, in the plain order and under a
+    first-row order, on complete and partial matrices of several shapes."""
+    rng = np.random.default_rng(77)
+    cases_ = [np.stack([oracle.sts_random_rows(15, 99, i) for i in range(40)])]
+    sts = cases.load_sts15()
+    cases_.append(np.stack([G.pack_rows(M) for M, _ in sts]))
+    for rows in cases_:
+        for r in rows:
+            r = np.ascontiguousarray(r, np.uint64)
+            a, m = _conv_vs_max(host, r, 15, 35)
+            assert a == m
+            order = rng.permutation(15)
+            o0 = sum(int(x) << (4 * q) for q, x in enumerate(order))
+            a, m = _conv_vs_max(host, r, 15, 35, o0)
+            assert a == m
+            for k in (5, 9, 12):
+                p = np.ascontiguousarray(r[:k])
+                a, m = _conv_vs_max(host, p, k, 35)
+                assert a == m
+    for params in ((8, 14, 7, 4, 3), (11, 11, 5, 5, 2), (13, 26, 6, 3, 1), (7, 14, 6, 3, 2)):
+        for M, _ in cases.bibd_designs(*params):
+            X = cases.permute_normalize(M, rng)
+            r = np.ascontiguousarray(G.pack_rows(X), np.uint64)
+            for k in range(2, params[0] + 1):
+                a, m = _conv_vs_max(host, np.ascontiguousarray(r[:k]), k, params[1])
+                assert a == m, (params, k)
