@@ -228,7 +228,89 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.i, b, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        const int state = eval_node_uniform(sm, st.i, b, b, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        if (!conv_after_eval(sm, st, state, tied, arr, b))
+            finish(0);
+    }
+}
+
+// The lex-max pass over work items (the batched path: canon_sync, and the check
+// without allocation) in the converged layout.  Items may differ in rows and
+// columns; every lane walks bt columns (the widest item of the launch), the
+// columns past an item's own being empty.
+template <int BCAP, int VCAP>
+__global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__restrict__ items, uint32_t n_items,
+                                                              const uint64_t *__restrict__ words, Outputs out,
+                                                              uint64_t max_nodes, unsigned *ticket, uint32_t bt) {
+    __shared__ uint64_t s_rows[VCAP * TPB];
+    __shared__ uint64_t s_lvl[(VCAP + 1) * TPB];
+    __shared__ uint16_t s_vd[VCAP * TPB];
+    __shared__ uint16_t s_cm[BCAP * TPB];
+    const unsigned tid = threadIdx.x;
+    SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    ConvState st{};
+    uint32_t o_i = 0;
+    unsigned b = 1;
+    bool have = false, done = false;
+    auto finish = [&](uint8_t stat) {
+        const bool can = !stat && !st.improved;
+        out.canonical[o_i] = can ? 1 : 0;
+        out.status[o_i] = stat;
+        out.aut[2 * (size_t)o_i] = stat ? 0 : conv_leaves(st);
+        out.aut[2 * (size_t)o_i + 1] = 0;
+        out.player_index[o_i] = -1;
+        out.n_auts[o_i] = 0;
+        out.len_aut[o_i] = 0;
+        have = false;
+    };
+    for (;;) {
+        int ref_lv = -1;
+        unsigned ref_x = 0;
+        bool eval = false;
+        while (!done && !eval) {
+            if (!have) {
+                const unsigned it = atomicAdd(ticket, 1u);
+                if (it >= n_items) {
+                    done = true;
+                    break;
+                }
+                const Item item = items[it];
+                const unsigned n = item.nrows;
+                b = item.ncols;
+                o_i = item.out_idx;
+                conv_start(st, n >= 1 && n <= VCAP ? n : 1, ID16);
+                have = true;
+                if (item.kind != KIND_BIBD || n < 1 || n > VCAP || b < 1 || b > BMAX || b > BCAP || b > bt ||
+                    !load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW)) {
+                    finish(ST_BADINPUT);
+                    continue;
+                }
+                for (unsigned c = b; c < bt; ++c)
+                    CM_(c) = 0;
+                eval = true;
+                break;
+            }
+            if (conv_next(sm, st, ref_lv, ref_x)) {
+                eval = true;
+                break;
+            }
+            finish(0);
+        }
+        if (__all_sync(0xFFFFFFFFu, done))
+            break;
+        if (!eval)
+            continue;
+        if (ref_lv >= 0)
+            refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
+        if (++st.nodes > max_nodes) {
+            st.timeout = true;
+            finish(ST_TIMEOUT);
+            continue;
+        }
+        unsigned tied = st.allrows & ~st.used;
+        uint64_t arr = 0;
+        const bool hb = st.i < st.valid;
+        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }
@@ -545,17 +627,19 @@ cudaError_t launch_bibd_check_two_pass(const Item *d_items, uint32_t n_items, co
     CANON_TRY(cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s));
     const int need = (int)((n_items + TPB - 1) / TPB);
     const int shape = (max_v <= 15 && max_b <= 35) ? 0 : (max_b <= 40 ? 1 : 2);
-    const void *kfn = shape == 0 ? (const void *)bibd_items_max_kernel<35, 15>
-                      : shape == 1 ? (const void *)bibd_items_max_kernel<40, 16>
-                                   : (const void *)bibd_items_max_kernel<64, 16>;
+    const uint32_t bt = max_b < 1 ? 1 : (max_b > BMAX ? BMAX : max_b);
+    // the lex-max pass in the converged layout (every lane walks the widest item's columns)
+    const void *kfn = shape == 0 ? (const void *)bibd_items_conv_kernel<35, 15>
+                      : shape == 1 ? (const void *)bibd_items_conv_kernel<40, 16>
+                                   : (const void *)bibd_items_conv_kernel<64, 16>;
     int grid = 0;
     CANON_TRY(grid_for(kfn, num_sms, need, &grid));
     if (shape == 0)
-        bibd_items_max_kernel<35, 15><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+        bibd_items_conv_kernel<35, 15><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk, bt);
     else if (shape == 1)
-        bibd_items_max_kernel<40, 16><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+        bibd_items_conv_kernel<40, 16><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk, bt);
     else
-        bibd_items_max_kernel<64, 16><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk);
+        bibd_items_conv_kernel<64, 16><<<grid, TPB, 0, s>>>(d_items, n_items, d_words, out, max_trials, tk, bt);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
@@ -576,7 +660,9 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
     const bool ref_order = flags & (F_SAVE_AUTS | F_REFERENCE_ORDER);
     const bool two = !ref_order && (variant < 0 ? (flags & (F_AUT_CANON | F_FULL_AUT)) != 0
                                                 : (variant == VARIANT_TWO_PASS || variant == VARIANT_CONVERGED));
-    const bool conv = variant == VARIANT_CONVERGED;
+    // the converged layout of the lex-max pass by default; the original one only when
+    // the autotuner asks for it by name
+    const bool conv = variant != VARIANT_TWO_PASS;
     if (two) {
         // |Aut| wanted for every matrix: two passes, the lex-max search for all,
         // the reference-order witness for the rejected ones.  (Without it the

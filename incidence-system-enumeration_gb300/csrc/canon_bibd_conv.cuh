@@ -32,19 +32,23 @@ namespace bibd {
 namespace {
 
 // the greatest arranged row over `tied` at level lv, compared with `bound`:
-// 0 equal so far, 1 greater, 2 smaller (have_bound false: never compared, 0)
+// 0 equal so far, 1 greater, 2 smaller (have_bound false: never compared, 0).
+// b: the matrix's columns; bt >= b: the columns every lane of the launch walks (the
+// widest matrix of a mixed launch).  Columns b..bt-1 hold no 1 (CM_() is 0 there)
+// and each closes an orbit of its own, so they change neither the row nor the
+// comparison.
 template <typename S>
-__device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned &tied, uint64_t &arr,
-                                                 bool have_bound, uint64_t bound) {
+__device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned bt, unsigned &tied,
+                                                 uint64_t &arr, bool have_bound, uint64_t bound) {
     const uint64_t lvl = L_(lv);
     // bit p: column p closes an orbit (the next column starts one, or p is the last)
-    const uint64_t ends = (lvl >> 1) | (1ull << (b - 1));
+    const uint64_t ends = (lvl >> 1) | (~0ull << (b - 1));
     unsigned t0 = tied;
     uint64_t a = 0;
     int state = 0;
     unsigned p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
     unsigned s = 0;
-    for (unsigned p = 0; p < b; ++p) {
+    for (unsigned p = 0; p < bt; ++p) {
         unsigned carry = (unsigned)CM_(p) & t0, t;
         t = p0 & carry; p0 ^= carry; carry = t;
         t = p1 & carry; p1 ^= carry; carry = t;
@@ -76,12 +80,13 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
 }
 
 // the columns of level lv+1 after row x was taken at level lv: inside every orbit of
-// level lv, the columns with a 1 in row x first (one pass, a write pointer per orbit)
+// level lv, the columns with a 1 in row x first (one pass, a write pointer per orbit);
+// bt: the columns walked (columns past the matrix's own hold no 1 and never move)
 template <typename S>
-__device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, unsigned b) {
+__device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, unsigned bt) {
     const uint64_t starts = L_(lv);
     unsigned w = 0;
-    for (unsigned p = 0; p < b; ++p) {
+    for (unsigned p = 0; p < bt; ++p) {
         if ((starts >> p) & 1u)
             w = p;
         const uint16_t c = CM_(p);

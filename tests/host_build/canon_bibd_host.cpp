@@ -87,27 +87,30 @@ extern "C" int emu_maxsearch_root2(const uint64_t *rows, unsigned n, unsigned b,
 // The converged layout of the same search (canon_bibd_conv.cuh), one lane: control
 // steps until a node is due, then the node step, as bibd_conv_kernel runs them.
 #include "../../incidence-system-enumeration_gb300/csrc/canon_bibd_conv.cuh"
-extern "C" int emu_conv_search(const uint64_t *rows, unsigned n, unsigned b, uint64_t order0, uint64_t *leaves,
-                               uint64_t *nodes, uint8_t *improved) {
+// bt >= b: the columns walked (a mixed launch walks its widest item's columns)
+extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, unsigned bt, uint64_t order0,
+                                  uint64_t *leaves, uint64_t *nodes, uint8_t *improved) {
     static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
     static uint16_t s_vd[VMAX * TPB];
     static uint16_t s_cm[64 * TPB];
     SmemMax sm{s_rows, s_lvl, nullptr, s_cm, s_vd};
     if (!load_rows(sm, rows, n, b, F_RAW))
         return -1;
+    for (unsigned c = b; c < bt; ++c)
+        CM_(c) = 0;
     ConvState st;
     conv_start(st, n, order0);
     int ref_lv = -1;
     unsigned ref_x = 0;
     for (;;) {
         if (ref_lv >= 0)
-            refine_uniform(sm, (unsigned)ref_lv, ref_x, b);
+            refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
         if (++st.nodes > (1ull << 30))
             return -2;
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.i, b, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             break;
         if (!conv_next(sm, st, ref_lv, ref_x))
@@ -117,6 +120,11 @@ extern "C" int emu_conv_search(const uint64_t *rows, unsigned n, unsigned b, uin
     *nodes = st.nodes;
     *improved = st.improved;
     return 0;
+}
+
+extern "C" int emu_conv_search(const uint64_t *rows, unsigned n, unsigned b, uint64_t order0, uint64_t *leaves,
+                               uint64_t *nodes, uint8_t *improved) {
+    return emu_conv_search_bt(rows, n, b, b, order0, leaves, nodes, improved);
 }
 
 // max_search() with a first-row order (the learned order's effect on the search)

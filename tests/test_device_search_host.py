@@ -302,10 +302,19 @@ def test_converged_layout_walks_the_same_tree(host):
                 p = np.ascontiguousarray(r[:k])
                 a, m = _conv_vs_max(host, p, k, 35)
                 assert a == m
+    u64 = ctypes.c_uint64
     for params in ((8, 14, 7, 4, 3), (11, 11, 5, 5, 2), (13, 26, 6, 3, 1), (7, 14, 6, 3, 2)):
         for M, _ in cases.bibd_designs(*params):
             X = cases.permute_normalize(M, rng)
             r = np.ascontiguousarray(G.pack_rows(X), np.uint64)
             for k in range(2, params[0] + 1):
-                a, m = _conv_vs_max(host, np.ascontiguousarray(r[:k]), k, params[1])
+                p = np.ascontiguousarray(r[:k])
+                a, m = _conv_vs_max(host, p, k, params[1])
                 assert a == m, (params, k)
+                # walking more columns than the matrix has (the widest item of a mixed
+                # launch) changes nothing
+                leaves, nodes, imp = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint8()
+                assert host.emu_conv_search_bt(p.ctypes.data_as(ctypes.POINTER(u64)), k, params[1], 35,
+                                               ctypes.c_uint64(0xFEDCBA9876543210), ctypes.byref(leaves),
+                                               ctypes.byref(nodes), ctypes.byref(imp)) == 0
+                assert (leaves.value, nodes.value, imp.value) == a, (params, k)
