@@ -161,13 +161,12 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
                                                         uint64_t *aut, uint8_t *status, uint64_t max_nodes,
                                                         unsigned *ticket, const uint64_t *__restrict__ orders,
                                                         uint64_t *nodes_out) {
-    // no per-level words: the converged search keeps the current level's orbit starts
-    // in a register (218 B of shared memory per thread for v <= 15, b <= 35)
     __shared__ uint64_t s_rows[VCAP * TPB];
+    __shared__ uint64_t s_lvl[(VCAP + 1) * TPB];
     __shared__ uint16_t s_vd[VCAP * TPB];
     __shared__ uint16_t s_cm[BCAP * TPB];
     const unsigned tid = threadIdx.x;
-    SmemMax sm{s_rows + tid, nullptr, nullptr, s_cm + tid, s_vd + tid};
+    SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
     const bool want_aut = flags & (F_AUT_CANON | F_FULL_AUT);
     ConvState st{};
     uint32_t it = 0;
@@ -191,7 +190,6 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
         // control steps until this thread has a node to evaluate, or no work is left
         int ref_lv = -1;
         unsigned ref_x = 0;
-        uint64_t ref_starts = 0;
         bool eval = false;
         while (!done && !eval) {
             if (!have) {
@@ -200,16 +198,16 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
                     done = true;
                     break;
                 }
-                conv_start(st, v, b, orders ? orders[it] : ID16);
+                conv_start(st, v, orders ? orders[it] : ID16);
                 have = true;
-                if (!conv_load(sm, rows + (size_t)it * v, v, b, flags & F_RAW)) {
+                if (!load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW)) {
                     finish(ST_BADINPUT);
                     continue;
                 }
                 eval = true;        // the root: no arrangement step
                 break;
             }
-            if (conv_next(sm, st, ref_lv, ref_x, ref_starts)) {
+            if (conv_next(sm, st, ref_lv, ref_x)) {
                 eval = true;
                 break;
             }
@@ -221,7 +219,7 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
             continue;
         // the node step: every lane with a node runs the same b-column passes
         if (ref_lv >= 0)
-            refine_uniform(sm, ref_starts, ref_x, b);
+            refine_uniform(sm, (unsigned)ref_lv, ref_x, b);
         if (++st.nodes > max_nodes) {
             st.timeout = true;
             finish(ST_TIMEOUT);
@@ -230,8 +228,8 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.lcur, b, b, tied, arr, hb, hb ? R_(st.i) : 0ull);
-        if (!conv_after_eval(sm, st, state, tied, arr))
+        const int state = eval_node_uniform(sm, st.i, b, b, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }
 }
@@ -245,10 +243,11 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
                                                               const uint64_t *__restrict__ words, Outputs out,
                                                               uint64_t max_nodes, unsigned *ticket, uint32_t bt) {
     __shared__ uint64_t s_rows[VCAP * TPB];
+    __shared__ uint64_t s_lvl[(VCAP + 1) * TPB];
     __shared__ uint16_t s_vd[VCAP * TPB];
     __shared__ uint16_t s_cm[BCAP * TPB];
     const unsigned tid = threadIdx.x;
-    SmemMax sm{s_rows + tid, nullptr, nullptr, s_cm + tid, s_vd + tid};
+    SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
     ConvState st{};
     uint32_t o_i = 0;
     unsigned b = 1;
@@ -267,7 +266,6 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
     for (;;) {
         int ref_lv = -1;
         unsigned ref_x = 0;
-        uint64_t ref_starts = 0;
         bool eval = false;
         while (!done && !eval) {
             if (!have) {
@@ -280,11 +278,10 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
                 const unsigned n = item.nrows;
                 b = item.ncols;
                 o_i = item.out_idx;
-                const bool shape_ok = item.kind == KIND_BIBD && n >= 1 && n <= VCAP && b >= 1 && b <= BMAX &&
-                                      b <= BCAP && b <= bt;
-                conv_start(st, shape_ok ? n : 1, shape_ok ? b : 1, ID16);
+                conv_start(st, n >= 1 && n <= VCAP ? n : 1, ID16);
                 have = true;
-                if (!shape_ok || !conv_load(sm, words + item.data_off, n, b, item.flags & F_RAW)) {
+                if (item.kind != KIND_BIBD || n < 1 || n > VCAP || b < 1 || b > BMAX || b > BCAP || b > bt ||
+                    !load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW)) {
                     finish(ST_BADINPUT);
                     continue;
                 }
@@ -293,7 +290,7 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
                 eval = true;
                 break;
             }
-            if (conv_next(sm, st, ref_lv, ref_x, ref_starts)) {
+            if (conv_next(sm, st, ref_lv, ref_x)) {
                 eval = true;
                 break;
             }
@@ -304,7 +301,7 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
         if (!eval)
             continue;
         if (ref_lv >= 0)
-            refine_uniform(sm, ref_starts, ref_x, bt);
+            refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
         if (++st.nodes > max_nodes) {
             st.timeout = true;
             finish(ST_TIMEOUT);
@@ -313,8 +310,8 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.lcur, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
-        if (!conv_after_eval(sm, st, state, tied, arr))
+        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }
 }

@@ -38,9 +38,9 @@ namespace {
 // and each closes an orbit of its own, so they change neither the row nor the
 // comparison.
 template <typename S>
-__device__ __forceinline__ int eval_node_uniform(S sm, uint64_t lvl, unsigned b, unsigned bt, unsigned &tied,
+__device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned bt, unsigned &tied,
                                                  uint64_t &arr, bool have_bound, uint64_t bound) {
-    // lvl: the orbit-start columns of the node's level
+    const uint64_t lvl = L_(lv);
     // bit p: column p closes an orbit (the next column starts one, or p is the last)
     const uint64_t ends = (lvl >> 1) | (~0ull << (b - 1));
     unsigned t0 = tied;
@@ -83,8 +83,8 @@ __device__ __forceinline__ int eval_node_uniform(S sm, uint64_t lvl, unsigned b,
 // level lv, the columns with a 1 in row x first (one pass, a write pointer per orbit);
 // bt: the columns walked (columns past the matrix's own hold no 1 and never move)
 template <typename S>
-__device__ __forceinline__ void refine_uniform(S sm, uint64_t starts, unsigned x, unsigned bt) {
-    // starts: the orbit-start columns of the parent's level
+__device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, unsigned bt) {
+    const uint64_t starts = L_(lv);
     unsigned w = 0;
     for (unsigned p = 0; p < bt; ++p) {
         if ((starts >> p) & 1u)
@@ -98,34 +98,15 @@ __device__ __forceinline__ void refine_uniform(S sm, uint64_t starts, unsigned x
     }
 }
 
-// the per-thread state of one lex-max search (max_search()'s locals).  The orbit
-// starts of the current level live in a register (lcur) rather than one word per
-// level in shared memory: a level's starts follow from the bound's rows above it,
-// so they are extended on the way down and rebuilt on the way up.
+// the per-thread state of one lex-max search (max_search()'s locals)
 struct ConvState {
     uint64_t perm, orb, order, leaves, nodes, order0;
-    uint64_t lcur, cols;
     unsigned n, valid, used, id_top, i, allrows;
     uint64_t nmask1;
     bool improved, timeout;
 };
 
-// orbit starts of level lv: column 0, and every column where one of the bound's rows
-// 0..lv-1 changes from 1 to 0 (an orbit of a level is a run of columns equal in the
-// rows above it; the rows are 1s-first inside the orbits above them)
-template <typename S>
-__device__ __forceinline__ uint64_t level_starts(S sm, const ConvState &st, unsigned lv) {
-    uint64_t m = 1ull;
-    for (unsigned r = 0; r < lv; ++r) {
-        const uint64_t x = R_(r);
-        m |= (x ^ (x << 1)) & st.cols & ~1ull;
-    }
-    return m;
-}
-
-__device__ __forceinline__ void conv_start(ConvState &st, unsigned n, unsigned b, uint64_t order0) {
-    st.lcur = 1ull;
-    st.cols = (1ull << b) - 1ull;
+__device__ __forceinline__ void conv_start(ConvState &st, unsigned n, uint64_t order0) {
     st.n = n;
     st.allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     st.nmask1 = (n >= 16) ? NIB1 : (NIB1 & ((1ull << (4 * n)) - 1ull));
@@ -147,7 +128,7 @@ __device__ __forceinline__ void conv_start(ConvState &st, unsigned n, unsigned b
 // is due for evaluation (returns true with ref_lv / ref_x set: ref_lv < 0 for none)
 // or the search is over (returns false).
 template <typename S>
-__device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsigned &ref_x, uint64_t &ref_starts) {
+__device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsigned &ref_x) {
     const unsigned n = st.n;
     for (;;) {
         const bool pr = !st.improved;
@@ -172,7 +153,6 @@ __device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsi
             if (st.id_top > i)
                 st.id_top = i;
             st.i = i;
-            st.lcur = level_starts(sm, st, i);
             continue;
         }
         unsigned x = __ffs(rem) - 1;
@@ -193,9 +173,6 @@ __device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsi
         if (i + 1 < n) {
             ref_lv = (int)i;
             ref_x = x;
-            ref_starts = st.lcur;
-            const uint64_t row = R_(i);
-            st.lcur |= (row ^ (row << 1)) & st.cols & ~1ull;
             st.i = i + 1;
             return true;
         }
@@ -206,7 +183,6 @@ __device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsi
             st.orb = merge_orbits(st.perm, st.orb, n, st.id_top, st.nmask1);
             st.i = st.id_top;
             st.used = (1u << st.i) - 1u;
-            st.lcur = level_starts(sm, st, st.i);
             continue;
         }
         ++st.leaves;
@@ -220,7 +196,8 @@ __device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsi
 // After the node at level st.i was evaluated: prune, or raise the bound and keep
 // the children.  Returns false when the search is over (only at the root).
 template <typename S>
-__device__ __forceinline__ bool conv_after_eval(S sm, ConvState &st, int state, unsigned tied, uint64_t arr) {
+__device__ __forceinline__ bool conv_after_eval(S sm, ConvState &st, int state, unsigned tied, uint64_t arr,
+                                                unsigned b) {
     const unsigned i = st.i;
     if (state == 2) {
         // smaller than the bound: every extension is smaller too
@@ -230,7 +207,6 @@ __device__ __forceinline__ bool conv_after_eval(S sm, ConvState &st, int state, 
         st.used &= ~(1u << pg(st.perm, i - 1));
         if (st.id_top > i - 1)
             st.id_top = i - 1;
-        st.lcur = level_starts(sm, st, i - 1);
         return true;
     }
     if (state == 1 || i >= st.valid) {
@@ -238,69 +214,13 @@ __device__ __forceinline__ bool conv_after_eval(S sm, ConvState &st, int state, 
             st.improved = true;
             st.leaves = 0;
         }
+        const uint64_t cols = (1ull << b) - 1ull;
         R_(i) = arr;
+        L_(i + 1) = L_(i) | ((arr ^ (arr << 1)) & cols & ~1ull);
         st.valid = i + 1;
     }
     VD_(i) = (uint16_t)tied;
     return true;
-}
-
-// The rows of one matrix into shared memory for the converged search: the bound's rows
-// and the column masks, no per-level words.  raw: bring the columns into orbit normal
-// form first (as normalize_columns(), with the column codes kept in the column-mask
-// area); returns false if a row is not 1s-first inside the orbits of the rows above.
-template <typename S>
-__device__ __forceinline__ bool conv_load(S sm, const uint64_t *src, unsigned n, unsigned b, bool raw) {
-    for (unsigned r = 0; r < n; ++r)
-        R_(r) = src[r];
-    if (raw) {
-        // the pattern of each column read from row 0 down; columns sorted by decreasing
-        // pattern (ties in column order)
-        for (unsigned c = 0; c < b; ++c) {
-            unsigned code = 0;
-            for (unsigned r = 0; r < n; ++r)
-                code = (code << 1) | (unsigned)((R_(r) >> c) & 1u);
-            CM_(c) = (uint16_t)code;
-        }
-        uint64_t acc[VMAX];
-#pragma unroll
-        for (unsigned r = 0; r < VMAX; ++r)
-            acc[r] = 0;
-        for (unsigned c = 0; c < b; ++c) {
-            const unsigned kc = CM_(c);
-            unsigned rank = 0;
-            for (unsigned c2 = 0; c2 < b; ++c2) {
-                const unsigned k2 = CM_(c2);
-                rank += (k2 > kc) || (k2 == kc && c2 < c);
-            }
-#pragma unroll
-            for (unsigned r = 0; r < VMAX; ++r)
-                if (r < n)
-                    acc[r] |= (uint64_t)((kc >> (n - 1 - r)) & 1u) << rank;
-        }
-#pragma unroll
-        for (unsigned r = 0; r < VMAX; ++r)
-            if (r < n)
-                R_(r) = acc[r];
-    }
-    const uint64_t cols = (1ull << b) - 1ull;
-    uint64_t m = 1ull;
-    bool ok = true;
-    for (unsigned r = 0; r < n; ++r) {
-        const uint64_t x = R_(r);
-        if (x & ~cols)
-            ok = false;
-        if (x & ~(x << 1) & ~m & cols & ~1ull)
-            ok = false;
-        m |= (x ^ (x << 1)) & cols & ~1ull;
-    }
-    for (unsigned c = 0; c < b; ++c) {
-        unsigned col = 0;
-        for (unsigned r = 0; r < n; ++r)
-            col |= (unsigned)((R_(r) >> c) & 1u) << r;
-        CM_(c) = (uint16_t)col;
-    }
-    return ok;
 }
 
 // |Aut| (the number of labelings reaching the canonical form) once the search is over

@@ -90,31 +90,30 @@ extern "C" int emu_maxsearch_root2(const uint64_t *rows, unsigned n, unsigned b,
 // bt >= b: the columns walked (a mixed launch walks its widest item's columns)
 extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, unsigned bt, uint64_t order0,
                                   uint64_t *leaves, uint64_t *nodes, uint8_t *improved) {
-    static uint64_t s_rows[VMAX * TPB];
+    static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
     static uint16_t s_vd[VMAX * TPB];
     static uint16_t s_cm[64 * TPB];
-    SmemMax sm{s_rows, nullptr, nullptr, s_cm, s_vd};
-    if (!conv_load(sm, rows, n, b, true))
+    SmemMax sm{s_rows, s_lvl, nullptr, s_cm, s_vd};
+    if (!load_rows(sm, rows, n, b, F_RAW))
         return -1;
     for (unsigned c = b; c < bt; ++c)
         CM_(c) = 0;
     ConvState st;
-    conv_start(st, n, b, order0);
+    conv_start(st, n, order0);
     int ref_lv = -1;
     unsigned ref_x = 0;
-    uint64_t ref_starts = 0;
     for (;;) {
         if (ref_lv >= 0)
-            refine_uniform(sm, ref_starts, ref_x, bt);
+            refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
         if (++st.nodes > (1ull << 30))
             return -2;
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.lcur, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
-        if (!conv_after_eval(sm, st, state, tied, arr))
+        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        if (!conv_after_eval(sm, st, state, tied, arr, b))
             break;
-        if (!conv_next(sm, st, ref_lv, ref_x, ref_starts))
+        if (!conv_next(sm, st, ref_lv, ref_x))
             break;
     }
     *leaves = conv_leaves(st);
