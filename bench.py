@@ -392,7 +392,7 @@ def run_enum(args):
             found, st = ctx.enumerate_ksys(*params)
         runs.append((len(found), st.checks, st.seconds, st.kernel_ms, st.batches,
                      [int(x) for x in st.level_checks], [round(float(x), 3) for x in st.level_kernel_ms],
-                     st.gen_seconds))
+                     st.gen_seconds, int(st.trials)))
     timed = runs[args.warmup:]
     secs = sum(r[2] for r in timed)
     checks = sum(r[1] for r in timed)
@@ -420,6 +420,9 @@ def run_enum(args):
             "checks_per_s": checks / secs, "kernel_ms_per_step": sum(r[3] for r in timed) / args.steps,
             "gen_ms_per_step": 1e3 * sum(r[7] for r in timed) / args.steps,
             "cpu_baseline": cpu}
+    if kind == "ksys":
+        # relabelings the checks tried (cnvCheckNew candidates), the k-system check's unit of work
+        line["relabelings_tried_per_step"] = timed[0][8]
     print(json.dumps(line), flush=True)
     ctx.close()
 

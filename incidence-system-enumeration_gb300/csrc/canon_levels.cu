@@ -34,6 +34,7 @@
 #include "canon_ctx.h"
 #include "canon_internal.h"
 #include "canon_rows.cuh"
+#include "canon_ksys_rounds.cuh"
 
 namespace {
 
@@ -342,6 +343,63 @@ void parallel_ranges(uint64_t n, F fn) {
         x.join();
 }
 
+// ---- k-system rounds on the device ----------------------------------------
+__global__ void ksys_count_kernel(int np, const uint8_t *parents, uint32_t n_par, int d, uint32_t *counts) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_par; p += stride)
+        counts[p] = canon::ksys_children(np, parents + (size_t)p * d * np, d, nullptr);
+}
+
+// the children of parents [p0, p1) at offsets[p] - offsets[p0], and one work item each
+__global__ void ksys_emit_kernel(int np, const uint8_t *parents, uint32_t p0, uint32_t p1, int d,
+                                 const uint64_t *offsets, uint8_t *out, canon::Item *items) {
+    const uint64_t base = offsets[p0];
+    const uint32_t m = (uint32_t)d + 1;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += stride) {
+        const uint64_t o = offsets[p] - base;
+        const uint32_t cnt = canon::ksys_children(np, parents + (size_t)p * d * np, d, out + o * m * np);
+        for (uint32_t j = 0; j < cnt; ++j) {
+            canon::Item it{};
+            it.data_off = (uint32_t)((o + j) * m * np);
+            it.kind = canon::KIND_KSYS;
+            it.nrows = (uint8_t)m;
+            it.ncols = (uint8_t)np;
+            it.flags = 0;
+            it.out_idx = (uint32_t)(o + j);
+            items[o + j] = it;
+        }
+    }
+}
+
+// the canonical children of a slice into the next level, their |Aut| when complete,
+// and the relabelings tried (summed per block)
+__global__ void ksys_compact_kernel(uint64_t n_cand, uint32_t bytes, const uint8_t *cand, const uint8_t *canonical,
+                                    const uint8_t *status, const uint64_t *aut, const uint64_t *trials,
+                                    const uint64_t *offs, uint8_t *dst, uint64_t *aut_dst, unsigned *bad,
+                                    unsigned long long *trials_sum) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long tsum = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_cand; i += stride) {
+        tsum += trials[i];
+        if (status[i] & (canon::ST_TIMEOUT | canon::ST_BADINPUT))
+            atomicOr(bad, 1u);
+        if (!canonical[i])
+            continue;
+        const uint64_t o = offs[i];
+        for (uint32_t q = 0; q < bytes; ++q)
+            dst[o * bytes + q] = cand[i * bytes + q];
+        if (aut_dst) {
+            aut_dst[2 * o] = aut[2 * i];
+            aut_dst[2 * o + 1] = aut[2 * i + 1];
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        tsum += __shfl_down_sync(0xFFFFFFFFu, tsum, off);
+    if ((threadIdx.x & 31u) == 0 && tsum)
+        atomicAdd(trials_sum, tsum);
+}
+
 }  // namespace
 
 extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32_t r, uint32_t k, uint32_t lambda,
@@ -591,6 +649,224 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 cb(user, (const uint8_t *)(rows.data() + i * v), v, b, auts[2 * i], auts[2 * i + 1]);
     }
     st.seconds = since(t0);
+    if (stats)
+        *stats = st;
+    return done(CANON_OK, "", cudaSuccess);
+}
+
+// All 1-factorizations of K_np up to isomorphism, round by round with every level in
+// HBM: the next rounds of all canonical parents are generated on the GPU
+// (ksys_count_kernel, a scan, ksys_emit_kernel), checked there (the warp-per-matrix
+// cnvCheckNew() kernel), and the canonical ones compacted into the next level.  The
+// work of alldata::Run() for group size 2 with the check at every level
+// (k-Factorization/TripleSys/Source/TripleSys.cpp:80-775, check at
+// checkCurrentResult.cpp:91).
+extern "C" int canon_enumerate_ksys(canon_ctx *c, uint32_t np, canon_design_cb cb, void *user,
+                                    canon_enum_stats *stats) {
+    if (!c || np < 4 || np > (uint32_t)canon::KS_MAXNP || (np & 1u))
+        return CANON_EINVAL;
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaSetDevice(c->device);
+    cudaStream_t s = c->stream;
+    canon_enum_stats st{};
+    DevBuf<uint8_t> lev, next, cand, can, status, rrow, rtc, wit, len_aut;
+    DevBuf<uint64_t> doffs, coffs, sums, aut, aut_out, trials;
+    DevBuf<uint32_t> dcounts;
+    DevBuf<int32_t> pidx;
+    DevBuf<uint16_t> n_auts;
+    DevBuf<canon::Item> items;
+    DevBuf<unsigned> ticket;
+    DevBuf<unsigned long long> tsum;
+    cudaEvent_t e0 = nullptr, e1 = nullptr, g0 = nullptr, g1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventCreate(&g0);
+    cudaEventCreate(&g1);
+    auto done = [&](int rc, const char *what, cudaError_t e) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaEventDestroy(g0);
+        cudaEventDestroy(g1);
+        if (rc != CANON_OK)
+            c->err = std::string("enumerate k-systems: ") + what +
+                     (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e) : std::string());
+        return rc;
+    };
+    cudaError_t e = ticket.ensure(2);      // [0] work-stealing counter, [1] bad-status flag
+    if (e == cudaSuccess)
+        e = tsum.ensure(1);
+    if (e == cudaSuccess)
+        e = lev.ensure(np);
+    if (e != cudaSuccess)
+        return done(CANON_ENOMEM, "setup", e);
+    // level 1: round 0 = (0 1)(2 3)...
+    {
+        uint8_t r0[canon::KS_MAXNP];
+        for (uint32_t i = 0; i < np; ++i)
+            r0[i] = (uint8_t)i;
+        e = cudaMemcpyAsync(lev.p, r0, np, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(ticket.p + 1, 0, sizeof(unsigned), s);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(tsum.p, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess)
+            return done(CANON_ECUDA, "setup", e);
+    }
+    const uint32_t rounds = np - 1;
+    uint64_t n_par = 1;
+    uint32_t n = 1;
+    const int grid_cap = 4 * (c->num_sms > 0 ? c->num_sms : 1);
+    while (n < rounds && n_par) {
+        const uint32_t m = n + 1;
+        const bool complete = m == rounds;
+        // 1: children per parent and their offsets (on the GPU)
+        e = dcounts.ensure(n_par);
+        if (e == cudaSuccess)
+            e = doffs.ensure(n_par + 1);
+        if (e != cudaSuccess)
+            return done(CANON_ENOMEM, "level buffers", e);
+        int g = (int)((n_par + 127) / 128);
+        if (g > grid_cap)
+            g = grid_cap;
+        cudaEventRecord(g0, s);
+        ksys_count_kernel<<<g, 128, 0, s>>>((int)np, lev.p, (uint32_t)n_par, (int)n, dcounts.p);
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = exclusive_scan(dcounts.p, n_par, doffs.p, sums, s);
+        cudaEventRecord(g1, s);
+        std::vector<uint64_t> offs(n_par + 1);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(offs.data(), doffs.p, offs.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess)
+            return done(CANON_ECUDA, "count", e);
+        float gms = 0.f;
+        cudaEventElapsedTime(&gms, g0, g1);
+        st.gen_seconds += gms * 1e-3;
+        c->launches += 4;
+        const uint64_t n_cand = offs[n_par];
+        const size_t bytes = (size_t)m * np;
+        e = next.ensure((n_cand ? n_cand : 1) * bytes);
+        if (e == cudaSuccess && complete)
+            e = aut_out.ensure((size_t)(n_cand ? n_cand : 1) * 2);
+        if (e != cudaSuccess)
+            return done(CANON_ENOMEM, "next level", e);
+        uint64_t n_next = 0, p0 = 0;
+        while (p0 < n_par) {
+            uint64_t p1 = p0 + 1;
+            while (p1 < n_par && offs[p1 + 1] - offs[p0] <= SLICE_CAP)
+                ++p1;
+            const uint64_t ns = offs[p1] - offs[p0];
+            const size_t cap = ns ? ns : 1;
+            e = cand.ensure(cap * bytes);
+            if (e == cudaSuccess) e = items.ensure(cap);
+            if (e == cudaSuccess) e = can.ensure(cap);
+            if (e == cudaSuccess) e = status.ensure(cap);
+            if (e == cudaSuccess) e = rrow.ensure(cap);
+            if (e == cudaSuccess) e = rtc.ensure(cap);
+            if (e == cudaSuccess) e = pidx.ensure(cap);
+            if (e == cudaSuccess) e = wit.ensure(cap * 16);
+            if (e == cudaSuccess) e = aut.ensure(cap * 2);
+            if (e == cudaSuccess) e = trials.ensure(cap);
+            if (e == cudaSuccess) e = n_auts.ensure(cap);
+            if (e == cudaSuccess) e = len_aut.ensure(cap);
+            if (e == cudaSuccess) e = coffs.ensure(cap + 1);
+            if (e != cudaSuccess)
+                return done(CANON_ENOMEM, "slice buffers", e);
+            // 2: the children and their work items
+            int ge = (int)((p1 - p0 + 127) / 128);
+            if (ge > grid_cap)
+                ge = grid_cap;
+            cudaEventRecord(g0, s);
+            ksys_emit_kernel<<<ge, 128, 0, s>>>((int)np, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, doffs.p, cand.p,
+                                                items.p);
+            cudaEventRecord(g1, s);
+            e = cudaGetLastError();
+            // 3: the verdicts
+            canon::Outputs o{};
+            o.canonical = can.p;
+            o.status = status.p;
+            o.reject_row = rrow.p;
+            o.row_to_change = rtc.p;
+            o.player_index = pidx.p;
+            o.witness = wit.p;
+            o.aut = aut.p;
+            o.trials = trials.p;
+            o.n_auts = n_auts.p;
+            o.len_aut = len_aut.p;
+            o.auts = nullptr;
+            o.aut_cap = 0;
+            cudaEventRecord(e0, s);
+            if (e == cudaSuccess)
+                e = canon::launch_ksys_check(items.p, (uint32_t)ns, cand.p, o, ticket.p, c->num_sms, s);
+            cudaEventRecord(e1, s);
+            // 4: the canonical ones into the next level
+            if (e == cudaSuccess)
+                e = exclusive_scan(can.p, ns, coffs.p, sums, s);
+            if (e == cudaSuccess) {
+                const int gc = (int)((ns + 255) / 256 < 4096 ? (ns + 255) / 256 : 4096);
+                ksys_compact_kernel<<<gc ? gc : 1, 256, 0, s>>>(ns, (uint32_t)bytes, cand.p, can.p, status.p, aut.p,
+                                                                trials.p, coffs.p, next.p + n_next * bytes,
+                                                                complete ? aut_out.p + 2 * n_next : nullptr,
+                                                                ticket.p + 1, tsum.p);
+                e = cudaGetLastError();
+            }
+            uint64_t n_can = 0;
+            if (e == cudaSuccess)
+                e = read_u64(coffs.p + ns, &n_can, s);
+            if (e != cudaSuccess)
+                return done(CANON_ECUDA, "check", e);
+            float ms = 0.f, gms2 = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventElapsedTime(&gms2, g0, g1);
+            st.gen_seconds += gms2 * 1e-3;
+            st.kernel_ms += ms;
+            st.level_kernel_ms[m - 1] += ms;
+            ++st.batches;
+            c->launches += 7;
+            n_next += n_can;
+            p0 = p1;
+        }
+        st.checks += n_cand;
+        st.level_checks[m - 1] += n_cand;
+        ++st.levels;
+        lev.swap(next);
+        n_par = n_next;
+        n = m;
+    }
+    unsigned bad = 0;
+    unsigned long long tried = 0;
+    e = cudaMemcpyAsync(&bad, ticket.p + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&tried, tsum.p, sizeof(tried), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return done(CANON_ECUDA, "status", e);
+    st.trials = tried;
+    if (bad) {
+        if (stats)
+            *stats = st;
+        return done(CANON_ETIMEOUT, "a check reported a bad status", cudaSuccess);
+    }
+    if (n == rounds && n_par) {
+        const size_t bytes = (size_t)rounds * np;
+        std::vector<uint8_t> mats((size_t)n_par * bytes);
+        std::vector<uint64_t> auts((size_t)n_par * 2);
+        e = cudaMemcpyAsync(mats.data(), lev.p, mats.size(), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(auts.data(), aut_out.p, auts.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess)
+            return done(CANON_ECUDA, "designs", e);
+        st.designs = n_par;
+        if (cb)
+            for (uint64_t i = 0; i < n_par; ++i)
+                cb(user, mats.data() + i * bytes, rounds, np, auts[2 * i], auts[2 * i + 1]);
+    }
+    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats)
         *stats = st;
     return done(CANON_OK, "", cudaSuccess);

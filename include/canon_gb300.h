@@ -246,7 +246,9 @@ typedef struct {
      * level_checks[v-1] counts the complete matrices constructed */
     uint64_t level_checks[16];
     double   level_kernel_ms[16];
-    double   gen_seconds; /* host time spent generating the candidates */
+    double   gen_seconds; /* time spent generating the candidates (host wall time, or
+                             device time of the generation kernels) */
+    uint64_t trials;      /* k-systems: relabelings tried by all checks (cnvCheckNew candidates) */
 } canon_enum_stats;
 
 /* Called for every canonical complete matrix: BIBD rows as rows x uint64 (cast to
@@ -260,10 +262,12 @@ typedef void (*canon_design_cb)(void *user, const uint8_t *matrix, uint32_t rows
  * (Source/Enumerator.cpp:540-1024; checks at :446-447 and :364).  v <= 16, b <= 63. */
 int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uint32_t k, uint32_t lambda,
                          canon_design_cb cb, void *user, canon_enum_stats *stats);
-/* All 1-factorizations of K_np up to isomorphism, round by round, every round's
- * partial matrices checked in batches on the GPU: the work of alldata::Run() for
- * group size 2 with the check at every level (k-Factorization/TripleSys/Source/
- * TripleSys.cpp:80-775, check at checkCurrentResult.cpp:91).  np even, <= 12. */
+/* All 1-factorizations of K_np up to isomorphism, round by round with every level in
+ * HBM: the next rounds of all canonical parents are generated on the GPU (the round
+ * construction of processOneDay()/getNextPlayer(), k-Factorization/TripleSys/Source/
+ * TripleSys.cpp:487-775), checked there and the canonical ones kept: the work of
+ * alldata::Run() for group size 2 with the check at every level (TripleSys.cpp:80-775,
+ * check at checkCurrentResult.cpp:91).  np even, <= 12. */
 int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *user, canon_enum_stats *stats);
 
 /* ---- seeded inputs of an uneven batched check ----
