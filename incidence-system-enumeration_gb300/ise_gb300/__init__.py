@@ -59,8 +59,10 @@ HEADER_SYMBOLS = [
     "canon_label_first_rows", "canon_mlp_forward", "canon_mlp_grad", "canon_mlp_train",
     "canon_design_properties", "canon_report_bibd", "canon_ksys_cycles", "canon_report_ksys",
     "canon_tune_bibd", "canon_generate_partial_bibd", "canon_generate_partial_ksys", "canon_lexmax_nodes_bibd",
-    "canon_measure_int_peak",
+    "canon_measure_int_peak", "canon_canonize_ksys_binary",
 ]
+# the reference's plugin (k-Factorization/Utils/Include/CDTools.h:9-11)
+PLUGIN_SYMBOLS = ["createCanonizer", "releaseCanonizer", "runCanonizer"]
 MLP_PARAMS = 128 * 64 + 128 + 128 * 128 + 128 + 128 + 1
 
 
@@ -200,6 +202,12 @@ def load_library(path=LIB_PATH):
     L.canon_generate_partial_ksys.argtypes = [u32, u32, u64, u32, u32, u8p, u8p]
     L.canon_lexmax_nodes_bibd.argtypes = [vp, u32, u32, u32, u32, vp, vp]
     L.canon_measure_int_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    L.canon_canonize_ksys_binary.argtypes = [vp, u32, u32, u32, u8p, u8p, u64p]
+    L.createCanonizer.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.createCanonizer.restype = vp
+    L.releaseCanonizer.argtypes = [vp]
+    L.runCanonizer.argtypes = [vp, u8p, ctypes.c_int, ctypes.c_int]
+    L.runCanonizer.restype = ctypes.POINTER(ctypes.c_uint8)
     _lib = L
     return L
 
@@ -457,6 +465,18 @@ class Context:
         self._check(self.lib.canon_measure_int_peak(self.h, ctypes.byref(x)))
         return x.value
 
+    def canonize_ksys_binary(self, data, np_, days):
+        """Canonical binary matrices (n x np x days*np/2) of n k-systems' first `days`
+        rounds, and the labelings reaching each (canon_canonize_ksys_binary)."""
+        X = np.ascontiguousarray(data, np.uint8).reshape(-1, days, np_)
+        n = X.shape[0]
+        b = days * np_ // 2
+        out = np.zeros((n, np_, b), np.uint8)
+        aut = np.zeros(n, np.uint64)
+        self._check(self.lib.canon_canonize_ksys_binary(self.h, n, np_, days, _ptr(X, ctypes.c_uint8),
+                                                        _ptr(out, ctypes.c_uint8), _ptr(aut, ctypes.c_uint64)))
+        return out, aut
+
     def tune_bibd(self, n, v, b, flags, d_rows):
         """Autotunes the check variant for (v, b, flags) on n device-resident matrices;
         returns (variant kept, [ms per variant: -1 not applicable, -2 outputs differed])."""
@@ -539,6 +559,39 @@ class Context:
 
     def kernel_launches(self):
         return int(self.lib.canon_kernel_launches(self.h))
+
+
+class Canonizer:
+    """The reference's plugin (createCanonizer / runCanonizer / releaseCanonizer,
+    k-Factorization/Utils/Include/CDTools.h:9-11) through the C ABI."""
+
+    def __init__(self, v, k=2):
+        self.lib = load_library()
+        self.v, self.k = v, k
+        self.h = self.lib.createCanonizer(v, k)
+        if not self.h:
+            raise CanonError(CANON_EINVAL, "createCanonizer(%d, %d) failed" % (v, k))
+
+    def run(self, matrix, iDay=0):
+        """runCanonizer(): the canonical binary matrix (v x days*v/k) or None on error."""
+        M = np.ascontiguousarray(matrix, np.uint8)
+        p = self.lib.runCanonizer(self.h, _ptr(M, ctypes.c_uint8), self.k, iDay)
+        if not p:
+            return None
+        days = (self.v - 1) // (self.k - 1) if iDay <= 0 else iDay
+        b = days * self.v // self.k
+        return np.ctypeslib.as_array(p, shape=(self.v * b,)).reshape(self.v, b).copy()
+
+    def close(self):
+        if self.h:
+            self.lib.releaseCanonizer(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class CanonicityChecker:

@@ -297,6 +297,30 @@ int canon_generate_partial_bibd(uint32_t v, uint32_t b, uint32_t r, uint32_t k, 
 int canon_generate_partial_ksys(uint32_t np, uint32_t n, uint64_t seed, uint32_t min_rounds, uint32_t max_rounds,
                                 uint8_t *data, uint8_t *nrows);
 
+/* ---- the canonical binary matrix of k-systems (the reference's plugin) ----
+ * createCanonizer / runCanonizer / releaseCanonizer replace the reference's exported
+ * plugin of the same names and signatures (k-Factorization/Utils/Include/CDTools.h:9-11,
+ * Source/CDTools.cpp:5-52).  runCanonizer() writes the first iDay rounds of a k-system
+ * (all numDays = (v-1)/(k-1) rounds when iDay <= 0; rounds as result() holds them) as a
+ * binary matrix -- one column per group of each day, row p = player p
+ * (convertToBinaryMatrix, Source/matrix.h:198-209) -- and returns its canonical form,
+ * the matrix CanonizeMatrix(k, NULL, numClasses) converges to
+ * (Source/MatrixCanonChecker.cpp:420-564): the lexicographically greatest matrix over
+ * permutations of the players, of the groups inside each day and, when all days are
+ * given, of the days.  v rows of iDay*v/k bytes, owned by the canonizer and valid until
+ * its next call; NULL on error.  Group size k = 2, v even, 6 <= v <= 16; the
+ * canonizer holds a context on GPU 0.  Not thread-safe per canonizer (as the
+ * reference's). */
+void *createCanonizer(int v, int k);
+void releaseCanonizer(void *pCanonizer);
+const unsigned char *runCanonizer(void *pCanonizer, const unsigned char *pMatrix, int k, int iDay);
+/* The same for n k-systems at once: data = n x days x np bytes (host), out = n x np x
+ * (days*np/2) bytes (host), aut_out[n] (optional) = the number of player labelings that
+ * reach the canonical form (the order of its automorphism group).  One GPU thread per
+ * k-system. */
+int canon_canonize_ksys_binary(canon_ctx *ctx, uint32_t n, uint32_t np, uint32_t days, const uint8_t *data,
+                               uint8_t *out, uint64_t *aut_out);
+
 /* ---- result tables (the reference's text output of a finished run) ----
  * Per complete design: simple[i] = no two equal columns (no replicated blocks) and
  * transitive[i] = Aut(D) transitive on the points, the properties that the

@@ -200,6 +200,8 @@ void or_set_group_impl(void *np_fn, void *aa_fn, void *ugo_fn)
  * orbits of level n are given by their start columns.
  * ===================================================================== */
 #define OR_BMAX 64
+#define OR_RMAX 16      /* entries below this (rank of the coloured first row of a k-system) */
+#define OR_KS_NPMAX 16  /* players of a k-system whose binary matrix is canonised */
 typedef struct {
     int n;                    /* number of orbits */
     uint8_t start[OR_BMAX];
@@ -248,10 +250,13 @@ int or_bibd_is_normal(const uint8_t *M, int nrows, int b)
  * 0..nrows-1 in turn with column swaps carried into the rows below (pColPermut
  * == NULL branch): inside every orbit the first 0 from the left is swapped with
  * the last 1 from the right until the row is 1s-first. */
-void or_bibd_normalize(uint8_t *M, int nrows, int b)
+/* GenerateBinaryColumnOrbits() of binary rows from..nrows-1 (rows above `from` are
+ * kept as they are; they may hold other values, as the coloured first row of a
+ * k-system's binary matrix does) */
+static void or_normalize_rows(uint8_t *M, int nrows, int b, int from)
 {
     or_orbits o;
-    for (int r = 0; r < nrows; r++) {
+    for (int r = from; r < nrows; r++) {
         or_level_orbits(M, r, b, &o);
         uint8_t *row = M + r * b;
         for (int q = 0; q < o.n; q++) {
@@ -285,31 +290,58 @@ void or_bibd_normalize(uint8_t *M, int nrows, int b)
     }
 }
 
-/* checkColOrbit(), CanonicityChecker.cpp:191-223 (rank 2): compare the number of
- * 1s of row `row` inside orbit [s, s+len) with the number of 1s of the permuted
- * row under the current column arrangement; on equality reorder permCol inside
- * the orbit (1s first, each part keeping its order). */
-static int or_check_col_orbit(int len, int s, const uint8_t *row, const uint8_t *rowPerm,
-                              uint8_t *permCol)
+void or_bibd_normalize(uint8_t *M, int nrows, int b)
 {
-    uint8_t ones[OR_BMAX], zeros[OR_BMAX];
-    int n1 = 0, n0 = 0, c1 = 0;
+    or_normalize_rows(M, nrows, b, 0);
+}
+
+/* checkColOrbit(), CanonicityChecker.cpp:191-223: compare, from the greatest value
+ * down to 1, the number of entries of each value of row `row` inside orbit
+ * [s, s+len) with the same count of the permuted row under the current column
+ * arrangement; on equality reorder permCol inside the orbit by decreasing value
+ * (each value class keeping its order).  Rank 2 is the incidence-matrix case
+ * (counts of 1s); the binary matrix of a k-system has a first row of rank > 2. */
+static int or_check_col_orbit(int len, int s, const uint8_t *row, const uint8_t *rowPerm,
+                              uint8_t *permCol, int rank)
+{
+    int cnt_row[OR_RMAX] = {0}, cnt_perm[OR_RMAX] = {0};
     for (int i = 0; i < len; i++) {
-        uint8_t col = permCol[s + i];
-        if (rowPerm[col])
-            ones[n1++] = col;
-        else
-            zeros[n0++] = col;
-        c1 += row[s + i];
+        cnt_row[row[s + i]]++;
+        cnt_perm[rowPerm[permCol[s + i]]]++;
     }
-    int diff = c1 - n1;
-    if (diff < 0)
-        return -1;
-    if (diff > 0)
-        return 1;
-    memcpy(permCol + s, ones, n1);
-    memcpy(permCol + s + n1, zeros, n0);
+    for (int v = rank - 1; v >= 1; v--) {
+        const int diff = cnt_row[v] - cnt_perm[v];
+        if (diff < 0)
+            return -1;
+        if (diff > 0)
+            return 1;
+    }
+    uint8_t out[OR_BMAX];
+    int k = 0;
+    for (int v = rank - 1; v >= 0; v--)
+        for (int i = 0; i < len; i++)
+            if (rowPerm[permCol[s + i]] == v)
+                out[k++] = permCol[s + i];
+    memcpy(permCol + s, out, len);
     return 0;
+}
+
+/* every row non-increasing inside every column orbit of the rows above it (for rank
+ * 2: 1s-first); values below `rank` */
+static int or_rank_is_normal(const uint8_t *M, int nrows, int b, int rank)
+{
+    or_orbits o;
+    for (int r = 0; r < nrows; r++) {
+        or_level_orbits(M, r, b, &o);
+        for (int q = 0; q < o.n; q++)
+            for (int c = o.start[q]; c < o.start[q] + o.len[q]; c++) {
+                if (M[r * b + c] >= rank)
+                    return 0;
+                if (c > o.start[q] && M[r * b + c] > M[r * b + c - 1])
+                    return 0;
+            }
+    }
+    return 1;
 }
 
 /* TestCanonicity(), Source/CanonicityChecker.h:255-586, for numParts == 1, no
@@ -317,12 +349,22 @@ static int or_check_col_orbit(int len, int s, const uint8_t *row, const uint8_t 
  * matrices: out_info = OR_SAVE_ROW_PERM | OR_SAVE_ROW_TO_CHANGE (Enumerator.cpp:696);
  * partial matrices: OR_SAVE_NOTHING (Enumerator.cpp:446-447), automorphisms are
  * stored as permutations of the column orbits of the last level (:427-451). */
+static int or_test_rank(const uint8_t *M, int nrows, int b, int rank, unsigned out_info, int len_stab,
+                        or_bibd_result *res);
+
 int or_bibd_test(const uint8_t *M, int nrows, int b, unsigned out_info, int len_stab,
                  or_bibd_result *res)
 {
-    if (nrows < 1 || nrows > 64 || b < 1 || b > OR_BMAX)
+    return or_test_rank(M, nrows, b, 2, out_info, len_stab, res);
+}
+
+/* TestCanonicity() for entries below `rank` (the reference's rank(): maxElement + 1) */
+static int or_test_rank(const uint8_t *M, int nrows, int b, int rank, unsigned out_info, int len_stab,
+                        or_bibd_result *res)
+{
+    if (nrows < 1 || nrows > 64 || b < 1 || b > OR_BMAX || rank < 2 || rank > OR_RMAX)
         return -1;
-    if (!or_bibd_is_normal(M, nrows, b))
+    if (!or_rank_is_normal(M, nrows, b, rank))
         return -2;
 
     const int row_permut = (out_info & OR_SAVE_ROW_PERM) != 0;
@@ -395,7 +437,7 @@ int or_bibd_test(const uint8_t *M, int nrows, int b, unsigned out_info, int len_
                 int s = o->start[q], len = o->len[q], diff;
                 res->st.orbits++;
                 if (len > 1)
-                    diff = or_check_col_orbit(len, s, row, rowPerm, permCol);
+                    diff = or_check_col_orbit(len, s, row, rowPerm, permCol, rank);
                 else
                     diff = (int)row[s] - (int)rowPerm[permCol[s]];
                 if (diff > 0)
@@ -514,6 +556,148 @@ int or_bibd_canonize(uint8_t *M, int nrows, int b, or_bibd_result *res)
         (void)first;
         or_bibd_normalize(M, nrows, b);
     }
+}
+
+/* =====================================================================
+ * runCanonizer(): the canonical binary matrix of a k-system
+ * (Source/CDTools.cpp:5-52).  createCanonizer(v, k) sets up a C_InSys of v+1 rows
+ * and b = numDays*v/k columns whose first row colours the columns by day
+ * (prepareFirstMatrixRow, Source/matrix.h:192-197: numDays groups of v/k columns,
+ * values numDays-1 down to 0); runCanonizer() fills rows 1..v from the k-system
+ * (convertToBinaryMatrix, matrix.h:198-209: column = one group of one day, row
+ * 1+p = player p), keeps only the first dayNumb days when fewer are given
+ * (adjustData: the columns of the first days dropped, the rank set to dayNumb,
+ * no class permutations), and calls CanonizeMatrix(k, NULL, numClasses)
+ * (Source/MatrixCanonChecker.cpp:420-564) with numClasses = numDays for a complete
+ * matrix.  The result is rows 1..v of the canonised matrix.
+ * ===================================================================== */
+
+static int or_cmp_desc_len;
+static int or_row_cmp_desc(const void *a, const void *b)
+{
+    return memcmp(b, a, (size_t)or_cmp_desc_len);   /* compareRows(), MatrixCanonChecker.cpp:389-392 */
+}
+
+/* sortRowsUpdateColumnOrbits(), MatrixCanonChecker.cpp:394-418: rows from..v-1 in
+ * decreasing order, then GenerateBinaryColumnOrbits() for each of them */
+static void or_sort_rows_update(uint8_t *M, int v, int b, int from)
+{
+    or_cmp_desc_len = b;
+    qsort(M + (size_t)from * b, (size_t)(v - from), (size_t)b, or_row_cmp_desc);
+    or_normalize_rows(M, v, b, from);
+}
+
+/* the TestCanonicity() loop of CanonizeMatrix() (:450-494) for a matrix whose first
+ * row is never moved (nRowStart = 1, k > 0); returns the number of calls */
+static int or_canonize_rank(uint8_t *M, int v, int b, int rank)
+{
+    or_bibd_result res;
+    memset(&res, 0, sizeof(res));
+    uint8_t tmp[(OR_KS_NPMAX + 1) * OR_BMAX];
+    int calls = 0;
+    for (;;) {
+        if (or_test_rank(M, v, b, rank, OR_SAVE_ROW_PERM, 0, &res) < 0)
+            return -1;
+        calls++;
+        if (res.canonical)
+            return calls;
+        /* row i of the new matrix is old row permRow()[i] (:458-475) */
+        memcpy(tmp, M, (size_t)v * b);
+        int first = -1;
+        for (int i = 1; i < v; i++) {
+            memcpy(M + (size_t)i * b, tmp + (size_t)res.witness[i] * b, (size_t)b);
+            if (first < 0 && res.witness[i] != i)
+                first = i;
+        }
+        if (first < 0)
+            return -1;      /* a rejection always moves a row */
+        /* GenerateBinaryColumnOrbits() from the first moved row on (:476-486), then,
+         * k > 0, sortRowsUpdateColumnOrbits() from there (:488-492) */
+        or_normalize_rows(M, v, b, first);
+        or_sort_rows_update(M, v, b, first);
+    }
+}
+
+int or_ksys_binary_canonize(const uint8_t *R, int np, int k, int day_numb, uint8_t *out, long *class_steps)
+{
+    if (k < 2 || np < 2 * k || np % k || (np - 1) % (k - 1) || np > OR_KS_NPMAX)
+        return -1;
+    const int num_days = (np - 1) / (k - 1);
+    const int g = np / k;                           /* groups (columns) of one day */
+    if (day_numb <= 0)
+        day_numb = num_days;
+    if (day_numb < 2 || day_numb > num_days || day_numb * g > OR_BMAX)
+        return -1;
+    const int num_classes = day_numb == num_days ? num_days : 0;
+    const int rank = day_numb;
+    const int v = np + 1, b = day_numb * g;
+    uint8_t M[(OR_KS_NPMAX + 1) * OR_BMAX];
+    memset(M, 0, sizeof(M));
+    for (int c = 0; c < b; c++)
+        M[c] = (uint8_t)(day_numb - 1 - c / g);     /* the day colours, highest first */
+    for (int d = 0; d < day_numb; d++)
+        for (int j = 0; j < g; j++)
+            for (int n = 0; n < k; n++)
+                M[(size_t)(1 + R[d * np + j * k + n]) * b + d * g + j] = 1;
+    /* k > 0: rows sorted and made 1s-first inside the day groups (:440-451) */
+    or_sort_rows_update(M, v, b, 1);
+
+    const size_t len_data = (size_t)np * b;         /* rows 1..v of the matrix */
+    uint8_t comp[OR_KS_NPMAX * OR_BMAX];
+    int have_comp = 0, cmp = 1;
+    uint8_t idx = OR_IMAX;
+    uint8_t cperm[OR_KS_NPMAX], corb[OR_KS_NPMAX];
+    or_group cg;
+    memset(&cg, 0, sizeof(cg));
+    cg.order = 1;
+    long steps = 0;
+    for (;;) {
+        if (or_canonize_rank(M, v, b, rank) < 0)
+            return -2;
+        if (!num_classes)
+            break;
+        steps++;
+        if (have_comp) {
+            const int c = memcmp(M + b, comp, len_data);
+            cmp = (c > 0) - (c < 0);
+            if (!cmp) {
+                /* the same matrix again: an automorphism on the classes */
+                g_aa(&cg, (unsigned)num_classes, cperm, corb, 1, 1);
+                idx = OR_IMAX;
+            } else if (cmp < 0) {
+                memcpy(M + b, comp, len_data);
+            }
+        } else {
+            have_comp = 1;
+        }
+        if (cmp == 1) {
+            /* initOrbits(), CanonicityChecker.h:78-87: identity, trivial orbits */
+            cg.stab = cg.stab_aut = (unsigned)num_classes - 1;
+            for (int i = 0; i < num_classes; i++)
+                cperm[i] = corb[i] = (uint8_t)i;
+            memcpy(comp, M + b, len_data);
+        }
+        idx = g_np(&cg, cperm, corb, (uint8_t)num_classes, idx, 0);
+        if (idx == OR_EMAX)
+            break;
+        /* The reference passes lenPerm as the next index; next_permutation() then takes
+         * its branch for an index past the last element, which reverses nothing and
+         * continues as a plain next permutation (ELEMENT_MAX, no stabiliser). */
+        idx = OR_EMAX;
+        int i = 0;
+        while (cperm[i] == i)
+            i++;
+        /* the column groups of rows 1..v in the order of the class permutation (:526-535) */
+        for (; i < num_classes; i++)
+            for (int r = 1; r < v; r++)
+                memcpy(M + (size_t)r * b + (size_t)i * g, comp + (size_t)(r - 1) * b + (size_t)cperm[i] * g,
+                       (size_t)g);
+        or_sort_rows_update(M, v, b, 1);
+    }
+    memcpy(out, M + b, len_data);
+    if (class_steps)
+        *class_steps = steps;
+    return b;
 }
 
 /* =====================================================================

@@ -94,6 +94,12 @@ typedef struct {
 
 int or_ksys_test(const uint8_t *R, int nrows, int np, int g, int full_aut, or_ksys_result *res);
 
+/* runCanonizer() (Source/CDTools.cpp:5-52): the canonical binary matrix of a k-system
+ * of np players in groups of k, its first day_numb rounds (<= 0: all); R holds the
+ * rounds as result() does.  out: np x b bytes (b = day_numb * np / k, returned);
+ * class_steps (optional): canonisations of the class loop.  <0 on invalid input. */
+int or_ksys_binary_canonize(const uint8_t *R, int np, int k, int day_numb, uint8_t *out, long *class_steps);
+
 /* ---- enumerators used to pin the oracle on the reference's known answers ---- */
 typedef void (*or_design_cb)(void *user, const uint8_t *M, int v, int b, uint64_t aut_lo, uint64_t aut_hi);
 /* orderly row-by-row generation of all BIBD(v,b,r,k,lambda); returns #canonical designs */

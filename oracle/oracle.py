@@ -159,6 +159,19 @@ def ksys_test(R, full_aut=False, aut_cap=0):
     return out
 
 
+def ksys_binary_canonize(R, np_, k=2, day_numb=0):
+    """runCanonizer(): the canonical binary matrix (np x day_numb*np/k bytes) of the
+    first day_numb rounds of a k-system (all rounds when day_numb <= 0)."""
+    R = np.ascontiguousarray(R, dtype=np.uint8)
+    days = (np_ - 1) // (k - 1) if day_numb <= 0 else day_numb
+    out = np.zeros(np_ * days * (np_ // k), np.uint8)
+    steps = ctypes.c_long()
+    b = lib().or_ksys_binary_canonize(_u8p(R), np_, k, day_numb, _u8p(out), ctypes.byref(steps))
+    if b < 0:
+        raise ValueError("oracle rejected input (rc=%d)" % b)
+    return out.reshape(np_, b), steps.value
+
+
 def bibd_enumerate(v, b, r, k, lam):
     found = []
 

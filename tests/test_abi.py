@@ -26,6 +26,24 @@ def test_library_exports_header_symbols():
     assert sorted(ise_gb300.HEADER_SYMBOLS) == names
 
 
+def test_library_exports_the_reference_plugin():
+    """createCanonizer / runCanonizer / releaseCanonizer, the reference's exported
+    plugin (k-Factorization/Utils/Include/CDTools.h:9-11), are declared and exported
+    under their own names."""
+    conftest.build_native()
+    import ise_gb300
+    lib = ctypes.CDLL(ise_gb300.LIB_PATH)
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    for name in ise_gb300.PLUGIN_SYMBOLS:
+        assert re.search(r"\b%s\s*\(" % name, src), name
+        assert hasattr(lib, name), name
+    # arguments the plugin refuses without touching a GPU
+    lib = ise_gb300.load_library()
+    assert not lib.createCanonizer(10, 3)          # group size 2 only
+    assert not lib.createCanonizer(7, 2)           # v must be even
+    assert not lib.runCanonizer(None, None, 2, 0)
+
+
 def test_create_without_gpu_fails_cleanly():
     import torch
     if torch.cuda.is_available():
