@@ -375,8 +375,9 @@ ENUM_WORKLOADS = {
     # so they carry no CPU leg
     "enum-12-22": ("bibd", (12, 22, 11, 6, 5), "all BIBD(12,22,11,6,5) (11,603 designs) by orderly generation"),
     "enum-9-36": ("bibd", (9, 36, 12, 3, 3), "all BIBD(9,36,12,3,3) (22,521 designs) by orderly generation"),
+    "enum-16-24": ("bibd", (16, 24, 9, 6, 3), "all BIBD(16,24,9,6,3) (18,920 designs) by orderly generation"),
 }
-ENUM_NO_CPU = {"enum-12-22", "enum-9-36"}
+ENUM_NO_CPU = {"enum-12-22", "enum-9-36", "enum-16-24"}
 
 
 def run_enum(args):

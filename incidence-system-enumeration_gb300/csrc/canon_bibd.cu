@@ -123,6 +123,33 @@ __global__ void __launch_bounds__(TPB) bibd_max_kernel(uint32_t n_items, uint32_
     }
 }
 
+// Automorphisms of canonical matrices (the parents of the next enumeration level):
+// the pruned lex-max search of each, recording the automorphisms it finds while the
+// matrix is still its own bound (at most gcap per matrix, row permutations
+// nibble-packed); they prune the parent's children in the row generator.
+__global__ void __launch_bounds__(TPB) bibd_autgen_kernel(uint32_t n_items, uint32_t v, uint32_t b,
+                                                          const uint64_t *__restrict__ rows, uint64_t *gens,
+                                                          uint8_t *ngens, uint32_t gcap, uint64_t max_nodes,
+                                                          unsigned *ticket) {
+    __shared__ uint64_t s_rows[VMAX * TPB];
+    __shared__ uint64_t s_lvl[(VMAX + 1) * TPB];
+    __shared__ uint16_t s_vd[VMAX * TPB];
+    __shared__ uint16_t s_cm[64 * TPB];
+    const unsigned tid = threadIdx.x;
+    SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
+    for (;;) {
+        const unsigned it = atomicAdd(ticket, 1u);
+        if (it >= n_items)
+            break;
+        MaxOut mo{};
+        uint64_t *g = gens + (size_t)it * gcap;
+        if (load_rows(sm, rows + (size_t)it * v, v, b, 0))
+            max_search(sm, v, b, max_nodes, mo, ID16, true, false, 0xFFFFu, nullptr, 0xFFFFu, g, gcap);
+        // a matrix found not canonical (or out of budget) prunes nothing
+        ngens[it] = (uint8_t)((mo.improved || mo.timeout) ? 0 : mo.n_gens);
+    }
+}
+
 // Throughput of the integer pipes on this GPU: every thread runs eight independent
 // chains of 32-bit XOR / ADD / shift-add steps (LOP3 and IADD3 class operations)
 // for `iters` rounds; a round is 24 operations per thread.  The result is stored
@@ -738,6 +765,19 @@ cudaError_t launch_bibd_lexmax_nodes(uint32_t n, uint32_t v, uint32_t b, uint32_
         bibd_max_kernel<64, 16><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, nullptr, nullptr, nullptr, max_nodes,
                                                      tk, d_orders, d_nodes);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bibd_autgen(uint32_t n, uint32_t v, uint32_t b, const uint64_t *d_rows, uint64_t *d_gens,
+                               uint8_t *d_ngens, uint32_t gcap, uint64_t max_nodes, unsigned *tk, int num_sms,
+                               cudaStream_t s) {
+    if (!n)
+        return cudaSuccess;
+    CANON_TRY(cudaMemsetAsync(tk, 0, sizeof(unsigned), s));
+    const int need = (int)((n + TPB - 1) / TPB);
+    int grid = 0;
+    CANON_TRY(grid_for((const void *)bibd_autgen_kernel, num_sms, need, &grid));
+    bibd_autgen_kernel<<<grid, TPB, 0, s>>>(n, v, b, d_rows, d_gens, d_ngens, gcap, max_nodes, tk);
     return cudaGetLastError();
 }
 

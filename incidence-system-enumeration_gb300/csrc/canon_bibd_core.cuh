@@ -591,6 +591,7 @@ struct MaxOut {
     unsigned first_rows;  // rows that start a labeling reaching the canonical form
     unsigned orbit0;      // pruned search of a canonical M: the first rows found in the orbit of row 0
     unsigned orbit1;      // ... and the second rows (under row 0) found in the orbit of row 1
+    unsigned n_gens;      // automorphisms written to gens_out (pruned search, M canonical so far)
 };
 
 // The arranged column masks for level lv+1 after row `cand` was taken at level
@@ -636,11 +637,14 @@ __device__ __forceinline__ void refine_arranged(S sm, unsigned lv, unsigned cand
 // under the automorphisms that fix row 0.
 // stop: a flag that another thread of a split search raises once it has shown M
 // not to be canonical; it is read every 64 nodes and ends this share early.
+// gens_out: the automorphisms the pruned search finds while M may still be canonical,
+// as row permutations (nibble i = the row at position i), at most gens_cap of them;
+// they generate the group whose orbits the pruning uses.
 template <typename S>
 __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, MaxOut &o,
                            uint64_t order0 = ID16, bool prune = true, bool stop_on_improve = false,
                            unsigned root_mask = 0xFFFFu, const volatile unsigned *stop = nullptr,
-                           unsigned root_mask1 = 0xFFFFu) {
+                           unsigned root_mask1 = 0xFFFFu, uint64_t *gens_out = nullptr, unsigned gens_cap = 0) {
     const unsigned allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     const uint64_t cols = (1ull << b) - 1ull;
     const uint64_t sentinel = 1ull << b;
@@ -652,6 +656,7 @@ __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, Max
     o.first_rows = 0;
     o.orbit0 = 0;
     o.orbit1 = 0;
+    o.n_gens = 0;
     unsigned valid = n;        // rows 0..valid-1 of the bound (and levels 0..valid) are set
     unsigned used = 0;
     uint64_t perm = 0;
@@ -667,6 +672,8 @@ __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, Max
                 if (pr && id_top < n) {
                     // an automorphism moving row id_top: merge its orbits and go back
                     // to the identity node it branched from
+                    if (gens_out && o.n_gens < gens_cap)
+                        gens_out[o.n_gens++] = perm;
                     orb = merge_orbits(perm, orb, n, id_top, nmask1);
                     i = id_top;
                     used = (1u << i) - 1u;

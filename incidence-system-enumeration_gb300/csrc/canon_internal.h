@@ -89,6 +89,11 @@ cudaError_t launch_bibd_labels(uint32_t n, uint32_t v, uint32_t b, uint32_t flag
 cudaError_t launch_bibd_lexmax_nodes(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
                                      uint64_t *d_nodes, uint64_t max_nodes, unsigned *d_ticket, int num_sms,
                                      cudaStream_t s, const uint64_t *d_orders = nullptr);
+// automorphisms (row permutations, nibble-packed) of n canonical matrices, at most gcap
+// each: d_gens n*gcap words, d_ngens n bytes
+cudaError_t launch_bibd_autgen(uint32_t n, uint32_t v, uint32_t b, const uint64_t *d_rows, uint64_t *d_gens,
+                               uint8_t *d_ngens, uint32_t gcap, uint64_t max_nodes, unsigned *d_ticket,
+                               int num_sms, cudaStream_t s);
 // integer-pipe throughput probe: *ops = 32-bit lane operations of the launch
 cudaError_t launch_int_peak(uint32_t iters, int num_sms, uint32_t *d_sink, cudaStream_t s, uint64_t *ops);
 // order of the rows as first-row candidates by decreasing score (scores: n x v floats)

@@ -25,6 +25,7 @@
 // exactly those the depth-first search finds.
 #include <sched.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -96,15 +97,18 @@ struct DevBuf {
 // copies for parents with at most this many children
 constexpr uint32_t ROW_CACHE = 16;
 
+// gens / ngens: automorphisms of every parent that prune its children (none if null)
 __global__ void __launch_bounds__(GEN_TPB) rows_count_kernel(canon::rows::Params d, const uint64_t *parents,
                                                              uint32_t n_par, int n, uint32_t *counts,
-                                                             uint64_t *cache, unsigned *ticket) {
+                                                             uint64_t *cache, unsigned *ticket,
+                                                             const uint64_t *gens, const uint8_t *ngens) {
     for (;;) {
         const unsigned p = atomicAdd(ticket, 1u);
         if (p >= n_par)
             break;
-        counts[p] = canon::rows::children<canon::rows::NEW_ROW>(d, parents + (size_t)p * n, n,
-                                                               cache + (size_t)p * ROW_CACHE, ROW_CACHE);
+        counts[p] = canon::rows::children<canon::rows::NEW_ROW>(
+            d, parents + (size_t)p * n, n, cache + (size_t)p * ROW_CACHE, ROW_CACHE,
+            gens ? gens + (size_t)p * canon::rows::AUT_GENS : nullptr, gens ? ngens[p] : 0);
     }
 }
 
@@ -112,7 +116,8 @@ __global__ void __launch_bounds__(GEN_TPB) rows_emit_kernel(canon::rows::Params 
                                                             uint32_t p0, uint32_t p1, int n,
                                                             const uint64_t *offsets, const uint32_t *counts,
                                                             const uint64_t *cache, uint64_t *out,
-                                                            unsigned *ticket) {
+                                                            unsigned *ticket, const uint64_t *gens,
+                                                            const uint8_t *ngens) {
     const uint64_t base = offsets[p0];
     for (;;) {
         const unsigned p = p0 + atomicAdd(ticket, 1u);
@@ -128,7 +133,9 @@ __global__ void __launch_bounds__(GEN_TPB) rows_emit_kernel(canon::rows::Params 
                 dst[(size_t)j * (n + 1) + n] = cache[(size_t)p * ROW_CACHE + j];
             }
         } else {
-            canon::rows::children<canon::rows::CHILD>(d, par, n, dst, cnt);
+            canon::rows::children<canon::rows::CHILD>(d, par, n, dst, cnt,
+                                                      gens ? gens + (size_t)p * canon::rows::AUT_GENS : nullptr,
+                                                      gens ? ngens[p] : 0);
         }
     }
 }
@@ -414,7 +421,12 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
     cudaStream_t s = c->stream;
     canon_enum_stats st{};
     const canon::rows::Params prm{(int)v, (int)b, (int)r, (int)k, (int)lambda};
-    DevBuf<uint64_t> lev, next, cand, doffs, coffs, sums, aut, aut_out, rcache;
+    DevBuf<uint64_t> lev, next, cand, doffs, coffs, sums, aut, aut_out, rcache, gens;
+    DevBuf<uint8_t> ngens;
+    constexpr uint32_t NG = canon::rows::AUT_GENS;
+    std::vector<uint64_t> hgens(NG, 0);     // automorphisms of the host level's parents
+    std::vector<uint8_t> hngens(1, 0);
+    bool have_gens = false;
     DevBuf<uint32_t> dcounts;
     DevBuf<uint8_t> can, status;
     DevBuf<unsigned> ticket, stop;
@@ -452,18 +464,28 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
         if (!dev) {
             if (!host_valid) {
                 level.resize((size_t)n_par * n);
+                hgens.resize((size_t)n_par * NG);
+                hngens.resize(n_par);
                 e = cudaMemcpyAsync(level.data(), lev.p, level.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
+                if (e == cudaSuccess && have_gens)
+                    e = cudaMemcpyAsync(hgens.data(), gens.p, hgens.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                        s);
+                if (e == cudaSuccess && have_gens)
+                    e = cudaMemcpyAsync(hngens.data(), ngens.p, n_par, cudaMemcpyDeviceToHost, s);
                 if (e == cudaSuccess)
                     e = cudaStreamSynchronize(s);
                 if (e != cudaSuccess)
                     return done(CANON_ECUDA, "level to host", e);
+                if (!have_gens)
+                    std::fill(hngens.begin(), hngens.end(), (uint8_t)0);
                 host_valid = true;
             }
             counts.resize(n_par);
             parallel_ranges(n_par, [&](uint64_t lo, uint64_t hi) {
                 for (uint64_t p = lo; p < hi; ++p)
                     counts[p] = canon::rows::children<canon::rows::COUNT>(prm, level.data() + p * n, (int)n,
-                                                                         nullptr, 0);
+                                                                         nullptr, 0, hgens.data() + p * NG,
+                                                                         hngens[p]);
             });
             offs.assign(n_par + 1, 0);
             for (uint64_t p = 0; p < n_par; ++p)
@@ -484,7 +506,7 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
             if (e != cudaSuccess)
                 return done(CANON_ECUDA, "count", e);
             rows_count_kernel<<<grid, GEN_TPB, 0, s>>>(prm, lev.p, (uint32_t)n_par, (int)n, dcounts.p, rcache.p,
-                                                       ticket.p);
+                                                       ticket.p, have_gens ? gens.p : nullptr, ngens.p);
             e = cudaGetLastError();
             if (e == cudaSuccess)
                 e = exclusive_scan(dcounts.p, n_par, doffs.p, sums, s);
@@ -554,7 +576,8 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 parallel_ranges(p1 - p0, [&](uint64_t lo, uint64_t hi) {
                     for (uint64_t p = p0 + lo; p < p0 + hi; ++p)
                         canon::rows::children<canon::rows::CHILD>(prm, level.data() + p * n, (int)n,
-                                                                  hcand.p + (offs[p] - base) * m, counts[p]);
+                                                                  hcand.p + (offs[p] - base) * m, counts[p],
+                                                                  hgens.data() + p * NG, hngens[p]);
                 });
                 e = cudaMemcpyAsync(cand.p, hcand.p, (size_t)ns * m * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
             } else {
@@ -565,7 +588,8 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 if (e != cudaSuccess)
                     return done(CANON_ECUDA, "children", e);
                 rows_emit_kernel<<<grid, GEN_TPB, 0, s>>>(prm, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, doffs.p,
-                                                          dcounts.p, rcache.p, cand.p, ticket.p);
+                                                          dcounts.p, rcache.p, cand.p, ticket.p,
+                                                          have_gens ? gens.p : nullptr, ngens.p);
                 e = cudaGetLastError();
                 if (e == cudaSuccess)
                     e = cudaStreamSynchronize(s);
@@ -633,6 +657,28 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
         host_valid = false;
         n_par = n_next;
         n = m;
+        // automorphisms of the new parents, which prune their children
+        have_gens = false;
+        if (n < v && n_par && n >= 2) {
+            e = gens.ensure((size_t)n_par * NG);
+            if (e == cudaSuccess)
+                e = ngens.ensure(n_par);
+            if (e != cudaSuccess)
+                return done(CANON_ENOMEM, "automorphism buffers", e);
+            cudaEventRecord(e0, s);
+            e = canon::launch_bibd_autgen((uint32_t)n_par, n, b, lev.p, gens.p, ngens.p, NG, c->cfg.max_trials,
+                                          ticket.p, c->num_sms, s);
+            cudaEventRecord(e1, s);
+            if (e == cudaSuccess)
+                e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess)
+                return done(CANON_ECUDA, "automorphisms", e);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            st.gen_seconds += ms * 1e-3;
+            ++c->launches;
+            have_gens = true;
+        }
     }
     if (n == v && n_par) {
         std::vector<uint64_t> rows((size_t)n_par * v), auts((size_t)n_par * 2);

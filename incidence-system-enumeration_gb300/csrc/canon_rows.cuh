@@ -11,6 +11,18 @@
 // rows 0..i-1 as they are, so a greater row i there means a greater matrix and
 // the child is not canonical.  Inside each orbit the 1s come first, so every
 // child is again in orbit normal form.
+//
+// Automorphisms of the parent prune children too (the grouping of row solutions by
+// the parent's automorphism group, CRowSolution::sortSolutionsByGroup(),
+// Source/RowSolution.h:325-383, with the group built by CPermutStorage::constructGroup()
+// and the orbit representative found by findSolutionIndex(), Source/PermutStorage.h:
+// 183-335).  An automorphism of the parent permutes its rows by sigma and its column
+// orbits along: the orbit whose columns hold 1s in the rows of a set P goes to the
+// orbit of the rows sigma(P).  Applied to a child it keeps the parent and moves the
+// new row's 1s from orbit to orbit, giving an isomorphic child; if that child's row
+// is greater (read orbit by orbit, more 1s first), the child is not the greatest of
+// its class and cannot be canonical.  Each automorphism given and its inverse are
+// tried; a subset of the group prunes less but never wrongly.
 #pragma once
 #include <cstddef>
 #include <cstdint>
@@ -33,10 +45,16 @@ struct Params {
 // row alone at out[j].
 enum Emit { COUNT = 0, CHILD = 1, NEW_ROW = 2 };
 
+// at most this many automorphisms of a parent prune its children
+constexpr int AUT_GENS = 8;
+
 // Children of one parent with n rows (bit c of word i = row i, column c), in a
 // fixed order: orbits left to right, more 1s first.  Returns their number.
+// gens: ngens automorphisms of the parent as row permutations (nibble i = the row
+// that goes to position i), or none.
 template <int EMIT>
-CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint64_t *out, uint32_t out_cap) {
+CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint64_t *out, uint32_t out_cap,
+                           const uint64_t *gens = nullptr, int ngens = 0) {
     const int b = d.b, k = d.k;
     uint8_t start[64], len[64], weight[64];
     uint8_t split[64];      // the first row in which orbit q differs from orbit q-1
@@ -67,6 +85,29 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
             ++norb;
             s = c;
         }
+    }
+    // the orbit map of every automorphism: orbit q (1s in the rows of ones[q]) goes to
+    // the orbit with 1s in the rows sigma(ones[q])
+    uint8_t omap[AUT_GENS][64];
+    int na = 0;
+    for (int a = 0; a < ngens && a < AUT_GENS; ++a) {
+        const uint64_t sg = gens[a];
+        bool good = true;
+        for (int t = 0; t < norb && good; ++t) {
+            unsigned img = 0;
+            for (int i = 0; i < n; ++i)
+                if ((ones[t] >> i) & 1u)
+                    img |= 1u << ((sg >> (4 * i)) & 15u);
+            int u = 0;
+            while (u < norb && ones[u] != img)
+                ++u;
+            if (u == norb)
+                good = false;      // not an automorphism of this parent: not used
+            else
+                omap[na][t] = (uint8_t)u;
+        }
+        if (good)
+            ++na;
     }
     // hi/lo: the most / least 1s orbit q can take (full orbits none, orbits whose
     // columns need every remaining row all); rc/rn: the sums of hi/lo over the
@@ -121,6 +162,28 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
                         }
                         c += x[t];
                         ri += ((ones[t] >> i) & 1u) ? len[t] : 0;
+                    }
+                }
+                // an automorphism of the parent (or its inverse) that makes the row greater
+                for (int a = 0; ok && a < na; ++a) {
+                    for (int dir = 0; dir < 2 && ok; ++dir) {
+                        for (int t = 0; t < norb; ++t) {
+                            // dir 0: image row y[omap[t]] = x[t]; dir 1: y[t] = x[omap[t]]
+                            int yt;
+                            if (dir) {
+                                yt = x[omap[a][t]];
+                            } else {
+                                yt = -1;
+                                for (int u = 0; u < norb; ++u)
+                                    if (omap[a][u] == t)
+                                        yt = x[u];
+                            }
+                            if (yt != x[t]) {
+                                if (yt > x[t])
+                                    ok = false;
+                                break;
+                            }
+                        }
                     }
                 }
                 if (ok) {

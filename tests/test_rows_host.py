@@ -81,3 +81,56 @@ def test_children_are_normal_and_non_increasing(gen):
                 C = unpack(child, 35)
                 assert oracle.bibd_is_normal(C)
                 assert tuple(C[-1]) <= tuple(C[-2])
+
+
+def children_aut(L, params, parent, gens):
+    n = len(parent)
+    p = np.ascontiguousarray(parent, np.uint64)
+    g = np.ascontiguousarray(gens, np.uint64)
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    f = L.rows_children_aut
+    f.argtypes = [ctypes.c_int] * 5 + [u64p, ctypes.c_int, u64p, ctypes.c_uint32, u64p, ctypes.c_int]
+    f.restype = ctypes.c_uint32
+    gp = g.ctypes.data_as(u64p) if len(g) else None
+    cnt = f(*params, p.ctypes.data_as(u64p), n, None, 0, gp, len(g))
+    out = np.zeros(max(cnt, 1) * (n + 1), np.uint64)
+    assert f(*params, p.ctypes.data_as(u64p), n, out.ctypes.data_as(u64p), cnt, gp, len(g)) == cnt
+    return out[: cnt * (n + 1)].reshape(cnt, n + 1)
+
+
+def row_automorphisms(M):
+    """The row automorphisms that the oracle's TestCanonicity finds (t_outRowPermute),
+    nibble-packed: nibble i = the row that goes to position i."""
+    o = oracle.bibd_test(M, oracle.SAVE_ROW_PERM | oracle.SAVE_AUT_ROWS, perm_cap=64)
+    perms = o["perms"][1:] if len(o["perms"]) else []
+    return [sum(int(x) << (4 * i) for i, x in enumerate(p)) for p in perms]
+
+
+@pytest.mark.parametrize("key", ["7,14,6,3,2", "8,14,7,4,3", "9,12,4,3,1", "10,15,6,4,2", "13,26,6,3,1",
+                                 "16,20,5,4,1"])
+def test_automorphism_pruning_keeps_the_designs_and_drops_candidates(gen, key):
+    """Children that an automorphism of their parent maps to a greater child are not
+    generated: the same designs, with fewer candidates to check."""
+    params = tuple(map(int, key.split(",")))
+    v, b, r = params[:3]
+    level = [np.array([(1 << r) - 1], np.uint64)]
+    cand_plain = cand_aut = 0
+    for m in range(2, v + 1):
+        nxt = []
+        for parent in level:
+            gens = row_automorphisms(unpack(parent, b)) if len(parent) > 1 else []
+            cand_plain += len(children(gen, params, parent))
+            kids = children_aut(gen, params, parent, gens)
+            cand_aut += len(kids)
+            for child in kids:
+                M = unpack(child, b)
+                flags = (oracle.SAVE_ROW_PERM | oracle.SAVE_ROW_TO_CHANGE) if m == v else 0
+                o = oracle.bibd_test(M, flags)
+                if o["canonical"]:
+                    nxt.append((child, o["aut"]))
+        level = [c for c, _ in nxt]
+    got = {unpack(c, b).tobytes(): a for c, a in nxt}
+    ref, _ = oracle.bibd_enumerate(*params)
+    assert got == {M.tobytes(): a for M, a in ref}
+    assert cand_aut <= cand_plain
+    print(key, cand_plain, cand_aut)
