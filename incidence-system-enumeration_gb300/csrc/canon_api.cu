@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -176,6 +177,29 @@ cudaError_t compute_orders(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, con
 
 }  // namespace
 
+namespace {
+
+// fn(lo, hi) over [0, n) on up to 16 host threads, in contiguous ranges (small
+// batches on the calling thread): the copy into the pinned staging buffers and the
+// work descriptors of a large batch
+template <typename F>
+void pack_parallel(uint64_t n, F fn) {
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt > 16)
+        nt = 16;
+    if (n < (1u << 16) || nt < 2) {
+        fn((uint64_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t)
+        th.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
+    for (auto &x : th)
+        x.join();
+}
+
+}  // namespace
+
 extern "C" {
 
 canon_ctx *canon_create(const canon_cfg *cfg) {
@@ -293,17 +317,20 @@ int canon_submit_bibd(canon_ctx *c, const canon_bibd_batch *bt) {
         if (nr < 1 || nr > bt->v)
             return fail(c, CANON_EINVAL, "bibd batch: nrows out of range");
     }
-    std::memcpy(c->h_words + c->n_words, bt->rows, (size_t)bt->n * bt->v * sizeof(uint64_t));
-    for (uint32_t i = 0; i < bt->n; ++i) {
-        Item it{};
-        it.data_off = c->n_words + i * bt->v;
-        it.kind = canon::KIND_BIBD;
-        it.nrows = (uint8_t)(bt->nrows ? bt->nrows[i] : bt->v);
-        it.ncols = (uint8_t)bt->b;
-        it.flags = (uint8_t)bt->flags;
-        it.out_idx = total + i;
-        c->h_bitems[c->n_bitems + i] = it;
-    }
+    pack_parallel(bt->n, [&](uint64_t lo, uint64_t hi) {
+        std::memcpy(c->h_words + c->n_words + lo * bt->v, bt->rows + lo * bt->v,
+                    (size_t)(hi - lo) * bt->v * sizeof(uint64_t));
+        for (uint64_t i = lo; i < hi; ++i) {
+            Item it{};
+            it.data_off = c->n_words + (uint32_t)i * bt->v;
+            it.kind = canon::KIND_BIBD;
+            it.nrows = (uint8_t)(bt->nrows ? bt->nrows[i] : bt->v);
+            it.ncols = (uint8_t)bt->b;
+            it.flags = (uint8_t)bt->flags;
+            it.out_idx = total + (uint32_t)i;
+            c->h_bitems[c->n_bitems + i] = it;
+        }
+    });
     c->n_words += bt->n * bt->v;
     c->n_bitems += bt->n;
     c->item_kind.insert(c->item_kind.end(), bt->n, canon::KIND_BIBD);
@@ -331,17 +358,20 @@ int canon_submit_ksys(canon_ctx *c, const canon_ksys_batch *bt) {
         if (nr < 1 || nr > bt->rounds)
             return fail(c, CANON_EINVAL, "ksys batch: nrows out of range");
     }
-    std::memcpy(c->h_bytes + c->n_bytes, bt->data, bytes);
-    for (uint32_t i = 0; i < bt->n; ++i) {
-        Item it{};
-        it.data_off = c->n_bytes + i * bt->rounds * bt->np;
-        it.kind = canon::KIND_KSYS;
-        it.nrows = (uint8_t)(bt->nrows ? bt->nrows[i] : bt->rounds);
-        it.ncols = (uint8_t)bt->np;
-        it.flags = (uint8_t)bt->flags;
-        it.out_idx = total + i;
-        c->h_kitems[c->n_kitems + i] = it;
-    }
+    const uint64_t per = (uint64_t)bt->rounds * bt->np;
+    pack_parallel(bt->n, [&](uint64_t lo, uint64_t hi) {
+        std::memcpy(c->h_bytes + c->n_bytes + lo * per, bt->data + lo * per, (size_t)((hi - lo) * per));
+        for (uint64_t i = lo; i < hi; ++i) {
+            Item it{};
+            it.data_off = c->n_bytes + (uint32_t)(i * per);
+            it.kind = canon::KIND_KSYS;
+            it.nrows = (uint8_t)(bt->nrows ? bt->nrows[i] : bt->rounds);
+            it.ncols = (uint8_t)bt->np;
+            it.flags = (uint8_t)bt->flags;
+            it.out_idx = total + (uint32_t)i;
+            c->h_kitems[c->n_kitems + i] = it;
+        }
+    });
     c->n_bytes += (uint32_t)bytes;
     c->n_kitems += bt->n;
     c->item_kind.insert(c->item_kind.end(), bt->n, canon::KIND_KSYS);

@@ -367,10 +367,12 @@ class Context:
         self._check(self.lib.canon_submit_ksys(self.h, ctypes.byref(bt)))
         return n
 
-    def sync(self, allow_timeout=False, raw=False):
+    def sync(self, allow_timeout=False, raw=False, copy=True):
         """Runs canon_sync and copies the result arrays.  raw: |Aut| stays an (n, 2)
         uint64 array (low, high words) and the automorphism arena is not copied, so
-        no per-item Python work is done."""
+        no per-item Python work is done.  copy=False (with raw): the arrays are views
+        of the library's pinned result buffers, as the C API hands them out, valid
+        until the next sync or close of this context."""
         r = Results()
         rc = self.lib.canon_sync(self.h, ctypes.byref(r))
         if rc != CANON_OK and not (allow_timeout and rc == CANON_ETIMEOUT):
@@ -379,7 +381,8 @@ class Context:
         out = {"n": n, "kernel_ms": r.kernel_ms}
         if n and raw:
             def view(p, count, dt):
-                return np.ctypeslib.as_array(p, shape=(count,)).view(dt).copy()
+                a = np.ctypeslib.as_array(p, shape=(count,)).view(dt)
+                return a.copy() if copy else a
             out["canonical"] = view(r.canonical, n, np.uint8)
             out["status"] = view(r.status, n, np.uint8)
             out["witness"] = view(r.witness, n * 16, np.uint8).reshape(n, 16)
