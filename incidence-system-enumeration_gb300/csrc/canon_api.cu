@@ -398,9 +398,16 @@ int canon_sync(canon_ctx *c, canon_results *r) {
             cudaMemcpyAsync(c->d_bytes, c->h_bytes, c->n_bytes, cudaMemcpyHostToDevice, s);
         cudaEventRecord(c->ev0, s);
         if (c->n_bitems && c->n_kitems) {
-            // uneven batch: one persistent launch for both kinds
+            // uneven batch: one persistent launch for both kinds, sized by the widest
+            // incidence item
+            uint32_t mb = 0, mv = 0;
+            for (uint32_t i = 0; i < c->n_bitems; ++i) {
+                mb = std::max<uint32_t>(mb, c->h_bitems[i].ncols);
+                mv = std::max<uint32_t>(mv, c->h_bitems[i].nrows);
+            }
             e = canon::launch_mixed_check(c->d_bitems, c->n_bitems, c->d_kitems, c->n_kitems, c->d_words,
-                                          c->d_bytes, c->d_out, c->cfg.max_trials, c->d_ticket, c->num_sms, s);
+                                          c->d_bytes, c->d_out, c->cfg.max_trials, c->d_ticket, c->num_sms, s, mb,
+                                          mv);
             if (e != cudaSuccess)
                 return cuda_fail(c, e, "mixed check launch");
             ++c->launches;

@@ -129,9 +129,11 @@ cudaError_t launch_ksys_check(const Item *d_items, uint32_t n_items, const uint8
                               Outputs out, unsigned *d_ticket, int num_sms, cudaStream_t s);
 // one persistent launch over a mixed batch: k-system items (warp each) then incidence items (thread each);
 // d_ticket: two device words
+// (max_b, max_v: the widest incidence item, which sizes the per-thread state)
 cudaError_t launch_mixed_check(const Item *d_bitems, uint32_t nb, const Item *d_kitems, uint32_t nk,
                                const uint64_t *d_words, const uint8_t *d_bytes, Outputs out,
-                               uint64_t max_trials, unsigned *d_ticket, int num_sms, cudaStream_t s);
+                               uint64_t max_trials, unsigned *d_ticket, int num_sms, cudaStream_t s,
+                               uint32_t max_b = 63, uint32_t max_v = 16);
 cudaError_t ksys_upload_tables();
 
 }  // namespace canon

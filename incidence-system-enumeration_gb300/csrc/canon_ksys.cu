@@ -46,17 +46,21 @@ __global__ void __launch_bounds__(KTPB) ksys_kernel(const Item *__restrict__ ite
 constexpr int MTPB = bibd::TPB;     // 64: the per-thread shared-memory layout of the incidence checker
 constexpr int MW = MTPB / 32;
 
+// BCAP / VCAP bound the columns / rows of every incidence item of the launch, so the
+// per-thread state is sized by the launch's widest shape (v <= 15, b <= 35: 413 B,
+// 8 blocks of 64 per SM, against 6 for the general 16 x 63 layout).
+template <int BCAP, int VCAP>
 __global__ void __launch_bounds__(MTPB) mixed_kernel(const Item *__restrict__ bitems, uint32_t nb,
                                                      const Item *__restrict__ kitems, uint32_t nk,
                                                      const uint64_t *__restrict__ words,
                                                      const uint8_t *__restrict__ bytes, Outputs out,
                                                      uint64_t max_trials, unsigned *ticket) {
     __shared__ uint64_t s_seq[MW][16], s_part[MW][16], s_pair[MW][16];
-    __shared__ uint64_t s_rows[VMAX * MTPB];
-    __shared__ uint64_t s_lvl[(VMAX + 1) * MTPB];
-    __shared__ uint32_t s_vd[VMAX * MTPB];
-    __shared__ uint16_t s_cm[64 * MTPB];
-    __shared__ uint8_t s_pc[64 * MTPB];
+    __shared__ uint64_t s_rows[VCAP * MTPB];
+    __shared__ uint64_t s_lvl[(VCAP + 1) * MTPB];
+    __shared__ uint32_t s_vd[VCAP * MTPB];
+    __shared__ uint16_t s_cm[BCAP * MTPB];
+    __shared__ uint8_t s_pc[BCAP * MTPB];
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u, tid = threadIdx.x;
     for (;;) {
         unsigned it = 0;
@@ -72,7 +76,15 @@ __global__ void __launch_bounds__(MTPB) mixed_kernel(const Item *__restrict__ bi
         const unsigned it = atomicAdd(ticket + 1, 1u);
         if (it >= nb)
             break;
-        bibd::check_item(sm, bitems[it], words, out, max_trials);
+        const Item item = bitems[it];
+        if (item.nrows > VCAP || item.ncols > BCAP) {
+            // wider than the launch was sized for (the launcher sizes it by the batch)
+            Item bad = item;
+            bad.kind = 0xFFu;
+            bibd::check_item(sm, bad, words, out, max_trials);
+            continue;
+        }
+        bibd::check_item(sm, item, words, out, max_trials);
     }
 }
 
@@ -80,14 +92,19 @@ __global__ void __launch_bounds__(MTPB) mixed_kernel(const Item *__restrict__ bi
 
 cudaError_t launch_mixed_check(const Item *d_bitems, uint32_t nb, const Item *d_kitems, uint32_t nk,
                                const uint64_t *d_words, const uint8_t *d_bytes, Outputs out,
-                               uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s) {
+                               uint64_t max_trials, unsigned *tk, int num_sms, cudaStream_t s, uint32_t max_b,
+                               uint32_t max_v) {
     if (!nb && !nk)
         return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s);
     if (e != cudaSuccess)
         return e;
+    const int shape = (max_v <= 15 && max_b <= 35) ? 0 : (max_b <= 40 ? 1 : 2);
+    const void *kfn = shape == 0 ? (const void *)mixed_kernel<35, 15>
+                      : shape == 1 ? (const void *)mixed_kernel<40, 16>
+                                   : (const void *)mixed_kernel<64, 16>;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mixed_kernel, MTPB, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, MTPB, 0);
     if (e != cudaSuccess)
         return e;
     if (per_sm < 1)
@@ -96,7 +113,12 @@ cudaError_t launch_mixed_check(const Item *d_bitems, uint32_t nb, const Item *d_
     const long need = (long)((nb + MTPB - 1) / MTPB) + (long)((nk + MW - 1) / MW);
     if (grid > need)
         grid = (int)need;
-    mixed_kernel<<<grid, MTPB, 0, s>>>(d_bitems, nb, d_kitems, nk, d_words, d_bytes, out, max_trials, tk);
+    if (shape == 0)
+        mixed_kernel<35, 15><<<grid, MTPB, 0, s>>>(d_bitems, nb, d_kitems, nk, d_words, d_bytes, out, max_trials, tk);
+    else if (shape == 1)
+        mixed_kernel<40, 16><<<grid, MTPB, 0, s>>>(d_bitems, nb, d_kitems, nk, d_words, d_bytes, out, max_trials, tk);
+    else
+        mixed_kernel<64, 16><<<grid, MTPB, 0, s>>>(d_bitems, nb, d_kitems, nk, d_words, d_bytes, out, max_trials, tk);
     return cudaGetLastError();
 }
 
