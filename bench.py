@@ -543,6 +543,20 @@ def run_learned(args):
     d_lab = ctx.alloc(2 * n_eval)
     ctx.label_first_rows(n_eval, V, B, G.RAW, d_rows, d_lab)
     lab = ctx.d2h(np.zeros(n_eval, np.uint16), d_lab)
+    # the bound on what any first-row order can save: the exact labels as the order
+    # (the rows that start a labeling of the canonical form first, as a perfect network
+    # would rank them)
+    bits = ((lab[:, None] >> np.arange(V, dtype=np.uint16)) & 1).astype(np.int64)
+    rank = np.argsort(-bits * 16 + np.arange(V)[None, :], axis=1, kind="stable").astype(np.uint64)
+    perfect = (rank << (np.uint64(4) * np.arange(V, dtype=np.uint64))[None, :]).sum(axis=1, dtype=np.uint64)
+    perfect |= np.uint64(0xF) << np.uint64(4 * V)      # nibble 15: the unused position
+    d_ord = ctx.alloc(8 * n_eval)
+    ctx.h2d(d_ord, perfect)
+    ctx.lexmax_nodes_bibd(n_eval, V, B, flags, d_rows, d_nodes, d_ord)
+    nd = ctx.d2h(np.zeros(n_eval, np.uint64), d_nodes).astype(np.float64)
+    node_stats["exact labels as the order"] = {"mean": float(nd.mean()), "canonical_mean": float(nd[canon_mask].mean()),
+                                               "noncanonical_mean": float(nd[~canon_mask].mean())}
+    ctx.free(d_ord)
     d_feat = ctx.alloc(65536 * V * 64 * 2)
     d_log = ctx.alloc(65536 * V * 4)
     ctx.mlp_features(65536, V, B, d_rows, d_feat)

@@ -767,15 +767,15 @@ int canon_tune_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t f
 }
 
 int canon_lexmax_nodes_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
-                            const uint64_t *d_rows, uint64_t *d_nodes) {
+                            const uint64_t *d_rows, uint64_t *d_nodes, const uint64_t *d_orders) {
     if (!c || !d_rows || !d_nodes)
         return fail(c, CANON_EINVAL, "null argument");
     if (v < 1 || v > canon::VMAX || b < 1 || b > canon::BMAX)
         return fail(c, CANON_EINVAL, "nodes: need 1 <= v <= 16, 1 <= b <= 63");
     cudaSetDevice(c->device);
-    const uint64_t *orders = nullptr;
+    const uint64_t *orders = d_orders;
     cudaError_t e = cudaSuccess;
-    if (c->order_on) {
+    if (!orders && c->order_on) {
         // the learned first-row order, as canon_check_bibd_device applies it
         const size_t need = (size_t)n * 8 + 256;
         if (!c->d_orders_bytes || c->d_orders_bytes < need) {

@@ -200,7 +200,7 @@ def load_library(path=LIB_PATH):
     L.canon_generate_partial_bibd.argtypes = [u32, u32, u32, u32, u32, u32, u64, u32, u32, u64p, u8p,
                                               ctypes.POINTER(ctypes.c_uint32)]
     L.canon_generate_partial_ksys.argtypes = [u32, u32, u64, u32, u32, u8p, u8p]
-    L.canon_lexmax_nodes_bibd.argtypes = [vp, u32, u32, u32, u32, vp, vp]
+    L.canon_lexmax_nodes_bibd.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp]
     L.canon_measure_int_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.canon_canonize_ksys_binary.argtypes = [vp, u32, u32, u32, u8p, u8p, u64p]
     L.createCanonizer.argtypes = [ctypes.c_int, ctypes.c_int]
@@ -458,9 +458,10 @@ class Context:
         self._check(self.lib.canon_enumerate_bibd(self.h, v, b, r, k, lam, c, None, ctypes.byref(st)))
         return found, st
 
-    def lexmax_nodes_bibd(self, n, v, b, flags, d_rows, d_nodes):
-        """Lex-max nodes per matrix of the resident check's first pass (device array)."""
-        self._check(self.lib.canon_lexmax_nodes_bibd(self.h, n, v, b, flags, d_rows, d_nodes))
+    def lexmax_nodes_bibd(self, n, v, b, flags, d_rows, d_nodes, d_orders=None):
+        """Lex-max nodes per matrix of the resident check's first pass (device array);
+        d_orders: first-row orders (device, nibble-packed) or the installed / plain order."""
+        self._check(self.lib.canon_lexmax_nodes_bibd(self.h, n, v, b, flags, d_rows, d_nodes, d_orders))
 
     def measure_int_peak(self):
         """32-bit integer lane operations per second of this GPU (canon_measure_int_peak)."""

@@ -214,11 +214,12 @@ int canon_generate_sts_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint64_t s
 /* ---- measurement ----
  * Lex-max nodes visited per matrix by the search of the resident check's first pass
  * (its verdict and |Aut|), for n device-resident matrices: the work measure of the
- * check's integer roofline.  With a learned order installed (canon_set_ordering) the
- * search runs in that order, as canon_check_bibd_device runs it.  d_nodes: n device
- * words. */
+ * check's integer roofline.  d_orders (optional, n device words): the first-row order
+ * of every matrix, nibble-packed (nibble q = the row tried q-th); without it the
+ * search runs in the learned order when one is installed (canon_set_ordering), as
+ * canon_check_bibd_device runs it, else in the plain order.  d_nodes: n device words. */
 int canon_lexmax_nodes_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
-                            const uint64_t *d_rows, uint64_t *d_nodes);
+                            const uint64_t *d_rows, uint64_t *d_nodes, const uint64_t *d_orders);
 /* 32-bit integer lane operations per second that this GPU sustains on independent
  * XOR / ADD / shift chains (the peak of the check's integer roofline). */
 int canon_measure_int_peak(canon_ctx *ctx, double *lane_ops_per_s);
