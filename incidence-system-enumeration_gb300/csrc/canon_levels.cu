@@ -426,7 +426,7 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
     constexpr uint32_t NG = canon::rows::AUT_GENS;
     std::vector<uint64_t> hgens(NG, 0);     // automorphisms of the host level's parents
     std::vector<uint8_t> hngens(1, 0);
-    bool have_gens = false;
+    bool have_gens = false, aut_pruning = true;
     DevBuf<uint32_t> dcounts;
     DevBuf<uint8_t> can, status;
     DevBuf<unsigned> ticket, stop;
@@ -657,9 +657,12 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
         host_valid = false;
         n_par = n_next;
         n = m;
-        // automorphisms of the new parents, which prune their children
+        // automorphisms of the new parents, which prune their children.  Deeper levels
+        // hold fewer symmetric partial matrices; once under 2 % of a level's parents have
+        // a nontrivial automorphism the searches for them cost more than they prune, and
+        // the deeper levels go without.
         have_gens = false;
-        if (n < v && n_par && n >= 2) {
+        if (aut_pruning && n < v && n_par && n >= 2) {
             e = gens.ensure((size_t)n_par * NG);
             if (e == cudaSuccess)
                 e = ngens.ensure(n_par);
@@ -678,6 +681,15 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
             st.gen_seconds += ms * 1e-3;
             ++c->launches;
             have_gens = true;
+            std::vector<uint8_t> ng(n_par);
+            e = cudaMemcpy(ng.data(), ngens.p, n_par, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess)
+                return done(CANON_ECUDA, "automorphisms", e);
+            uint64_t with = 0;
+            for (uint8_t x : ng)
+                with += x != 0;
+            if (with * 50 < n_par)
+                aut_pruning = false;
         }
     }
     if (n == v && n_par) {
