@@ -2,9 +2,9 @@
 // scores every row of a matrix as the first row of the canonical labeling.
 //
 // Inference and the forward pass of training run on the tensor cores
-// (mma.sync m16n8k16, BF16 operands, FP32 accumulation), one warp per 16 rows;
-// the hidden activations stay in registers and feed the next layer as A
-// fragments.  The backward pass propagates through the same layers (the hidden
+// (mma.sync m16n8k16, BF16 operands, FP32 accumulation), one warp per 16 rows, the
+// weights staged once per block in shared memory; the hidden activations stay in
+// registers and feed the next layer as A fragments.  The backward pass propagates through the same layers (the hidden
 // gradient dH1 = dH2 * W2 also on the tensor cores), the weight gradients are
 // tiled FP32 reductions over the batch, and Adam keeps FP32 master weights from
 // which the BF16 copies are refreshed after every step.  No counterpart in the
@@ -51,10 +51,43 @@ struct MlpDev {
     const float *b3;           // [1]
 };
 
-// Forward pass of 16 rows per warp.  Writes logits; when h1/h2 are given also the
-// (BF16, post-ReLU) hidden activations for the backward pass.
-__global__ void mlp_forward_kernel(long n, const __nv_bfloat16 *__restrict__ x, MlpDev w, float *__restrict__ y,
-                                   __nv_bfloat16 *__restrict__ h1out, __nv_bfloat16 *__restrict__ h2out) {
+// The weights staged in shared memory once per block: W1 and W2 with their rows
+// padded by 8 BF16 (4 words), so that the 8 rows a B fragment load touches fall in 8
+// different banks; biases and w3 beside them.
+constexpr int W1_LD = IN + 8, W2_LD = HID + 8;
+constexpr size_t FWD_SMEM = (size_t)HID * W1_LD * 2 + (size_t)HID * W2_LD * 2 + (size_t)HID * 4 * 3 + 16;
+
+// two consecutive bf16 of a row of a staged matrix (leading dimension ld)
+__device__ __forceinline__ uint32_t lds2(const __nv_bfloat16 *m, int row, int ld, int col) {
+    return *reinterpret_cast<const uint32_t *>(m + row * ld + col);
+}
+
+// Forward pass of 16 rows per warp, the warps of a block sharing the staged weights.
+// Writes logits; when h1/h2 are given also the (BF16, post-ReLU) hidden activations
+// for the backward pass.
+__global__ void __launch_bounds__(128) mlp_forward_kernel(long n, const __nv_bfloat16 *__restrict__ x, MlpDev wg,
+                                                          float *__restrict__ y, __nv_bfloat16 *__restrict__ h1out,
+                                                          __nv_bfloat16 *__restrict__ h2out) {
+    extern __shared__ __align__(16) unsigned char fwd_smem[];
+    __nv_bfloat16 *sw1 = reinterpret_cast<__nv_bfloat16 *>(fwd_smem);
+    __nv_bfloat16 *sw2 = sw1 + HID * W1_LD;
+    float *sb1 = reinterpret_cast<float *>(sw2 + HID * W2_LD);
+    float *sb2 = sb1 + HID;
+    float *sw3 = sb2 + HID;
+    for (int i = threadIdx.x; i < HID * IN / 2; i += blockDim.x) {
+        const int r = i / (IN / 2), c = 2 * (i % (IN / 2));
+        *reinterpret_cast<uint32_t *>(sw1 + r * W1_LD + c) = *reinterpret_cast<const uint32_t *>(wg.w1 + r * IN + c);
+    }
+    for (int i = threadIdx.x; i < HID * HID / 2; i += blockDim.x) {
+        const int r = i / (HID / 2), c = 2 * (i % (HID / 2));
+        *reinterpret_cast<uint32_t *>(sw2 + r * W2_LD + c) = *reinterpret_cast<const uint32_t *>(wg.w2 + r * HID + c);
+    }
+    for (int i = threadIdx.x; i < HID; i += blockDim.x) {
+        sb1[i] = wg.b1[i];
+        sb2[i] = wg.b2[i];
+        sw3[i] = __bfloat162float(wg.w3[i]);
+    }
+    __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, tg = lane & 3;
     const long tiles = (n + 15) / 16;
     for (long tile = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < tiles;
@@ -75,11 +108,11 @@ __global__ void mlp_forward_kernel(long n, const __nv_bfloat16 *__restrict__ x, 
             float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
-                const uint32_t b0 = ld2(w.w1, HID, 8 * j + g, IN, 16 * t + 2 * tg);
-                const uint32_t b1 = ld2(w.w1, HID, 8 * j + g, IN, 16 * t + 8 + 2 * tg);
+                const uint32_t b0 = lds2(sw1, 8 * j + g, W1_LD, 16 * t + 2 * tg);
+                const uint32_t b1 = lds2(sw1, 8 * j + g, W1_LD, 16 * t + 8 + 2 * tg);
                 mma_bf16(acc, a[t], b0, b1);
             }
-            const float bb0 = w.b1[8 * j + 2 * tg], bb1 = w.b1[8 * j + 2 * tg + 1];
+            const float bb0 = sb1[8 * j + 2 * tg], bb1 = sb1[8 * j + 2 * tg + 1];
             h1[j][0] = pack_bf16(fmaxf(acc[0] + bb0, 0.f), fmaxf(acc[1] + bb1, 0.f));
             h1[j][1] = pack_bf16(fmaxf(acc[2] + bb0, 0.f), fmaxf(acc[3] + bb1, 0.f));
             if (h1out) {
@@ -97,11 +130,11 @@ __global__ void mlp_forward_kernel(long n, const __nv_bfloat16 *__restrict__ x, 
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
                 const uint32_t af[4] = {h1[2 * t][0], h1[2 * t][1], h1[2 * t + 1][0], h1[2 * t + 1][1]};
-                const uint32_t b0 = ld2(w.w2, HID, 8 * j + g, HID, 16 * t + 2 * tg);
-                const uint32_t b1 = ld2(w.w2, HID, 8 * j + g, HID, 16 * t + 8 + 2 * tg);
+                const uint32_t b0 = lds2(sw2, 8 * j + g, W2_LD, 16 * t + 2 * tg);
+                const uint32_t b1 = lds2(sw2, 8 * j + g, W2_LD, 16 * t + 8 + 2 * tg);
                 mma_bf16(acc, af, b0, b1);
             }
-            const float bb0 = w.b2[8 * j + 2 * tg], bb1 = w.b2[8 * j + 2 * tg + 1];
+            const float bb0 = sb2[8 * j + 2 * tg], bb1 = sb2[8 * j + 2 * tg + 1];
             const uint32_t p0 = pack_bf16(fmaxf(acc[0] + bb0, 0.f), fmaxf(acc[1] + bb1, 0.f));
             const uint32_t p1 = pack_bf16(fmaxf(acc[2] + bb0, 0.f), fmaxf(acc[3] + bb1, 0.f));
             if (h2out) {
@@ -110,7 +143,7 @@ __global__ void mlp_forward_kernel(long n, const __nv_bfloat16 *__restrict__ x, 
                 if (r0 + g + 8 < n)
                     *reinterpret_cast<uint32_t *>(h2out + (r0 + g + 8) * HID + 8 * j + 2 * tg) = p1;
             }
-            const float w30 = __bfloat162float(w.w3[8 * j + 2 * tg]), w31 = __bfloat162float(w.w3[8 * j + 2 * tg + 1]);
+            const float w30 = sw3[8 * j + 2 * tg], w31 = sw3[8 * j + 2 * tg + 1];
             part0 += bf_lo(p0) * w30 + bf_hi(p0) * w31;
             part1 += bf_lo(p1) * w30 + bf_hi(p1) * w31;
         }
@@ -120,9 +153,9 @@ __global__ void mlp_forward_kernel(long n, const __nv_bfloat16 *__restrict__ x, 
         part1 += __shfl_xor_sync(0xFFFFFFFFu, part1, 2);
         if (tg == 0) {
             if (r0 + g < n)
-                y[r0 + g] = part0 + w.b3[0];
+                y[r0 + g] = part0 + wg.b3[0];
             if (r0 + g + 8 < n)
-                y[r0 + g + 8] = part1 + w.b3[0];
+                y[r0 + g + 8] = part1 + wg.b3[0];
         }
     }
 }
@@ -389,13 +422,19 @@ cudaError_t forward(long n, const void *x, const void *w1, const float *b1, cons
                     const void *w3, const float *b3, float *y, void *h1, void *h2, int num_sms, cudaStream_t s) {
     MlpDev w{(const __nv_bfloat16 *)w1, b1, (const __nv_bfloat16 *)w2, b2, (const __nv_bfloat16 *)w3, b3};
     const long tiles = (n + 15) / 16;
+    // a persistent grid (the staged weights are loaded once per block): 4 blocks per SM
     long grid = (tiles + 3) / 4;
-    if (grid > 32L * num_sms)
-        grid = 32L * num_sms;
+    if (grid > 4L * num_sms)
+        grid = 4L * num_sms;
     if (grid < 1)
         grid = 1;
-    mlp_forward_kernel<<<(int)grid, 128, 0, s>>>(n, (const __nv_bfloat16 *)x, w, y, (__nv_bfloat16 *)h1,
-                                                  (__nv_bfloat16 *)h2);
+    // above 48 KB of dynamic shared memory a kernel must opt in (per device: set on every launch)
+    const cudaError_t e = cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)FWD_SMEM);
+    if (e != cudaSuccess)
+        return e;
+    mlp_forward_kernel<<<(int)grid, 128, FWD_SMEM, s>>>(n, (const __nv_bfloat16 *)x, w, y, (__nv_bfloat16 *)h1,
+                                                         (__nv_bfloat16 *)h2);
     return cudaGetLastError();
 }
 
