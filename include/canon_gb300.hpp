@@ -143,4 +143,24 @@ private:
     uint32_t np_;
 };
 
+// RAII owner of the reference's plugin handle (createCanonizer / runCanonizer /
+// releaseCanonizer, k-Factorization/Utils/Include/CDTools.h:9-11).
+class Canonizer {
+public:
+    Canonizer(int v, int k) : h_(createCanonizer(v, k)) {
+        if (!h_)
+            throw Error(CANON_EINVAL, "createCanonizer failed (k = 2, even v in 6..16, a GPU)");
+    }
+    ~Canonizer() { releaseCanonizer(h_); }
+    Canonizer(const Canonizer &) = delete;
+    Canonizer &operator=(const Canonizer &) = delete;
+    // the canonical binary matrix of the first iDay rounds (all when iDay <= 0), owned here
+    const unsigned char *run(const unsigned char *pMatrix, int k, int iDay = 0) {
+        return runCanonizer(h_, pMatrix, k, iDay);
+    }
+
+private:
+    void *h_;
+};
+
 }  // namespace canon_gb300
