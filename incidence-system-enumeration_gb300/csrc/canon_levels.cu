@@ -426,7 +426,7 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
     constexpr uint32_t NG = canon::rows::AUT_GENS;
     std::vector<uint64_t> hgens(NG, 0);     // automorphisms of the host level's parents
     std::vector<uint8_t> hngens(1, 0);
-    bool have_gens = false, aut_pruning = true;
+    bool have_gens = false, aut_pruning = (c->cfg.options & CANON_OPT_AUT_PRUNE) != 0;
     DevBuf<uint32_t> dcounts;
     DevBuf<uint8_t> can, status;
     DevBuf<unsigned> ticket, stop;

@@ -75,7 +75,10 @@ class CanonError(RuntimeError):
 class Cfg(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("max_items", ctypes.c_uint32),
                 ("max_words", ctypes.c_uint32), ("aut_cap", ctypes.c_uint32),
-                ("max_trials", ctypes.c_uint64)]
+                ("max_trials", ctypes.c_uint64), ("options", ctypes.c_uint32)]
+
+
+OPT_AUT_PRUNE = 0x1
 
 
 class BibdBatch(ctypes.Structure):
@@ -321,9 +324,9 @@ def unpack_rows(words, b):
 class Context:
     """One engine context (one CUDA stream) on one GPU."""
 
-    def __init__(self, device=0, max_items=1 << 16, max_words=0, aut_cap=64, max_trials=0):
+    def __init__(self, device=0, max_items=1 << 16, max_words=0, aut_cap=64, max_trials=0, options=0):
         self.lib = load_library()
-        cfg = Cfg(device, max_items, max_words, aut_cap, max_trials)
+        cfg = Cfg(device, max_items, max_words, aut_cap, max_trials, options)
         self.h = self.lib.canon_create(ctypes.byref(cfg))
         if not self.h:
             raise CanonError(CANON_ENODEV, "canon_create failed (no GPU?)")

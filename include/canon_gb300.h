@@ -96,7 +96,15 @@ typedef struct {
     uint32_t max_words;       /* capacity: 64-bit input words per sync (0 = 16*max_items) */
     uint32_t aut_cap;         /* automorphisms kept per matrix when CANON_SAVE_AUTS (0 = 64) */
     uint64_t max_trials;      /* per-matrix trial budget (0 = 1<<28) */
+    uint32_t options;         /* CANON_OPT_* bits (0 = none) */
 } canon_cfg;
+
+/* canon_enumerate_bibd prunes the children of every parent with the parent's
+ * automorphisms (the grouping of row solutions by CRowSolution::sortSolutionsByGroup(),
+ * Source/RowSolution.h:325-383): the same designs from fewer candidates, at the price of
+ * one automorphism search per parent of the shallow levels, whose latency outweighs the
+ * saving on the families measured; hence an option. */
+#define CANON_OPT_AUT_PRUNE 0x1u
 
 /* BIBD / incidence-system batch: n matrices of b columns (b <= 63), v rows each
  * (v <= 16), row j of matrix i at rows[i*v + j] with bit c = column c.

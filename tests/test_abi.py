@@ -50,7 +50,7 @@ def test_create_without_gpu_fails_cleanly():
         return
     import ise_gb300
     lib = ise_gb300.load_library()
-    cfg = ise_gb300.Cfg(0, 16, 0, 4, 0)
+    cfg = ise_gb300.Cfg(0, 16, 0, 4, 0, 0)
     assert not lib.canon_create(ctypes.byref(cfg))
 
 

@@ -87,3 +87,21 @@ def test_k10_results_table(ctx):
     text = G.report_ksys([R for R, _ in found], [a for _, a in found])
     with open(os.path.join(cases.GOLDEN, "k10_results_table.txt")) as f:
         assert text == f.read()
+
+
+@pytest.mark.parametrize("key", ["7,14,6,3,2", "8,14,7,4,3", "10,15,6,4,2", "13,26,6,3,1", "16,20,5,4,1"])
+def test_automorphism_pruning_keeps_the_designs(key):
+    """With CANON_OPT_AUT_PRUNE the children that an automorphism of their parent maps
+    to a greater child are not generated: the same designs and |Aut|, fewer checks."""
+    import ise_gb300 as G
+    params = tuple(map(int, key.split(",")))
+    plain = G.Context(max_items=1 << 18)
+    pruned = G.Context(max_items=1 << 18, options=G.OPT_AUT_PRUNE)
+    try:
+        f0, s0 = plain.enumerate_bibd(*params)
+        f1, s1 = pruned.enumerate_bibd(*params)
+    finally:
+        plain.close()
+        pruned.close()
+    assert {M.tobytes(): a for M, a in f1} == {M.tobytes(): a for M, a in f0}
+    assert s1.checks < s0.checks
