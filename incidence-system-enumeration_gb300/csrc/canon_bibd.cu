@@ -104,7 +104,15 @@ __global__ void __launch_bounds__(TPB) bibd_max_kernel(uint32_t n_items, uint32_
         if (!load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW)) {
             st = ST_BADINPUT;
         } else {
-            max_search(sm, v, b, max_nodes, mo, orders ? orders[it] : ID16);
+            const uint64_t o0 = orders ? orders[it] : ID16;
+            max_search(sm, v, b, max_nodes < CLIMB_CAP ? max_nodes : CLIMB_CAP, mo, o0);
+            if (mo.timeout && max_nodes > CLIMB_CAP) {
+                // the verdict and |Aut(M)| (= |Aut| of the canonical form) with the bound kept at M
+                load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW);
+                max_search(sm, v, b, max_nodes - CLIMB_CAP, mo, o0, true, false, 0xFFFFu, nullptr, 0xFFFFu, nullptr, 0,
+                           true);
+                mo.nodes += CLIMB_CAP;
+            }
             if (mo.timeout)
                 st = ST_TIMEOUT;
         }
@@ -252,10 +260,20 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
             finish(ST_TIMEOUT);
             continue;
         }
+        if (!st.aut_only && st.nodes > CLIMB_CAP) {
+            // start again with the bound kept at M: this node becomes the new root
+            load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW);
+            conv_start(st, v, orders ? orders[it] : ID16, true);
+            st.nodes = CLIMB_CAP + 1;
+        }
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.i, b, b, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        bool greater = false;
+        const int state = eval_node_uniform(sm, st.i, b, b, tied, arr, hb, hb ? R_(st.i) : 0ull, st.aut_only,
+                                            &greater);
+        if (greater)
+            st.improved = true;          // M is not canonical; the bound stays M
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }
@@ -276,6 +294,7 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
     const unsigned tid = threadIdx.x;
     SmemMax sm{s_rows + tid, s_lvl + tid, nullptr, s_cm + tid, s_vd + tid};
     ConvState st{};
+    Item cur{};
     uint32_t o_i = 0;
     unsigned b = 1;
     bool have = false, done = false;
@@ -306,6 +325,7 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
                 b = item.ncols;
                 o_i = item.out_idx;
                 conv_start(st, n >= 1 && n <= VCAP ? n : 1, ID16);
+                cur = item;
                 have = true;
                 if (item.kind != KIND_BIBD || n < 1 || n > VCAP || b < 1 || b > BMAX || b > BCAP || b > bt ||
                     !load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW)) {
@@ -334,10 +354,22 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
             finish(ST_TIMEOUT);
             continue;
         }
+        if (!st.aut_only && st.nodes > CLIMB_CAP) {
+            // start again with the bound kept at M: this node becomes the new root
+            load_rows(sm, words + cur.data_off, cur.nrows, b, cur.flags & F_RAW);
+            for (unsigned c = b; c < bt; ++c)
+                CM_(c) = 0;
+            conv_start(st, cur.nrows, ID16, true);
+            st.nodes = CLIMB_CAP + 1;
+        }
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        bool greater = false;
+        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull, st.aut_only,
+                                            &greater);
+        if (greater)
+            st.improved = true;          // M is not canonical; the bound stays M
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }
@@ -401,7 +433,13 @@ __global__ void __launch_bounds__(TPB) bibd_items_max_kernel(const Item *__restr
             !load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW)) {
             st = ST_BADINPUT;
         } else {
-            max_search(sm, n, b, max_nodes, mo);
+            max_search(sm, n, b, max_nodes < CLIMB_CAP ? max_nodes : CLIMB_CAP, mo);
+            if (mo.timeout && max_nodes > CLIMB_CAP) {
+                load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW);
+                max_search(sm, n, b, max_nodes - CLIMB_CAP, mo, ID16, true, false, 0xFFFFu, nullptr, 0xFFFFu, nullptr, 0,
+                           true);
+                mo.nodes += CLIMB_CAP;
+            }
             if (mo.timeout)
                 st = ST_TIMEOUT;
         }

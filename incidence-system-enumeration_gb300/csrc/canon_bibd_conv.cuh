@@ -37,9 +37,12 @@ namespace {
 // widest matrix of a mixed launch).  Columns b..bt-1 hold no 1 (CM_() is 0 there)
 // and each closes an orbit of its own, so they change neither the row nor the
 // comparison.
+// aut_only: instead of the greatest row, the rows whose best arrangement equals the
+// bound's row (M's) stay tied; *greater is set if a row's arrangement beats it.
 template <typename S>
 __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned bt, unsigned &tied,
-                                                 uint64_t &arr, bool have_bound, uint64_t bound) {
+                                                 uint64_t &arr, bool have_bound, uint64_t bound,
+                                                 bool aut_only = false, bool *greater = nullptr) {
     const uint64_t lvl = L_(lv);
     // bit p: column p closes an orbit (the next column starts one, or p is the last)
     const uint64_t ends = (lvl >> 1) | (~0ull << (b - 1));
@@ -57,22 +60,48 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
         t = p4 & carry; p4 ^= carry; carry = t;
         p5 ^= carry;
         if ((ends >> p) & 1u) {
-            unsigned cstar = 0;
-            t = t0 & p5; if (t) { t0 = t; cstar |= 32u; }
-            t = t0 & p4; if (t) { t0 = t; cstar |= 16u; }
-            t = t0 & p3; if (t) { t0 = t; cstar |= 8u; }
-            t = t0 & p2; if (t) { t0 = t; cstar |= 4u; }
-            t = t0 & p1; if (t) { t0 = t; cstar |= 2u; }
-            t = t0 & p0; if (t) { t0 = t; cstar |= 1u; }
-            a |= ((1ull << cstar) - 1ull) << s;
-            if (state == 0 && have_bound) {
+            if (aut_only) {
+                // compare every tied row's count with M's: greater rows are recorded and
+                // dropped, smaller ones dropped, equal ones kept
                 const uint64_t rng = ((2ull << p) - 1ull) & ~((1ull << s) - 1ull);
                 const unsigned cb = __popcll(bound & rng);
-                state = cstar > cb ? 1 : (cstar < cb ? 2 : 0);
+                const unsigned pl[6] = {p0, p1, p2, p3, p4, p5};
+                unsigned gt = 0, eq = t0;
+#pragma unroll
+                for (int k = 5; k >= 0; --k) {
+                    if ((cb >> k) & 1u) {
+                        eq &= pl[k];
+                    } else {
+                        gt |= eq & pl[k];
+                        eq &= ~pl[k];
+                    }
+                }
+                if (gt)
+                    *greater = true;
+                t0 = eq;
+            } else {
+                unsigned cstar = 0;
+                t = t0 & p5; if (t) { t0 = t; cstar |= 32u; }
+                t = t0 & p4; if (t) { t0 = t; cstar |= 16u; }
+                t = t0 & p3; if (t) { t0 = t; cstar |= 8u; }
+                t = t0 & p2; if (t) { t0 = t; cstar |= 4u; }
+                t = t0 & p1; if (t) { t0 = t; cstar |= 2u; }
+                t = t0 & p0; if (t) { t0 = t; cstar |= 1u; }
+                a |= ((1ull << cstar) - 1ull) << s;
+                if (state == 0 && have_bound) {
+                    const uint64_t rng = ((2ull << p) - 1ull) & ~((1ull << s) - 1ull);
+                    const unsigned cb = __popcll(bound & rng);
+                    state = cstar > cb ? 1 : (cstar < cb ? 2 : 0);
+                }
             }
             p0 = p1 = p2 = p3 = p4 = p5 = 0;
             s = p + 1;
         }
+    }
+    if (aut_only) {
+        tied = t0;
+        arr = bound;
+        return t0 ? 0 : 2;
     }
     tied = t0;
     arr = a;
@@ -99,14 +128,17 @@ __device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, un
 }
 
 // the per-thread state of one lex-max search (max_search()'s locals)
+// aut_only: as max_search()'s, a greater node marks M not canonical and is pruned, so
+// the bound stays M and |Aut| comes from the pruned count of M's automorphisms.
 struct ConvState {
     uint64_t perm, orb, order, leaves, nodes, order0;
     unsigned n, valid, used, id_top, i, allrows;
     uint64_t nmask1;
-    bool improved, timeout;
+    bool improved, timeout, aut_only;
 };
 
-__device__ __forceinline__ void conv_start(ConvState &st, unsigned n, uint64_t order0) {
+__device__ __forceinline__ void conv_start(ConvState &st, unsigned n, uint64_t order0, bool aut_only = false) {
+    st.aut_only = aut_only;
     st.n = n;
     st.allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     st.nmask1 = (n >= 16) ? NIB1 : (NIB1 & ((1ull << (4 * n)) - 1ull));
@@ -131,7 +163,7 @@ template <typename S>
 __device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsigned &ref_x) {
     const unsigned n = st.n;
     for (;;) {
-        const bool pr = !st.improved;
+        const bool pr = st.aut_only || !st.improved;
         unsigned i = st.i;
         unsigned rem = VD_(i);
         if (pr && st.id_top >= i) {
@@ -224,7 +256,9 @@ __device__ __forceinline__ bool conv_after_eval(S sm, ConvState &st, int state, 
 }
 
 // |Aut| (the number of labelings reaching the canonical form) once the search is over
-__device__ __forceinline__ uint64_t conv_leaves(const ConvState &st) { return st.improved ? st.leaves : st.order; }
+__device__ __forceinline__ uint64_t conv_leaves(const ConvState &st) {
+    return (st.improved && !st.aut_only) ? st.leaves : st.order;
+}
 
 }  // namespace
 }  // namespace bibd

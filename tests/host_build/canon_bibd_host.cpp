@@ -89,7 +89,7 @@ extern "C" int emu_maxsearch_root2(const uint64_t *rows, unsigned n, unsigned b,
 #include "../../incidence-system-enumeration_gb300/csrc/canon_bibd_conv.cuh"
 // bt >= b: the columns walked (a mixed launch walks its widest item's columns)
 extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, unsigned bt, uint64_t order0,
-                                  uint64_t *leaves, uint64_t *nodes, uint8_t *improved) {
+                                  uint64_t *leaves, uint64_t *nodes, uint8_t *improved, int aut_only) {
     static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
     static uint16_t s_vd[VMAX * TPB];
     static uint16_t s_cm[64 * TPB];
@@ -98,8 +98,9 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
         return -1;
     for (unsigned c = b; c < bt; ++c)
         CM_(c) = 0;
+    // aut_only: 0 climb, 1 bound kept at M, 2 climb with the fallback after CLIMB_CAP nodes
     ConvState st;
-    conv_start(st, n, order0);
+    conv_start(st, n, order0, aut_only == 1);
     int ref_lv = -1;
     unsigned ref_x = 0;
     for (;;) {
@@ -107,10 +108,21 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
             refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
         if (++st.nodes > (1ull << 30))
             return -2;
+        if (aut_only == 2 && !st.aut_only && st.nodes > CLIMB_CAP) {
+            load_rows(sm, rows, n, b, F_RAW);
+            for (unsigned c = b; c < bt; ++c)
+                CM_(c) = 0;
+            conv_start(st, n, order0, true);
+            st.nodes = CLIMB_CAP + 1;
+        }
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        bool greater = false;
+        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull, st.aut_only,
+                                            &greater);
+        if (greater)
+            st.improved = true;          // M is not canonical; the bound stays M
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             break;
         if (!conv_next(sm, st, ref_lv, ref_x))
@@ -123,13 +135,13 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
 }
 
 extern "C" int emu_conv_search(const uint64_t *rows, unsigned n, unsigned b, uint64_t order0, uint64_t *leaves,
-                               uint64_t *nodes, uint8_t *improved) {
-    return emu_conv_search_bt(rows, n, b, b, order0, leaves, nodes, improved);
+                               uint64_t *nodes, uint8_t *improved, int aut_only) {
+    return emu_conv_search_bt(rows, n, b, b, order0, leaves, nodes, improved, aut_only);
 }
 
 // max_search() with a first-row order (the learned order's effect on the search)
 extern "C" int emu_maxsearch_order(const uint64_t *rows, unsigned n, unsigned b, uint64_t order0, uint64_t *leaves,
-                                   uint64_t *nodes, uint8_t *improved) {
+                                   uint64_t *nodes, uint8_t *improved, int aut_only) {
     static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
     static uint16_t s_vd[VMAX * TPB];
     static uint16_t s_cm[64 * TPB];
@@ -137,7 +149,16 @@ extern "C" int emu_maxsearch_order(const uint64_t *rows, unsigned n, unsigned b,
     if (!load_rows(sm, rows, n, b, F_RAW))
         return -1;
     MaxOut mo;
-    max_search(sm, n, b, 1ull << 30, mo, order0);
+    if (aut_only == 2) {
+        max_search(sm, n, b, CLIMB_CAP, mo, order0);
+        if (mo.timeout) {
+            load_rows(sm, rows, n, b, F_RAW);
+            max_search(sm, n, b, 1ull << 30, mo, order0, true, false, 0xFFFFu, nullptr, 0xFFFFu, nullptr, 0, true);
+            mo.nodes += CLIMB_CAP;
+        }
+    } else {
+        max_search(sm, n, b, 1ull << 30, mo, order0, true, false, 0xFFFFu, nullptr, 0xFFFFu, nullptr, 0, aut_only != 0);
+    }
     *leaves = mo.leaves; *nodes = mo.nodes; *improved = mo.improved;
     return mo.timeout ? -2 : 0;
 }
