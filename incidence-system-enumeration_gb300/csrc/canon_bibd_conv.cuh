@@ -15,8 +15,9 @@
 // instruction (5.5 of 32 lanes active on STS(15)); here the heavy part runs with
 // every active lane.
 //
-// The search tree, the node count, the verdict and |Aut| are those of max_search()
-// with automorphism pruning (prune = true, stop_on_improve = false, all first rows):
+// Until restart_after nodes (see ConvState), the search tree and node count are those
+// of max_search() with automorphism pruning (prune = true, stop_on_improve = false, all
+// first rows); the verdict and |Aut| always are:
 //   - node evaluation: the greatest arranged row over the unused rows, orbit by
 //     orbit, bit-sliced over the rows (the comparison of checkColOrbit(),
 //     Source/CanonicityChecker.cpp:191-223), compared with the bound as it is built;
@@ -37,12 +38,9 @@ namespace {
 // widest matrix of a mixed launch).  Columns b..bt-1 hold no 1 (CM_() is 0 there)
 // and each closes an orbit of its own, so they change neither the row nor the
 // comparison.
-// aut_only: instead of the greatest row, the rows whose best arrangement equals the
-// bound's row (M's) stay tied; *greater is set if a row's arrangement beats it.
 template <typename S>
 __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned bt, unsigned &tied,
-                                                 uint64_t &arr, bool have_bound, uint64_t bound,
-                                                 bool aut_only = false, bool *greater = nullptr) {
+                                                 uint64_t &arr, bool have_bound, uint64_t bound) {
     const uint64_t lvl = L_(lv);
     // bit p: column p closes an orbit (the next column starts one, or p is the last)
     const uint64_t ends = (lvl >> 1) | (~0ull << (b - 1));
@@ -60,48 +58,22 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
         t = p4 & carry; p4 ^= carry; carry = t;
         p5 ^= carry;
         if ((ends >> p) & 1u) {
-            if (aut_only) {
-                // compare every tied row's count with M's: greater rows are recorded and
-                // dropped, smaller ones dropped, equal ones kept
+            unsigned cstar = 0;
+            t = t0 & p5; if (t) { t0 = t; cstar |= 32u; }
+            t = t0 & p4; if (t) { t0 = t; cstar |= 16u; }
+            t = t0 & p3; if (t) { t0 = t; cstar |= 8u; }
+            t = t0 & p2; if (t) { t0 = t; cstar |= 4u; }
+            t = t0 & p1; if (t) { t0 = t; cstar |= 2u; }
+            t = t0 & p0; if (t) { t0 = t; cstar |= 1u; }
+            a |= ((1ull << cstar) - 1ull) << s;
+            if (state == 0 && have_bound) {
                 const uint64_t rng = ((2ull << p) - 1ull) & ~((1ull << s) - 1ull);
                 const unsigned cb = __popcll(bound & rng);
-                const unsigned pl[6] = {p0, p1, p2, p3, p4, p5};
-                unsigned gt = 0, eq = t0;
-#pragma unroll
-                for (int k = 5; k >= 0; --k) {
-                    if ((cb >> k) & 1u) {
-                        eq &= pl[k];
-                    } else {
-                        gt |= eq & pl[k];
-                        eq &= ~pl[k];
-                    }
-                }
-                if (gt)
-                    *greater = true;
-                t0 = eq;
-            } else {
-                unsigned cstar = 0;
-                t = t0 & p5; if (t) { t0 = t; cstar |= 32u; }
-                t = t0 & p4; if (t) { t0 = t; cstar |= 16u; }
-                t = t0 & p3; if (t) { t0 = t; cstar |= 8u; }
-                t = t0 & p2; if (t) { t0 = t; cstar |= 4u; }
-                t = t0 & p1; if (t) { t0 = t; cstar |= 2u; }
-                t = t0 & p0; if (t) { t0 = t; cstar |= 1u; }
-                a |= ((1ull << cstar) - 1ull) << s;
-                if (state == 0 && have_bound) {
-                    const uint64_t rng = ((2ull << p) - 1ull) & ~((1ull << s) - 1ull);
-                    const unsigned cb = __popcll(bound & rng);
-                    state = cstar > cb ? 1 : (cstar < cb ? 2 : 0);
-                }
+                state = cstar > cb ? 1 : (cstar < cb ? 2 : 0);
             }
             p0 = p1 = p2 = p3 = p4 = p5 = 0;
             s = p + 1;
         }
-    }
-    if (aut_only) {
-        tied = t0;
-        arr = bound;
-        return t0 ? 0 : 2;
     }
     tied = t0;
     arr = a;
@@ -127,18 +99,28 @@ __device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, un
     }
 }
 
-// the per-thread state of one lex-max search (max_search()'s locals)
-// aut_only: as max_search()'s, a greater node marks M not canonical and is pruned, so
-// the bound stays M and |Aut| comes from the pruned count of M's automorphisms.
+// the per-thread state of one lex-max search (max_search()'s locals, and the restart)
+//
+// Restart.  Climbing, the search raises its bound to the canonical form C and then,
+// with the automorphism pruning off (the pruning holds for M's own automorphisms),
+// counts every labelling of C: a relabelled matrix whose C has a large group costs
+// 41K nodes (|Aut| 192) or 152K (|Aut| 20,160) against 6.2K on average.  So once
+// restart_after nodes are spent and the bound is a complete matrix (valid == n), the
+// search starts again on the bound: its rows become the matrix searched, the pruning
+// is on again, and the first matrix is remembered as rejected.  If the bound was C,
+// the new search is the pruned check of C (|Aut| from its orbit product); if not, it
+// climbs on and restarts again.  The verdict and |Aut| are those of the climb
+// (|Aut(M)| = |Aut(C)|); typical matrices finish before restart_after.
 struct ConvState {
-    uint64_t perm, orb, order, leaves, nodes, order0;
-    unsigned n, valid, used, id_top, i, allrows;
+    uint64_t perm, orb, order, leaves, nodes, order0, restart_after;
+    unsigned n, valid, used, id_top, i, allrows, b;
     uint64_t nmask1;
-    bool improved, timeout, aut_only;
+    bool improved, timeout, rejected;
 };
 
-__device__ __forceinline__ void conv_start(ConvState &st, unsigned n, uint64_t order0, bool aut_only = false) {
-    st.aut_only = aut_only;
+// a fresh search of the n rows in R_(); restart_after and b are the caller's
+__device__ __forceinline__ void conv_start(ConvState &st, unsigned n, uint64_t order0) {
+    st.rejected = false;
     st.n = n;
     st.allrows = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
     st.nmask1 = (n >= 16) ? NIB1 : (NIB1 & ((1ull << (4 * n)) - 1ull));
@@ -162,8 +144,18 @@ __device__ __forceinline__ void conv_start(ConvState &st, unsigned n, uint64_t o
 template <typename S>
 __device__ __forceinline__ bool conv_next(S sm, ConvState &st, int &ref_lv, unsigned &ref_x) {
     const unsigned n = st.n;
+    if (st.improved && st.valid == n && st.nodes > st.restart_after) {
+        // the bound is a complete matrix C > the searched one: search C from its root
+        build_levels(sm, n, st.b);
+        const uint64_t nodes = st.nodes;
+        conv_start(st, n, ID16);
+        st.nodes = nodes;
+        st.rejected = true;
+        ref_lv = -1;
+        return true;
+    }
     for (;;) {
-        const bool pr = st.aut_only || !st.improved;
+        const bool pr = !st.improved;
         unsigned i = st.i;
         unsigned rem = VD_(i);
         if (pr && st.id_top >= i) {
@@ -256,9 +248,10 @@ __device__ __forceinline__ bool conv_after_eval(S sm, ConvState &st, int state, 
 }
 
 // |Aut| (the number of labelings reaching the canonical form) once the search is over
-__device__ __forceinline__ uint64_t conv_leaves(const ConvState &st) {
-    return (st.improved && !st.aut_only) ? st.leaves : st.order;
-}
+__device__ __forceinline__ uint64_t conv_leaves(const ConvState &st) { return st.improved ? st.leaves : st.order; }
+
+// M is not canonical (a greater matrix was found in this search or one before it)
+__device__ __forceinline__ bool conv_rejected(const ConvState &st) { return st.improved || st.rejected; }
 
 }  // namespace
 }  // namespace bibd

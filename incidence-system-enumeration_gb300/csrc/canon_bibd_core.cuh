@@ -912,8 +912,14 @@ __device__ void max_search(S sm, unsigned n, unsigned b, uint64_t max_nodes, Max
 // PG(3,2) against 5.8K on average).  After this many nodes the pass starts again with the
 // bound kept at M (aut_only), where the pruning stays on; both give the same verdict and
 // |Aut|, and keeping M costs more on typical matrices (its tied tree is wider than the
-// canonical form's), so it is the fallback rather than the rule.
-constexpr uint64_t CLIMB_CAP = 32768;
+// canonical form's), so it is the fallback rather than the rule.  The cap sits above
+// the climbs of the next-largest STS(15) groups (|Aut| 192: about 41K nodes, where
+// keeping M takes 5K - 77K depending on the labelling).
+constexpr uint64_t CLIMB_CAP = 49152;
+
+// The converged search's restart threshold (canon_bibd_conv.cuh): typical STS(15) climbs
+// end within 10K nodes (6.2K on average), the climbs of large groups go on far longer.
+constexpr uint64_t RESTART_AFTER = 10000;
 
 // Trials the reference-order search may spend before the lex-max search decides:
 // a complete canonical matrix needs far more in the reference order (~52K for an

@@ -89,7 +89,7 @@ extern "C" int emu_maxsearch_root2(const uint64_t *rows, unsigned n, unsigned b,
 #include "../../incidence-system-enumeration_gb300/csrc/canon_bibd_conv.cuh"
 // bt >= b: the columns walked (a mixed launch walks its widest item's columns)
 extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, unsigned bt, uint64_t order0,
-                                  uint64_t *leaves, uint64_t *nodes, uint8_t *improved, int aut_only) {
+                                  uint64_t *leaves, uint64_t *nodes, uint8_t *improved, int mode) {
     static uint64_t s_rows[VMAX * TPB], s_lvl[(VMAX + 1) * TPB];
     static uint16_t s_vd[VMAX * TPB];
     static uint16_t s_cm[64 * TPB];
@@ -98,9 +98,12 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
         return -1;
     for (unsigned c = b; c < bt; ++c)
         CM_(c) = 0;
-    // aut_only: 0 climb, 1 bound kept at M, 2 climb with the fallback after CLIMB_CAP nodes
+    // mode: 0 climb, 1 restart after RESTART_AFTER nodes (the kernels' rule), 2 restart
+    // whenever the bound is complete and greater than the searched matrix
     ConvState st;
-    conv_start(st, n, order0, aut_only == 1);
+    conv_start(st, n, order0);
+    st.b = b;
+    st.restart_after = mode == 0 ? ~0ull : (mode == 1 ? RESTART_AFTER : 0);
     int ref_lv = -1;
     unsigned ref_x = 0;
     for (;;) {
@@ -108,21 +111,10 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
             refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
         if (++st.nodes > (1ull << 30))
             return -2;
-        if (aut_only == 2 && !st.aut_only && st.nodes > CLIMB_CAP) {
-            load_rows(sm, rows, n, b, F_RAW);
-            for (unsigned c = b; c < bt; ++c)
-                CM_(c) = 0;
-            conv_start(st, n, order0, true);
-            st.nodes = CLIMB_CAP + 1;
-        }
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        bool greater = false;
-        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull, st.aut_only,
-                                            &greater);
-        if (greater)
-            st.improved = true;          // M is not canonical; the bound stays M
+        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             break;
         if (!conv_next(sm, st, ref_lv, ref_x))
@@ -130,7 +122,7 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
     }
     *leaves = conv_leaves(st);
     *nodes = st.nodes;
-    *improved = st.improved;
+    *improved = conv_rejected(st);
     return 0;
 }
 

@@ -269,42 +269,52 @@ def test_search_split_by_first_row_combines_to_the_whole(host):
             assert aut == full["aut"]
 
 
-def _conv_vs_max(L, rows, n, b, order0=0xFEDCBA9876543210, aut_only=0):
+def _search(fn, rows, n, b, order0=0xFEDCBA9876543210, mode=0):
     u64 = ctypes.c_uint64
-    res = []
-    for fn in (L.emu_conv_search, L.emu_maxsearch_order):
-        leaves, nodes, imp = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint8()
-        rc = fn(rows.ctypes.data_as(ctypes.POINTER(u64)), n, b, ctypes.c_uint64(order0), ctypes.byref(leaves),
-                ctypes.byref(nodes), ctypes.byref(imp), aut_only)
-        assert rc == 0
-        res.append((leaves.value, nodes.value, imp.value))
-    return res
+    leaves, nodes, imp = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint8()
+    rc = fn(rows.ctypes.data_as(ctypes.POINTER(u64)), n, b, ctypes.c_uint64(order0), ctypes.byref(leaves),
+            ctypes.byref(nodes), ctypes.byref(imp), mode)
+    assert rc == 0
+    return leaves.value, nodes.value, imp.value
 
 
-def test_aut_of_m_mode_gives_the_same_verdict_and_order(host):
-    """The check's lex-max pass keeps the bound at M (a greater node marks M not
-    canonical and is pruned): same verdict and |Aut| as the search that climbs to the
-    canonical form, in both layouts, with far fewer nodes on symmetric non-canonical
-    matrices; the 80 STS(15) classes relabelled at random, and partial matrices."""
+def _conv_vs_max(L, rows, n, b, order0=0xFEDCBA9876543210, aut_only=0):
+    return [_search(L.emu_conv_search, rows, n, b, order0, 0),
+            _search(L.emu_maxsearch_order, rows, n, b, order0, aut_only)]
+
+
+def test_restart_and_aut_of_m_give_the_same_verdict_and_order(host):
+    """The converged lex-max pass restarts on its bound once it is a complete greater
+    matrix (after RESTART_AFTER nodes, or always); the thread-per-matrix pass falls back
+    to keeping the bound at M after CLIMB_CAP nodes.  Every mode gives the verdict and
+    |Aut| of the plain climb, with far fewer nodes on relabelled matrices of large
+    groups; the 80 STS(15) classes relabelled at random, and partial matrices."""
     rng = np.random.default_rng(80)
-    worst = {0: 0, 2: 0}
+    worst = {"climb": 0, "restart": 0, "cap": 0}
     for M, aut in cases.load_sts15():
         X = cases.permute_normalize(M, rng)
         r = np.ascontiguousarray(G.pack_rows(X), np.uint64)
-        climb, _ = _conv_vs_max(host, r, 15, 35)
+        climb, mclimb = _conv_vs_max(host, r, 15, 35)
+        assert climb == mclimb and climb[0] == aut
         for mode in (1, 2):
-            a, m = _conv_vs_max(host, r, 15, 35, aut_only=mode)
-            assert a == m
-            assert a[0] == climb[0] == aut and a[2] == climb[2]
-        worst[0] = max(worst[0], climb[1])
-        worst[2] = max(worst[2], a[1])
+            a = _search(host.emu_conv_search, r, 15, 35, mode=mode)
+            assert a[0] == aut and a[2] == climb[2]
+            m = _search(host.emu_maxsearch_order, r, 15, 35, mode=mode)
+            assert m[0] == aut and m[2] == climb[2]
+        worst["climb"] = max(worst["climb"], climb[1])
+        worst["restart"] = max(worst["restart"], _search(host.emu_conv_search, r, 15, 35, mode=1)[1])
+        worst["cap"] = max(worst["cap"], _search(host.emu_maxsearch_order, r, 15, 35, mode=2)[1])
         for k in (4, 7, 10):
             p = np.ascontiguousarray(r[:k])
-            c2, _ = _conv_vs_max(host, p, k, 35)
-            a2, m2 = _conv_vs_max(host, p, k, 35, aut_only=1)
-            assert a2 == m2 and a2[0] == c2[0] and a2[2] == c2[2]
-    # the fallback bounds the longest search (the relabelled PG(3,2): 151,636 nodes climbing)
-    assert worst[2] < worst[0]
+            c2 = _search(host.emu_conv_search, p, k, 35)
+            for mode in (1, 2):
+                a2 = _search(host.emu_conv_search, p, k, 35, mode=mode)
+                assert a2[0] == c2[0] and a2[2] == c2[2]
+            m2 = _search(host.emu_maxsearch_order, p, k, 35, mode=1)
+            assert m2[0] == c2[0] and m2[2] == c2[2]
+    # both bound the longest search (the relabelled PG(3,2): 151,636 nodes climbing)
+    assert worst["restart"] < worst["climb"] and worst["cap"] < worst["climb"]
+    print(worst)
 
 
 def test_converged_layout_walks_the_same_tree(host):
