@@ -254,9 +254,15 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
             break;
         if (!eval)
             continue;
-        // the node step: every lane with a node runs the same b-column passes
-        if (ref_lv >= 0)
-            refine_uniform(sm, (unsigned)ref_lv, ref_x, b);
+        // the node step: every lane with a node runs the same b-column passes (unrolled
+        // when the batch's b is the instance's column capacity)
+        const bool full = b == BCAP;
+        if (ref_lv >= 0) {
+            if (full)
+                refine_uniform<BCAP>(sm, (unsigned)ref_lv, ref_x, b);
+            else
+                refine_uniform(sm, (unsigned)ref_lv, ref_x, b);
+        }
         if (++st.nodes > max_nodes) {
             st.timeout = true;
             finish(ST_TIMEOUT);
@@ -265,7 +271,9 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.i, b, b, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        const uint64_t bnd = hb ? R_(st.i) : 0ull;
+        const int state = full ? eval_node_uniform<BCAP>(sm, st.i, b, b, tied, arr, hb, bnd)
+                               : eval_node_uniform(sm, st.i, b, b, tied, arr, hb, bnd);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }

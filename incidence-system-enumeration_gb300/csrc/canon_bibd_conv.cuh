@@ -38,9 +38,15 @@ namespace {
 // widest matrix of a mixed launch).  Columns b..bt-1 hold no 1 (CM_() is 0 there)
 // and each closes an orbit of its own, so they change neither the row nor the
 // comparison.
-template <typename S>
+// FB > 0: b == bt == FB, known at compile time (the loop is unrolled, every column's
+// shared-memory address and end test are constants)
+template <unsigned FB = 0, typename S>
 __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned bt, unsigned &tied,
                                                  uint64_t &arr, bool have_bound, uint64_t bound) {
+    if (FB) {
+        b = FB;
+        bt = FB;
+    }
     const uint64_t lvl = L_(lv);
     // bit p: column p closes an orbit (the next column starts one, or p is the last)
     const uint64_t ends = (lvl >> 1) | (~0ull << (b - 1));
@@ -49,6 +55,7 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
     int state = 0;
     unsigned p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
     unsigned s = 0;
+#pragma unroll(FB ? FB : 1)
     for (unsigned p = 0; p < bt; ++p) {
         unsigned carry = (unsigned)CM_(p) & t0, t;
         t = p0 & carry; p0 ^= carry; carry = t;
@@ -83,10 +90,13 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
 // the columns of level lv+1 after row x was taken at level lv: inside every orbit of
 // level lv, the columns with a 1 in row x first (one pass, a write pointer per orbit);
 // bt: the columns walked (columns past the matrix's own hold no 1 and never move)
-template <typename S>
+template <unsigned FB = 0, typename S>
 __device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, unsigned bt) {
+    if (FB)
+        bt = FB;
     const uint64_t starts = L_(lv);
     unsigned w = 0;
+#pragma unroll(FB ? FB : 1)
     for (unsigned p = 0; p < bt; ++p) {
         if ((starts >> p) & 1u)
             w = p;
