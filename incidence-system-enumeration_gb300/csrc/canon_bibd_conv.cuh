@@ -33,13 +33,18 @@ namespace bibd {
 namespace {
 
 // the greatest arranged row over `tied` at level lv, compared with `bound`:
-// 0 equal so far, 1 greater, 2 smaller (have_bound false: never compared, 0).
+// 0 equal, 1 greater, 2 smaller (have_bound false: never compared, 0).
 // b: the matrix's columns; bt >= b: the columns every lane of the launch walks (the
 // widest matrix of a mixed launch).  Columns b..bt-1 hold no 1 (CM_() is 0 there)
 // and each closes an orbit of its own, so they change neither the row nor the
 // comparison.
 // FB > 0: b == bt == FB, known at compile time (the loop is unrolled, every column's
-// shared-memory address and end test are constants)
+// shared-memory address and end test are constants).  The orbit ends stay a branch:
+// taking the greatest count at every column without one measured 1.45x slower.
+// The row is compared with the bound once it is complete: placed 1s-first inside
+// every orbit, the first orbit whose counts differ decides, which is the first
+// position where the two rows differ (a per-orbit comparison inside the loop
+// measured 1.13x slower).
 template <unsigned FB = 0, typename S>
 __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned bt, unsigned &tied,
                                                  uint64_t &arr, bool have_bound, uint64_t bound) {
@@ -52,7 +57,6 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
     const uint64_t ends = (lvl >> 1) | (~0ull << (b - 1));
     unsigned t0 = tied;
     uint64_t a = 0;
-    int state = 0;
     unsigned p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
     unsigned s = 0;
 #pragma unroll(FB ? FB : 1)
@@ -73,14 +77,14 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
             t = t0 & p1; if (t) { t0 = t; cstar |= 2u; }
             t = t0 & p0; if (t) { t0 = t; cstar |= 1u; }
             a |= ((1ull << cstar) - 1ull) << s;
-            if (state == 0 && have_bound) {
-                const uint64_t rng = ((2ull << p) - 1ull) & ~((1ull << s) - 1ull);
-                const unsigned cb = __popcll(bound & rng);
-                state = cstar > cb ? 1 : (cstar < cb ? 2 : 0);
-            }
             p0 = p1 = p2 = p3 = p4 = p5 = 0;
             s = p + 1;
         }
+    }
+    int state = 0;
+    if (have_bound) {
+        const uint64_t ka = __brevll(a), kb = __brevll(bound);
+        state = ka > kb ? 1 : (ka < kb ? 2 : 0);
     }
     tied = t0;
     arr = a;

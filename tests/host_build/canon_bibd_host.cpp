@@ -11,6 +11,12 @@
 static inline int __ffsll(long long x) { return __builtin_ffsll(x); }
 static inline int __ffs(unsigned x) { return __builtin_ffs((int)x); }
 static inline int __popcll(unsigned long long x) { return __builtin_popcountll(x); }
+static inline unsigned long long __brevll(unsigned long long x) {
+    unsigned long long r = 0;
+    for (int i = 0; i < 64; ++i)
+        r |= ((x >> i) & 1ull) << (63 - i);
+    return r;
+}
 static inline int __popc(unsigned x) { return __builtin_popcount(x); }
 static inline int __clzll(long long x) { return x ? __builtin_clzll((unsigned long long)x) : 64; }
 static inline int __clz(unsigned x) { return x ? __builtin_clz(x) : 32; }
@@ -106,15 +112,29 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
     st.restart_after = mode == 0 ? ~0ull : (mode == 1 ? RESTART_AFTER : 0);
     int ref_lv = -1;
     unsigned ref_x = 0;
+    // the kernels' unrolled node step where b is the instance's column capacity
+    const unsigned fb = (b == bt && (b == 35 || b == 40 || b == 64)) ? b : 0;
     for (;;) {
-        if (ref_lv >= 0)
-            refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
+        if (ref_lv >= 0) {
+            if (fb == 35)
+                refine_uniform<35>(sm, (unsigned)ref_lv, ref_x, bt);
+            else if (fb == 40)
+                refine_uniform<40>(sm, (unsigned)ref_lv, ref_x, bt);
+            else if (fb == 64)
+                refine_uniform<64>(sm, (unsigned)ref_lv, ref_x, bt);
+            else
+                refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
+        }
         if (++st.nodes > (1ull << 30))
             return -2;
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        const uint64_t bnd = hb ? R_(st.i) : 0ull;
+        const int state = fb == 35   ? eval_node_uniform<35>(sm, st.i, b, bt, tied, arr, hb, bnd)
+                          : fb == 40 ? eval_node_uniform<40>(sm, st.i, b, bt, tied, arr, hb, bnd)
+                          : fb == 64 ? eval_node_uniform<64>(sm, st.i, b, bt, tied, arr, hb, bnd)
+                                     : eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, bnd);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             break;
         if (!conv_next(sm, st, ref_lv, ref_x))
