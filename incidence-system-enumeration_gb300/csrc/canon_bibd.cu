@@ -348,8 +348,15 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
             break;
         if (!eval)
             continue;
-        if (ref_lv >= 0)
-            refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
+        // unrolled when every item of the launch has the instance's column capacity
+        // (bt == BCAP then holds for all lanes, and b == bt for every lane with a node)
+        const bool full = bt == BCAP && b == BCAP;
+        if (ref_lv >= 0) {
+            if (full)
+                refine_uniform<BCAP>(sm, (unsigned)ref_lv, ref_x, bt);
+            else
+                refine_uniform(sm, (unsigned)ref_lv, ref_x, bt);
+        }
         if (++st.nodes > max_nodes) {
             st.timeout = true;
             finish(ST_TIMEOUT);
@@ -358,7 +365,9 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
         unsigned tied = st.allrows & ~st.used;
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
-        const int state = eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, hb ? R_(st.i) : 0ull);
+        const uint64_t bnd = hb ? R_(st.i) : 0ull;
+        const int state = full ? eval_node_uniform<BCAP>(sm, st.i, b, bt, tied, arr, hb, bnd)
+                               : eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, bnd);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }
