@@ -236,6 +236,7 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
                 conv_start(st, v, orders ? orders[it] : ID16);
                 st.b = b;
                 st.restart_after = restart_after;
+                st.verdict_only = flags & F_VERDICT_ONLY;
                 have = true;
                 if (!load_rows(sm, rows + (size_t)it * v, v, b, flags & F_RAW)) {
                     finish(ST_BADINPUT);
@@ -327,6 +328,7 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
                 conv_start(st, n >= 1 && n <= VCAP ? n : 1, ID16);
                 st.b = b;
                 st.restart_after = restart_after;
+                st.verdict_only = item.flags & F_VERDICT_ONLY;
                 have = true;
                 if (item.kind != KIND_BIBD || n < 1 || n > VCAP || b < 1 || b > BMAX || b > BCAP || b > bt ||
                     !load_rows(sm, words + item.data_off, n, b, item.flags & F_RAW)) {

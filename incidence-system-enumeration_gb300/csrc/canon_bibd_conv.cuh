@@ -130,9 +130,10 @@ struct ConvState {
     unsigned n, valid, used, id_top, i, allrows, b;
     uint64_t nmask1;
     bool improved, timeout, rejected;
+    bool verdict_only;      // stop at the first greater node (M rejected; no |Aut|)
 };
 
-// a fresh search of the n rows in R_(); restart_after and b are the caller's
+// a fresh search of the n rows in R_(); restart_after, b and verdict_only are the caller's
 __device__ __forceinline__ void conv_start(ConvState &st, unsigned n, uint64_t order0) {
     st.rejected = false;
     st.n = n;
@@ -251,6 +252,8 @@ __device__ __forceinline__ bool conv_after_eval(S sm, ConvState &st, int state, 
         if (state == 1) {
             st.improved = true;
             st.leaves = 0;
+            if (st.verdict_only)
+                return false;
         }
         const uint64_t cols = (1ull << b) - 1ull;
         R_(i) = arr;

@@ -46,8 +46,10 @@ constexpr int SCAN_TILE = SCAN_TPB * SCAN_PER_THREAD;
 constexpr uint64_t SLICE_CAP = 1ull << 24;
 constexpr int GEN_TPB = 128;
 // levels with at least this many parents generate their children on the GPU
-// (enough independent searches to fill it); smaller ones on the host cores
-constexpr uint64_t DEVICE_GEN_MIN = 1ull << 17;
+// (enough independent searches to fill it); smaller ones on the host cores.  On
+// BIBD(12,22,11,6,5) a level of ~10K parents took 79 ms on 16 host cores against 170 ms
+// on the GPU, one of ~60K parents 1.15 s against 0.14 s.
+constexpr uint64_t DEVICE_GEN_MIN = 1ull << 14;
 // slices up to this size are checked with the search split by first row (one
 // thread per matrix and first row): small levels are latency bound
 constexpr uint64_t SPLIT_MAX = 1ull << 16;
@@ -516,7 +518,9 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 return done(CANON_ECUDA, "count", e);
             c->launches += 4;
         }
-        st.gen_seconds += since(tg);
+        const double g1 = since(tg);
+        st.gen_seconds += g1;
+        st.level_gen_ms[m - 1] += g1 * 1e3;
         e = next.ensure((size_t)(n_cand ? n_cand : 1) * m);
         if (e == cudaSuccess && complete)
             e = aut_out.ensure((size_t)(n_cand ? n_cand : 1) * 2);
@@ -595,7 +599,9 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                     e = cudaStreamSynchronize(s);
                 ++c->launches;
             }
-            st.gen_seconds += since(tg);
+            const double g2 = since(tg);
+            st.gen_seconds += g2;
+            st.level_gen_ms[m - 1] += g2 * 1e3;
             if (e != cudaSuccess)
                 return done(CANON_ECUDA, "children", e);
             // 3: the verdicts
@@ -610,10 +616,14 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                                                        cand.p, can.p, complete ? aut.p : nullptr, status.p, parts.p,
                                                        stop.p, c->cfg.max_trials, c->d_ticket, c->num_sms, s);
             } else {
+                // the converged lex-max pass, stopping at the first greater node: 6-8x less
+                // check time than the one-pass reference-order check on the large families
+                // (BIBD(16,24,9,6,3): 4.2 s against 32.7 s)
                 e = canon::launch_bibd_check_uniform((uint32_t)ns, m, b,
                                                      canon::F_VERDICT_ONLY | (complete ? canon::F_COMPLETE : 0u),
                                                      cand.p, can.p, nullptr, complete ? aut.p : nullptr, status.p,
-                                                     nullptr, c->cfg.max_trials, c->d_ticket, c->num_sms, s);
+                                                     nullptr, c->cfg.max_trials, c->d_ticket, c->num_sms, s,
+                                                     nullptr, canon::VARIANT_CONVERGED);
             }
             cudaEventRecord(e1, s);
             // 4: pack the canonical ones into the next level

@@ -48,6 +48,30 @@ enum Emit { COUNT = 0, CHILD = 1, NEW_ROW = 2 };
 // at most this many automorphisms of a parent prune its children
 constexpr int AUT_GENS = 8;
 
+// one byte per row (rows 0-7 in w[0], 8-15 in w[1])
+constexpr uint64_t B64 = 0x4040404040404040ull;    // 64 in every byte
+constexpr uint64_t HIB = 0x8080808080808080ull;    // the high bit of every byte
+struct Bytes16 {
+    uint64_t w[2];
+    // += / -= v times the 0/1 bytes of m (v <= 63: no byte leaves 0..127)
+    CANON_HD void add(const Bytes16 &m, unsigned v) {
+        w[0] += m.w[0] * v;
+        w[1] += m.w[1] * v;
+    }
+    CANON_HD void sub(const Bytes16 &m, unsigned v) {
+        w[0] -= m.w[0] * v;
+        w[1] -= m.w[1] * v;
+    }
+};
+
+// bit j of m (j < 8) -> byte j, as 0 or 1
+CANON_HD inline uint64_t spread8(unsigned m) {
+    const uint64_t v = ((uint64_t)(m & 0xFFu) * 0x0101010101010101ull) & 0x8040201008040201ull;
+    return (((v + 0x7F7F7F7F7F7F7F7Full) | v) >> 7) & 0x0101010101010101ull;
+}
+// bit i of m (i < 16) -> byte i of the two words
+CANON_HD inline Bytes16 spread16(unsigned m) { return Bytes16{{spread8(m & 0xFFu), spread8((m >> 8) & 0xFFu)}}; }
+
 // Children of one parent with n rows (bit c of word i = row i, column c), in a
 // fixed order: orbits left to right, more 1s first.  Returns their number.
 // gens: ngens automorphisms of the parent as row permutations (nibble i = the row
@@ -110,33 +134,38 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
             ++na;
     }
     // hi/lo: the most / least 1s orbit q can take (full orbits none, orbits whose
-    // columns need every remaining row all); rc/rn: the sums of hi/lo over the
-    // orbits from the current one on that meet row i (ca/cn over all orbits), kept
-    // as the search moves, so a row whose lambda can no longer be met ends the
-    // branch at once
+    // columns need every remaining row all).  Per row i, with one byte per row in two
+    // 64-bit words (rows 0-7, 8-15): LAM = the 1s row i still needs in common with the
+    // new row, plus 64; RC / RN = the sums of hi / lo over the orbits from the current
+    // one on that meet row i.  A value xv for orbit q is admissible when every row
+    // keeps RN - lo[q] <= lam - xv <= RC - hi[q] (rows in the orbit; the others keep
+    // RN <= lam <= RC), tested for all rows at once: bytes stay in 0..127, so
+    // ((a | 0x80) - b) has its byte's high bit set exactly when a >= b.  A row whose
+    // lambda can no longer be met ends the branch at once.
     const int rem_rows = d.v - n - 1;
     uint8_t hi[64], lo[64];
-    int rc[16], rn[16], ca = 0, cn = 0;
-    for (int i = 0; i < n; ++i)
-        rc[i] = rn[i] = 0;
+    // rows 0..n-1 need lambda (byte 64 + lambda), rows past n nothing (byte 64)
+    const unsigned rows_mask = (n >= 16) ? 0xFFFFu : ((1u << n) - 1u);
+    Bytes16 rc{{0, 0}}, rn{{0, 0}};
+    Bytes16 lamb{{spread8(rows_mask & 0xFFu) * (uint64_t)d.lambda + B64,
+                  spread8(rows_mask >> 8) * (uint64_t)d.lambda + B64}};
+    int ca = 0, cn = 0;
     for (int q = 0; q < norb; ++q) {
         hi[q] = (weight[q] >= k) ? 0 : len[q];
         lo[q] = (k - weight[q] > rem_rows) ? len[q] : 0;
         ca += hi[q];
         cn += lo[q];
-        for (int i = 0; i < n; ++i)
-            if ((ones[q] >> i) & 1u) {
-                rc[i] += hi[q];
-                rn[i] += lo[q];
-            }
+        const Bytes16 m = spread16(ones[q]);
+        rc.add(m, hi[q]);
+        rn.add(m, lo[q]);
     }
-    int lam[16];
-    for (int i = 0; i < n; ++i)
-        lam[i] = d.lambda;
     // iterative depth-first search over the orbits: x[q] the 1s given to orbit q,
     // nxt[q] the next value to try, left[q] the 1s still to place before orbit q,
     // tied bit q: the row equals row n-1 on the orbits before q
     uint8_t x[64], nxt[64], mn[64], left[65];
+    // of the orbit q being filled: 1 in the bytes of the rows it meets, and RN - lo[q] + 64,
+    // RC - hi[q] + 64
+    Bytes16 mq{{0, 0}}, lo64{{0, 0}}, up64{{0, 0}};
     uint64_t tied = 1;
     uint32_t count = 0;
     int q = 0;
@@ -145,9 +174,7 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
     for (;;) {
         if (enter) {
             if (q == norb) {
-                bool ok = left[q] == 0;
-                for (int i = 0; ok && i < n; ++i)
-                    ok = lam[i] == 0;
+                bool ok = left[q] == 0 && lamb.w[0] == B64 && lamb.w[1] == B64;
                 // the swap test against every row i >= 1 (the orbits of level i are
                 // runs of orbits not split by rows 0..i-1; row 0 has the same weight)
                 for (int i = 1; ok && i < n; ++i) {
@@ -206,16 +233,23 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
                 if (q == 0)
                     break;
                 --q;
+                mq = spread16(ones[q]);
                 ca += hi[q];
                 cn += lo[q];
-                for (int i = 0; i < n; ++i)
-                    if ((ones[q] >> i) & 1u) {
-                        rc[i] += hi[q];
-                        rn[i] += lo[q];
-                    }
+                rc.add(mq, hi[q]);
+                rn.add(mq, lo[q]);
+                lo64 = rn;
+                lo64.sub(mq, lo[q]);
+                lo64.w[0] += B64;
+                lo64.w[1] += B64;
+                up64 = rc;
+                up64.sub(mq, hi[q]);
+                up64.w[0] += B64;
+                up64.w[1] += B64;
                 enter = false;
                 continue;
             }
+            mq = spread16(ones[q]);
             const int lf = left[q];
             const int ca1 = ca - hi[q], cn1 = cn - lo[q];      // orbits after q
             int minx = lo[q], maxx = hi[q];
@@ -232,28 +266,30 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
             x[q] = 0xFF;                           // nothing applied yet
             if (maxx < minx)
                 nxt[q] = mn[q];                    // empty range
+            lo64 = rn;
+            lo64.sub(mq, lo[q]);
+            lo64.w[0] += B64;
+            lo64.w[1] += B64;
+            up64 = rc;
+            up64.sub(mq, hi[q]);
+            up64.w[0] += B64;
+            up64.w[1] += B64;
         }
         // undo the value applied at level q, then try the next one
         if (x[q] != 0xFF) {
-            for (int i = 0; i < n; ++i)
-                if ((ones[q] >> i) & 1u)
-                    lam[i] += x[q];
+            lamb.add(mq, x[q]);
             x[q] = 0xFF;
         }
         bool moved = false;
         while (nxt[q] > mn[q]) {
             const int xv = --nxt[q];
-            bool ok = true;
-            for (int i = 0; i < n && ok; ++i) {
-                const bool in = (ones[q] >> i) & 1u;
-                const int l = lam[i] - (in ? xv : 0);
-                ok = l >= rn[i] - (in ? lo[q] : 0) && l <= rc[i] - (in ? hi[q] : 0);
-            }
-            if (!ok)
+            Bytes16 l = lamb;
+            l.sub(mq, (unsigned)xv);
+            const uint64_t g0 = ((l.w[0] | HIB) - lo64.w[0]) & ((up64.w[0] | HIB) - l.w[0]) & HIB;
+            const uint64_t g1 = ((l.w[1] | HIB) - lo64.w[1]) & ((up64.w[1] | HIB) - l.w[1]) & HIB;
+            if (g0 != HIB || g1 != HIB)
                 continue;
-            for (int i = 0; i < n; ++i)
-                if ((ones[q] >> i) & 1u)
-                    lam[i] -= xv;
+            lamb = l;
             x[q] = (uint8_t)xv;
             left[q + 1] = (uint8_t)(left[q] - xv);
             // still equal to row n-1: its value on the orbit taken everywhere
@@ -268,11 +304,8 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
         if (moved) {
             ca -= hi[q];
             cn -= lo[q];
-            for (int i = 0; i < n; ++i)
-                if ((ones[q] >> i) & 1u) {
-                    rc[i] -= hi[q];
-                    rn[i] -= lo[q];
-                }
+            rc.sub(mq, hi[q]);
+            rn.sub(mq, lo[q]);
             ++q;
             enter = true;
             continue;
@@ -280,13 +313,19 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
         if (q == 0)
             break;
         --q;
+        mq = spread16(ones[q]);
         ca += hi[q];
         cn += lo[q];
-        for (int i = 0; i < n; ++i)
-            if ((ones[q] >> i) & 1u) {
-                rc[i] += hi[q];
-                rn[i] += lo[q];
-            }
+        rc.add(mq, hi[q]);
+        rn.add(mq, lo[q]);
+        lo64 = rn;
+        lo64.sub(mq, lo[q]);
+        lo64.w[0] += B64;
+        lo64.w[1] += B64;
+        up64 = rc;
+        up64.sub(mq, hi[q]);
+        up64.w[0] += B64;
+        up64.w[1] += B64;
         enter = false;
     }
     return count;

@@ -106,7 +106,8 @@ class EnumStats(ctypes.Structure):
     _fields_ = [("checks", ctypes.c_uint64), ("designs", ctypes.c_uint64), ("levels", ctypes.c_uint32),
                 ("batches", ctypes.c_uint32), ("seconds", ctypes.c_double), ("kernel_ms", ctypes.c_double),
                 ("level_checks", ctypes.c_uint64 * 16), ("level_kernel_ms", ctypes.c_double * 16),
-                ("gen_seconds", ctypes.c_double), ("trials", ctypes.c_uint64)]
+                ("gen_seconds", ctypes.c_double), ("trials", ctypes.c_uint64),
+                ("level_gen_ms", ctypes.c_double * 16)]
 
 
 DESIGN_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint8), ctypes.c_uint32,

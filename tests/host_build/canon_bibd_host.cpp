@@ -110,6 +110,7 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
     conv_start(st, n, order0);
     st.b = b;
     st.restart_after = mode == 0 ? ~0ull : (mode == 1 ? RESTART_AFTER : 0);
+    st.verdict_only = mode == 3;
     int ref_lv = -1;
     unsigned ref_x = 0;
     // the kernels' unrolled node step where b is the instance's column capacity

@@ -301,6 +301,9 @@ def test_restart_and_aut_of_m_give_the_same_verdict_and_order(host):
             assert a[0] == aut and a[2] == climb[2]
             m = _search(host.emu_maxsearch_order, r, 15, 35, mode=mode)
             assert m[0] == aut and m[2] == climb[2]
+        # verdict only: stops at the first greater node, the verdict is the climb's
+        vo = _search(host.emu_conv_search, r, 15, 35, mode=3)
+        assert vo[2] == climb[2] and (vo[2] or vo[0] == aut)
         worst["climb"] = max(worst["climb"], climb[1])
         worst["restart"] = max(worst["restart"], _search(host.emu_conv_search, r, 15, 35, mode=1)[1])
         worst["cap"] = max(worst["cap"], _search(host.emu_maxsearch_order, r, 15, 35, mode=2)[1])
@@ -310,6 +313,8 @@ def test_restart_and_aut_of_m_give_the_same_verdict_and_order(host):
             for mode in (1, 2):
                 a2 = _search(host.emu_conv_search, p, k, 35, mode=mode)
                 assert a2[0] == c2[0] and a2[2] == c2[2]
+            v2 = _search(host.emu_conv_search, p, k, 35, mode=3)
+            assert v2[2] == c2[2] and (v2[2] or v2[0] == c2[0])
             m2 = _search(host.emu_maxsearch_order, p, k, 35, mode=1)
             assert m2[0] == c2[0] and m2[2] == c2[2]
     # both bound the longest search (the relabelled PG(3,2): 151,636 nodes climbing)
