@@ -96,20 +96,26 @@ struct DevBuf {
 };
 
 // new rows kept per parent by the counting pass, so that the emitting pass only
-// copies for parents with at most this many children
-constexpr uint32_t ROW_CACHE = 16;
+// copies for parents with at most that many children: up to ROW_CACHE_MAX rows a
+// parent while the cache stays within ROW_CACHE_BYTES, at least ROW_CACHE_MIN
+constexpr uint32_t ROW_CACHE_MIN = 16, ROW_CACHE_MAX = 64;
+constexpr uint64_t ROW_CACHE_BYTES = 4ull << 30;
+uint32_t row_cache_rows(uint64_t n_par) {
+    const uint64_t fit = ROW_CACHE_BYTES / (8 * (n_par ? n_par : 1));
+    return fit >= ROW_CACHE_MAX ? ROW_CACHE_MAX : (fit <= ROW_CACHE_MIN ? ROW_CACHE_MIN : (uint32_t)fit);
+}
 
 // gens / ngens: automorphisms of every parent that prune its children (none if null)
 __global__ void __launch_bounds__(GEN_TPB) rows_count_kernel(canon::rows::Params d, const uint64_t *parents,
                                                              uint32_t n_par, int n, uint32_t *counts,
-                                                             uint64_t *cache, unsigned *ticket,
+                                                             uint64_t *cache, uint32_t cache_rows, unsigned *ticket,
                                                              const uint64_t *gens, const uint8_t *ngens) {
     for (;;) {
         const unsigned p = atomicAdd(ticket, 1u);
         if (p >= n_par)
             break;
         counts[p] = canon::rows::children<canon::rows::NEW_ROW>(
-            d, parents + (size_t)p * n, n, cache + (size_t)p * ROW_CACHE, ROW_CACHE,
+            d, parents + (size_t)p * n, n, cache + (size_t)p * cache_rows, cache_rows,
             gens ? gens + (size_t)p * canon::rows::AUT_GENS : nullptr, gens ? ngens[p] : 0);
     }
 }
@@ -117,7 +123,7 @@ __global__ void __launch_bounds__(GEN_TPB) rows_count_kernel(canon::rows::Params
 __global__ void __launch_bounds__(GEN_TPB) rows_emit_kernel(canon::rows::Params d, const uint64_t *parents,
                                                             uint32_t p0, uint32_t p1, int n,
                                                             const uint64_t *offsets, const uint32_t *counts,
-                                                            const uint64_t *cache, uint64_t *out,
+                                                            const uint64_t *cache, uint32_t cache_rows, uint64_t *out,
                                                             unsigned *ticket, const uint64_t *gens,
                                                             const uint8_t *ngens) {
     const uint64_t base = offsets[p0];
@@ -128,11 +134,11 @@ __global__ void __launch_bounds__(GEN_TPB) rows_emit_kernel(canon::rows::Params 
         const uint32_t cnt = counts[p];
         const uint64_t *par = parents + (size_t)p * n;
         uint64_t *dst = out + (offsets[p] - base) * (n + 1);
-        if (cnt <= ROW_CACHE) {
+        if (cnt <= cache_rows) {
             for (uint32_t j = 0; j < cnt; ++j) {
                 for (int i = 0; i < n; ++i)
                     dst[(size_t)j * (n + 1) + i] = par[i];
-                dst[(size_t)j * (n + 1) + n] = cache[(size_t)p * ROW_CACHE + j];
+                dst[(size_t)j * (n + 1) + n] = cache[(size_t)p * cache_rows + j];
             }
         } else {
             canon::rows::children<canon::rows::CHILD>(d, par, n, dst, cnt,
@@ -498,7 +504,7 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
             if (e == cudaSuccess)
                 e = doffs.ensure(n_par + 1);
             if (e == cudaSuccess)
-                e = rcache.ensure((size_t)n_par * ROW_CACHE);
+                e = rcache.ensure((size_t)n_par * row_cache_rows(n_par));
             if (e != cudaSuccess)
                 return done(CANON_ENOMEM, "level buffers", e);
             int grid = 0;
@@ -508,7 +514,8 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
             if (e != cudaSuccess)
                 return done(CANON_ECUDA, "count", e);
             rows_count_kernel<<<grid, GEN_TPB, 0, s>>>(prm, lev.p, (uint32_t)n_par, (int)n, dcounts.p, rcache.p,
-                                                       ticket.p, have_gens ? gens.p : nullptr, ngens.p);
+                                                       row_cache_rows(n_par), ticket.p,
+                                                       have_gens ? gens.p : nullptr, ngens.p);
             e = cudaGetLastError();
             if (e == cudaSuccess)
                 e = exclusive_scan(dcounts.p, n_par, doffs.p, sums, s);
@@ -592,8 +599,8 @@ extern "C" int canon_enumerate_bibd(canon_ctx *c, uint32_t v, uint32_t b, uint32
                 if (e != cudaSuccess)
                     return done(CANON_ECUDA, "children", e);
                 rows_emit_kernel<<<grid, GEN_TPB, 0, s>>>(prm, lev.p, (uint32_t)p0, (uint32_t)p1, (int)n, doffs.p,
-                                                          dcounts.p, rcache.p, cand.p, ticket.p,
-                                                          have_gens ? gens.p : nullptr, ngens.p);
+                                                          dcounts.p, rcache.p, row_cache_rows(n_par), cand.p,
+                                                          ticket.p, have_gens ? gens.p : nullptr, ngens.p);
                 e = cudaGetLastError();
                 if (e == cudaSuccess)
                     e = cudaStreamSynchronize(s);
