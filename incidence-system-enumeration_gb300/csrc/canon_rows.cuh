@@ -51,6 +51,8 @@ constexpr int AUT_GENS = 8;
 // one byte per row (rows 0-7 in w[0], 8-15 in w[1])
 constexpr uint64_t B64 = 0x4040404040404040ull;    // 64 in every byte
 constexpr uint64_t HIB = 0x8080808080808080ull;    // the high bit of every byte
+constexpr uint64_t LOW7 = 0x7F7F7F7F7F7F7F7Full;
+constexpr uint64_t ONE8 = 0x0101010101010101ull;
 struct Bytes16 {
     uint64_t w[2];
     // += / -= v times the 0/1 bytes of m (v <= 63: no byte leaves 0..127)
@@ -285,9 +287,22 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
             const int xv = --nxt[q];
             Bytes16 l = lamb;
             l.sub(mq, (unsigned)xv);
-            const uint64_t g0 = ((l.w[0] | HIB) - lo64.w[0]) & ((up64.w[0] | HIB) - l.w[0]) & HIB;
-            const uint64_t g1 = ((l.w[1] | HIB) - lo64.w[1]) & ((up64.w[1] | HIB) - l.w[1]) & HIB;
-            if (g0 != HIB || g1 != HIB)
+            // per row, with the 1s left after this orbit (left'), the capacities of the
+            // later orbits (ca', cn') and their parts that meet row i (RC', RN'):
+            //   RN' <= lam' <= RC'                  (byte high bits of a and bb)
+            //   RC' - lam' <= ca' - left'           (the 1s outside row i's orbits fit)
+            //   lam' - RN' <= left' - cn'           (and fill what must be filled)
+            const int lf1 = left[q] - xv;
+            const uint64_t k2 = ONE8 * (uint64_t)(ca - hi[q] - lf1) | HIB;
+            const uint64_t k3 = ONE8 * (uint64_t)(lf1 - (cn - lo[q])) | HIB;
+            uint64_t g = HIB;
+#pragma unroll
+            for (int w = 0; w < 2; ++w) {
+                const uint64_t a = (up64.w[w] | HIB) - l.w[w];      // 128 + RC' - lam'
+                const uint64_t bb = (l.w[w] | HIB) - lo64.w[w];     // 128 + lam' - RN'
+                g &= a & bb & (k2 - (a & LOW7)) & (k3 - (bb & LOW7));
+            }
+            if (g != HIB)
                 continue;
             lamb = l;
             x[q] = (uint8_t)xv;

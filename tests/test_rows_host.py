@@ -134,3 +134,83 @@ def test_automorphism_pruning_keeps_the_designs_and_drops_candidates(gen, key):
     assert got == {M.tobytes(): a for M, a in ref}
     assert cand_aut <= cand_plain
     print(key, cand_plain, cand_aut)
+
+
+def _orbits(parent, n, b):
+    """The parent's column orbits: (start, len, rows with 1s as a bit set, split row)."""
+    cols = [sum(((int(parent[i]) >> c) & 1) << i for i in range(n)) for c in range(b)]
+    orbs, s = [], 0
+    for c in range(1, b + 1):
+        if c == b or cols[c] != cols[c - 1]:
+            split = 0
+            if orbs:
+                while split < n and ((cols[s] >> split) & 1) == ((cols[s - 1] >> split) & 1):
+                    split += 1
+            orbs.append((s, c - s, cols[s], split))
+            s = c
+    return orbs
+
+
+def _brute_children(params, parent):
+    """Every admissible next row by brute force over the 1s per orbit, with the
+    generator's rules written out: weight r, lambda with every row, no column above k,
+    columns that need every remaining row, not above row n-1, and the swap test."""
+    import itertools
+    v, b, r, k, lam = params
+    n = len(parent)
+    orbs = _orbits(parent, n, b)
+    rem = v - n - 1
+    rngs = []
+    for _, ln, om, _ in orbs:
+        w = bin(om).count("1")
+        hi = 0 if w >= k else ln
+        lo = ln if k - w > rem else 0
+        rngs.append(range(lo, hi + 1))
+    prev = [ln if (om >> (n - 1)) & 1 else 0 for _, ln, om, _ in orbs]
+    out = []
+    for x in itertools.product(*[list(rg)[::-1] for rg in rngs]):
+        if sum(x) != r:
+            continue
+        if any(sum(x[t] for t, o in enumerate(orbs) if (o[2] >> i) & 1) != lam for i in range(n)):
+            continue
+        if list(x) > prev:
+            continue
+        ok = True
+        for i in range(1, n):
+            c = ri = 0
+            for t in range(len(orbs) + 1):
+                if t == len(orbs) or (t > 0 and orbs[t][3] < i):
+                    if c > ri:
+                        ok = False
+                    if c != ri or t == len(orbs):
+                        break
+                    c = ri = 0
+                c += x[t]
+                ri += orbs[t][1] if (orbs[t][2] >> i) & 1 else 0
+            if not ok:
+                break
+        if ok:
+            row = 0
+            for t, (st, _, _, _) in enumerate(orbs):
+                row |= ((1 << x[t]) - 1) << st
+            out.append(row)
+    return out
+
+
+@pytest.mark.parametrize("key,levels", [("8,14,7,4,3", 6), ("10,15,6,4,2", 6), ("13,26,8,4,2", 4),
+                                        ("12,22,11,6,5", 4)])
+def test_children_equal_the_rules_by_brute_force(gen, key, levels):
+    """The generator's depth-first search with its bounds (per-row lambda windows, the
+    1s that must fit outside every row's orbits, the swap test run orbit by orbit) gives
+    exactly the rows that the rules admit, in the same order (orbits left to right,
+    more 1s first)."""
+    params = tuple(map(int, key.split(",")))
+    v, b, r = params[:3]
+    level = [np.array([(1 << r) - 1], np.uint64)]
+    for m in range(2, levels + 1):
+        nxt = []
+        for parent in level[:60]:
+            kids = children(gen, params, parent)
+            assert [int(c[-1]) for c in kids] == _brute_children(params, parent), (key, m)
+            nxt.extend(kids)
+        level = nxt
