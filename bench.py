@@ -42,10 +42,10 @@ WORKLOAD = ("1,048,576 STS(15) 15x35 bit-packed matrices, seed %d, odd items can
             "outputs canonical flag + first rejecting permutation + |Aut|" % SEED)
 IN_BYTES = V * 8          # packed rows read per check
 OUT_BYTES = 1 + 16 + 16   # flag + witness + |Aut| written per check
-# DRAM bytes per check of the lex-max pass: dram__bytes_read.sum + dram__bytes_write.sum of one ncu
-# capture of 131,072 checks (15,918,592 B + 0 B; profiles/bibd_max_kernel_sts15_131k.md), scaled by
-# the checks of a launch (traffic grows with the number of matrices read).
-TRAFFIC_PER_CHECK = 15918592.0 / 131072
+# DRAM bytes per check of the converged lex-max pass: dram__bytes_read.sum + dram__bytes_write.sum
+# of one ncu capture of 65,536 checks (8,426,496 B + 0 B; profiles/bibd_conv_kernel_sts15_65k.md),
+# scaled by the checks of a launch (traffic grows with the number of matrices read).
+TRAFFIC_PER_CHECK = 8426496.0 / 65536
 # Integer work of the lex-max search (the check's roofline): a node compares the best
 # arrangement of every candidate row with the bound, one bit-sliced step per column of
 # the matrix: the column's row mask ANDed with the tied rows, a 6-plane carry chain
@@ -438,7 +438,8 @@ def run_mix(args):
     batches = workloads.config3_mix(n_total, SEED + 3)
     gen_s = time.perf_counter() - t0
     n = sum(len(bt["nrows"]) for bt in batches)
-    ctx = G.Context(max_items=n + 16, max_words=16 * n, aut_cap=1)
+    # a level-keeping caller reads only the verdicts: canon_sync returns canonical + status
+    ctx = G.Context(max_items=n + 16, max_words=16 * n, aut_cap=1, options=G.OPT_VERDICT_SYNC)
     for _ in range(args.warmup):
         workloads.submit_mix(ctx, batches)
         ctx.sync(raw=True)
@@ -464,8 +465,8 @@ def run_mix(args):
                       "canonical_fraction": float(can.mean()),
                       "from_complete_design": int(bt["from_complete"])})
         off += cnt
-    h2d = workloads.mix_input_bytes(batches) + 16 * n
-    d2h = 51 * n
+    h2d = sum(int(bt["data"].nbytes) for bt in batches) + 16 * n    # rows / rounds + work descriptors
+    d2h = 2 * n         # canonical + status (CANON_OPT_VERDICT_SYNC)
     line = {"metric": "exact canonicity checks/sec (config 3 uneven mix, one persistent launch)",
             "value": n * args.steps / (sum(kms) / 1e3), "unit": "checks/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": sum(kms) / args.steps, "higher_is_better": True,

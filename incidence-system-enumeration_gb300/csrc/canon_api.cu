@@ -1,13 +1,15 @@
 // canon_api.cu -- the C ABI (include/canon_gb300.h) over the sm_103a kernels.
 //
 // A context owns one CUDA stream, pinned host staging for queued batches and
-// device buffers sized at creation.  canon_submit_* only appends to the host
-// staging; canon_sync copies everything to the GPU in two copies (items, data),
-// launches the check kernels on the context's stream, copies the result arrays
-// back and waits.  This replaces CGPU_CanonChecker (Source/MatrixCanonChecker.h:
-// 204-350), which marshalled one C++ checker object per matrix onto the device
-// heap and launched TestCanonicity<<<1, nMatr>>> (Source/CanonicityChecker.cu:152-156).
+// device buffers sized at creation.  canon_submit_* appends a batch to the host
+// staging (on host threads) and queues its copy to the GPU at once, so the copy
+// of one batch runs while the next is packed; canon_sync launches the check
+// kernels on the context's stream, copies the result arrays back and waits.  This
+// replaces CGPU_CanonChecker (Source/MatrixCanonChecker.h:204-350), which
+// marshalled one C++ checker object per matrix onto the device heap and launched
+// TestCanonicity<<<1, nMatr>>> (Source/CanonicityChecker.cu:152-156).
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <thread>
@@ -269,6 +271,7 @@ void canon_destroy(canon_ctx *c) {
     if (c) {
         cudaFree(c->d_split_parts);
         cudaFree(c->d_split_stop);
+        cudaFree(c->d_kseg);
     }
     if (!c)
         return;
@@ -312,25 +315,53 @@ int canon_submit_bibd(canon_ctx *c, const canon_bibd_batch *bt) {
         return fail(c, CANON_ENOMEM, "item capacity exceeded (canon_cfg.max_items)");
     if ((uint64_t)c->n_words + (uint64_t)bt->n * bt->v > c->cfg.max_words)
         return fail(c, CANON_ENOMEM, "word capacity exceeded (canon_cfg.max_words)");
-    for (uint32_t i = 0; i < bt->n; ++i) {
-        const uint32_t nr = bt->nrows ? bt->nrows[i] : bt->v;
-        if (nr < 1 || nr > bt->v)
-            return fail(c, CANON_EINVAL, "bibd batch: nrows out of range");
-    }
+    // packed on host threads, each checking the filled-row counts of its range; a
+    // refused batch leaves the queue as it was (its bytes past the queue's end are
+    // overwritten by the next batch)
+    std::atomic<bool> bad{false};
     pack_parallel(bt->n, [&](uint64_t lo, uint64_t hi) {
         std::memcpy(c->h_words + c->n_words + lo * bt->v, bt->rows + lo * bt->v,
                     (size_t)(hi - lo) * bt->v * sizeof(uint64_t));
+        bool ok = true;
         for (uint64_t i = lo; i < hi; ++i) {
+            const uint32_t nr = bt->nrows ? bt->nrows[i] : bt->v;
+            ok = ok && nr >= 1 && nr <= bt->v;
             Item it{};
             it.data_off = c->n_words + (uint32_t)i * bt->v;
             it.kind = canon::KIND_BIBD;
-            it.nrows = (uint8_t)(bt->nrows ? bt->nrows[i] : bt->v);
+            it.nrows = (uint8_t)nr;
             it.ncols = (uint8_t)bt->b;
             it.flags = (uint8_t)bt->flags;
             it.out_idx = total + (uint32_t)i;
             c->h_bitems[c->n_bitems + i] = it;
         }
+        if (!ok)
+            bad.store(true, std::memory_order_relaxed);
     });
+    if (bad.load())
+        return fail(c, CANON_EINVAL, "bibd batch: nrows out of range");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->d_words + c->n_words, c->h_words + c->n_words, (size_t)bt->n * bt->v * 8,
+                            cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->d_bitems + c->n_bitems, c->h_bitems + c->n_bitems, (size_t)bt->n * sizeof(Item),
+                            cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "bibd batch upload");
+    const uint8_t f = (uint8_t)bt->flags;
+    c->q_two_pass = c->q_two_pass && (f & (canon::F_AUT_CANON | canon::F_FULL_AUT)) &&
+                    !(f & (canon::F_SAVE_AUTS | canon::F_REFERENCE_ORDER));
+    c->q_want_auts = c->q_want_auts || (f & canon::F_SAVE_AUTS);
+    c->q_max_b = std::max(c->q_max_b, bt->b);
+    // the widest filled-row count decides the kernel's row capacity, as the rows read
+    uint32_t mv = bt->v;
+    if (bt->nrows) {
+        mv = 0;
+        for (uint32_t i = 0; i < bt->n && mv < bt->v; ++i)
+            mv = std::max<uint32_t>(mv, bt->nrows[i]);
+    }
+    c->q_max_v = std::max(c->q_max_v, mv);
     c->n_words += bt->n * bt->v;
     c->n_bitems += bt->n;
     c->item_kind.insert(c->item_kind.end(), bt->n, canon::KIND_BIBD);
@@ -353,25 +384,46 @@ int canon_submit_ksys(canon_ctx *c, const canon_ksys_batch *bt) {
         return fail(c, CANON_ENOMEM, "item capacity exceeded (canon_cfg.max_items)");
     if ((uint64_t)c->n_bytes + bytes > c->max_bytes)
         return fail(c, CANON_ENOMEM, "byte capacity exceeded (8 * canon_cfg.max_words)");
-    for (uint32_t i = 0; i < bt->n; ++i) {
-        const uint32_t nr = bt->nrows ? bt->nrows[i] : bt->rounds;
-        if (nr < 1 || nr > bt->rounds)
-            return fail(c, CANON_EINVAL, "ksys batch: nrows out of range");
-    }
     const uint64_t per = (uint64_t)bt->rounds * bt->np;
+    std::atomic<bool> bad{false};
     pack_parallel(bt->n, [&](uint64_t lo, uint64_t hi) {
         std::memcpy(c->h_bytes + c->n_bytes + lo * per, bt->data + lo * per, (size_t)((hi - lo) * per));
+        bool ok = true;
         for (uint64_t i = lo; i < hi; ++i) {
+            const uint32_t nr = bt->nrows ? bt->nrows[i] : bt->rounds;
+            ok = ok && nr >= 1 && nr <= bt->rounds;
             Item it{};
             it.data_off = c->n_bytes + (uint32_t)(i * per);
             it.kind = canon::KIND_KSYS;
-            it.nrows = (uint8_t)(bt->nrows ? bt->nrows[i] : bt->rounds);
+            it.nrows = (uint8_t)nr;
             it.ncols = (uint8_t)bt->np;
             it.flags = (uint8_t)bt->flags;
             it.out_idx = total + (uint32_t)i;
             c->h_kitems[c->n_kitems + i] = it;
         }
+        if (!ok)
+            bad.store(true, std::memory_order_relaxed);
     });
+    if (bad.load())
+        return fail(c, CANON_EINVAL, "ksys batch: nrows out of range");
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->d_bytes + c->n_bytes, c->h_bytes + c->n_bytes, (size_t)bytes, cudaMemcpyHostToDevice,
+                            c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(c->d_kitems + c->n_kitems, c->h_kitems + c->n_kitems, (size_t)bt->n * sizeof(Item),
+                            cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(c, e, "ksys batch upload");
+    c->q_want_auts = c->q_want_auts || (bt->flags & canon::F_SAVE_AUTS);
+    c->q_ks_np = std::max(c->q_ks_np, bt->np);
+    uint32_t mr = bt->rounds;
+    if (bt->nrows) {
+        mr = 0;
+        for (uint32_t i = 0; i < bt->n && mr < bt->rounds; ++i)
+            mr = std::max<uint32_t>(mr, bt->nrows[i]);
+    }
+    c->q_ks_nr = std::max(c->q_ks_nr, mr);
     c->n_bytes += (uint32_t)bytes;
     c->n_kitems += bt->n;
     c->item_kind.insert(c->item_kind.end(), bt->n, canon::KIND_KSYS);
@@ -385,58 +437,69 @@ int canon_sync(canon_ctx *c, canon_results *r) {
     if (e != cudaSuccess)
         return cuda_fail(c, e, "cudaSetDevice");
     const uint32_t n = c->n_bitems + c->n_kitems;
+    const bool verdict_sync = c->cfg.options & CANON_OPT_VERDICT_SYNC;
     std::memset(r, 0, sizeof(*r));
     if (n) {
         cudaStream_t s = c->stream;
-        if (c->n_bitems)
-            cudaMemcpyAsync(c->d_bitems, c->h_bitems, c->n_bitems * sizeof(Item), cudaMemcpyHostToDevice, s);
-        if (c->n_kitems)
-            cudaMemcpyAsync(c->d_kitems, c->h_kitems, c->n_kitems * sizeof(Item), cudaMemcpyHostToDevice, s);
-        if (c->n_words)
-            cudaMemcpyAsync(c->d_words, c->h_words, c->n_words * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
-        if (c->n_bytes)
-            cudaMemcpyAsync(c->d_bytes, c->h_bytes, c->n_bytes, cudaMemcpyHostToDevice, s);
+        if (c->q_reupload) {
+            // the device staging was borrowed after the batches were queued: copy them again
+            if (c->n_bitems)
+                cudaMemcpyAsync(c->d_bitems, c->h_bitems, c->n_bitems * sizeof(Item), cudaMemcpyHostToDevice, s);
+            if (c->n_kitems)
+                cudaMemcpyAsync(c->d_kitems, c->h_kitems, c->n_kitems * sizeof(Item), cudaMemcpyHostToDevice, s);
+            if (c->n_words)
+                cudaMemcpyAsync(c->d_words, c->h_words, c->n_words * sizeof(uint64_t), cudaMemcpyHostToDevice, s);
+            if (c->n_bytes)
+                cudaMemcpyAsync(c->d_bytes, c->h_bytes, c->n_bytes, cudaMemcpyHostToDevice, s);
+            e = cudaGetLastError();
+            if (e != cudaSuccess)
+                return cuda_fail(c, e, "canon_sync upload");
+        }
         cudaEventRecord(c->ev0, s);
         if (c->n_bitems && c->n_kitems) {
             // uneven batch: one persistent launch for both kinds, sized by the widest
             // incidence item
-            uint32_t mb = 0, mv = 0;
-            for (uint32_t i = 0; i < c->n_bitems; ++i) {
-                mb = std::max<uint32_t>(mb, c->h_bitems[i].ncols);
-                mv = std::max<uint32_t>(mv, c->h_bitems[i].nrows);
-            }
             e = canon::launch_mixed_check(c->d_bitems, c->n_bitems, c->d_kitems, c->n_kitems, c->d_words,
-                                          c->d_bytes, c->d_out, c->cfg.max_trials, c->d_ticket, c->num_sms, s, mb,
-                                          mv);
+                                          c->d_bytes, c->d_out, c->cfg.max_trials, c->d_ticket, c->num_sms, s,
+                                          c->q_max_b, c->q_max_v);
             if (e != cudaSuccess)
                 return cuda_fail(c, e, "mixed check launch");
             ++c->launches;
         } else if (c->n_bitems) {
             // items that all want |Aut| without the reference order take the two-pass check
-            bool two_pass = true;
-            uint32_t max_b = 0, max_v = 0;
-            for (uint32_t i = 0; i < c->n_bitems; ++i) {
-                const uint8_t f = c->h_bitems[i].flags;
-                two_pass = two_pass && (f & (canon::F_AUT_CANON | canon::F_FULL_AUT)) &&
-                           !(f & (canon::F_SAVE_AUTS | canon::F_REFERENCE_ORDER));
-                if (c->h_bitems[i].ncols > max_b)
-                    max_b = c->h_bitems[i].ncols;
-                if (c->h_bitems[i].nrows > max_v)
-                    max_v = c->h_bitems[i].nrows;
-            }
+            const bool two_pass = c->q_two_pass;
             e = two_pass ? canon::launch_bibd_check_two_pass(c->d_bitems, c->n_bitems, c->d_words, c->d_out,
-                                                             c->cfg.max_trials, c->d_ticket, c->num_sms, s, max_b, max_v)
+                                                             c->cfg.max_trials, c->d_ticket, c->num_sms, s, c->q_max_b,
+                                                             c->q_max_v)
                          : canon::launch_bibd_check(c->d_bitems, c->n_bitems, c->d_words, c->d_out,
                                                     c->cfg.max_trials, c->d_ticket, c->num_sms, s);
             if (e != cudaSuccess)
                 return cuda_fail(c, e, "bibd check launch");
             c->launches += two_pass ? 2 : 1;
         } else if (c->n_kitems) {
-            e = canon::launch_ksys_check(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, c->d_ticket + 1,
-                                         c->num_sms, s);
+            const uint32_t seg =
+                c->q_want_auts ? 0u : canon::ksys_segment(c, c->n_kitems, c->q_ks_np, c->q_ks_nr);
+            if (seg) {
+                if (c->kseg_cap < (size_t)c->n_kitems + 1) {
+                    cudaFree(c->d_kseg);
+                    c->d_kseg = nullptr;
+                    c->kseg_cap = 0;
+                    e = cudaMalloc(&c->d_kseg, ((size_t)c->n_kitems + 1) * sizeof(canon::KsysSeg));
+                    if (e != cudaSuccess)
+                        return cuda_fail(c, e, "k-system segment state");
+                    c->kseg_cap = (size_t)c->n_kitems + 1;
+                }
+                e = canon::launch_ksys_check_split(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, seg,
+                                                   canon::ksys_candidates(c->q_ks_np, c->q_ks_nr), c->d_kseg,
+                                                   c->num_sms, s);
+                c->launches += 3;
+            } else {
+                e = canon::launch_ksys_check(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, c->d_ticket + 1,
+                                             c->num_sms, s);
+                ++c->launches;
+            }
             if (e != cudaSuccess)
                 return cuda_fail(c, e, "ksys check launch");
-            ++c->launches;
         }
         cudaEventRecord(c->ev1, s);
         const Outputs &d = c->d_out, &h = c->h_out;
@@ -444,20 +507,18 @@ int canon_sync(canon_ctx *c, canon_results *r) {
     cudaMemcpyAsync(h.field, d.field, (size_t)(count) * sizeof(*h.field), cudaMemcpyDeviceToHost, s)
         CANON_D2H(canonical, n);
         CANON_D2H(status, n);
-        CANON_D2H(reject_row, n);
-        CANON_D2H(row_to_change, n);
-        CANON_D2H(player_index, n);
-        CANON_D2H(witness, n * 16);
-        CANON_D2H(aut, n * 2);
-        CANON_D2H(trials, n);
-        CANON_D2H(n_auts, n);
-        CANON_D2H(len_aut, n);
+        if (!verdict_sync) {
+            CANON_D2H(reject_row, n);
+            CANON_D2H(row_to_change, n);
+            CANON_D2H(player_index, n);
+            CANON_D2H(witness, n * 16);
+            CANON_D2H(aut, n * 2);
+            CANON_D2H(trials, n);
+            CANON_D2H(n_auts, n);
+            CANON_D2H(len_aut, n);
+        }
 #undef CANON_D2H
-        bool want_auts = false;
-        for (uint32_t i = 0; i < c->n_bitems && !want_auts; ++i)
-            want_auts = c->h_bitems[i].flags & canon::F_SAVE_AUTS;
-        for (uint32_t i = 0; i < c->n_kitems && !want_auts; ++i)
-            want_auts = c->h_kitems[i].flags & canon::F_SAVE_AUTS;
+        const bool want_auts = c->q_want_auts && !verdict_sync;
         if (want_auts)
             cudaMemcpyAsync(h.auts, d.auts, (size_t)n * c->cfg.aut_cap * 64, cudaMemcpyDeviceToHost, s);
         e = cudaStreamSynchronize(s);
@@ -496,14 +557,32 @@ int canon_sync(canon_ctx *c, canon_results *r) {
     r->aut_cap = c->cfg.aut_cap;
     r->kernel_ms = c->last_ms;
     c->n_bitems = c->n_kitems = c->n_words = c->n_bytes = 0;
+    c->q_max_b = c->q_max_v = c->q_ks_np = c->q_ks_nr = 0;
+    c->q_two_pass = true;
+    c->q_want_auts = c->q_reupload = false;
     c->item_kind.clear();
-    int rc = CANON_OK;
-    for (uint32_t i = 0; i < n; ++i)
-        if (c->h_out.status[i] & canon::ST_TIMEOUT)
-            rc = CANON_ETIMEOUT;
-    if (rc != CANON_OK)
+    // any item out of trial budget: eight status bytes at a time
+    uint64_t any = 0;
+    uint32_t i = 0;
+    for (; i + 8 <= n; i += 8) {
+        uint64_t w;
+        std::memcpy(&w, c->h_out.status + i, 8);
+        any |= w;
+    }
+    for (; i < n; ++i)
+        any |= c->h_out.status[i];
+    if (any & 0x0202020202020202ull) {
         c->err = "a search hit the trial budget (canon_cfg.max_trials)";
-    return rc;
+        return CANON_ETIMEOUT;
+    }
+    return CANON_OK;
+}
+
+int canon_set_ksys_segment(canon_ctx *c, uint32_t cands) {
+    if (!c)
+        return CANON_EINVAL;
+    c->ksys_seg = cands;
+    return CANON_OK;
 }
 
 int canon_set_ordering(canon_ctx *c, const canon_mlp_weights *w) {
@@ -552,6 +631,9 @@ int canon_canonize_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint64
         return fail(c, CANON_ENOMEM, "canonize: batch exceeds context capacity");
     cudaSetDevice(c->device);
     cudaStream_t s = c->stream;
+    // borrows the device staging of queued batches: canon_sync copies them again
+    if (c->n_words)
+        c->q_reupload = true;
     cudaMemcpyAsync(c->d_words, rows, (size_t)n * v * 8, cudaMemcpyHostToDevice, s);
     cudaEventRecord(c->ev0, s);
     cudaError_t e = canon::launch_bibd_canonize(n, v, b, c->d_words, c->d_out.aut, c->d_out.status, 1, 0,
@@ -1119,6 +1201,29 @@ int canon_check_bibd_noalloc(uint32_t n, uint32_t v, uint32_t b, uint32_t flags,
 }  // extern "C"
 
 namespace canon {
+
+// Candidates per warp task of a k-system check.  A matrix whose rounds are all
+// canonical tries every one of its ng! * 2^ng * rounds relabelings, so a batch of
+// fewer matrices than the GPU holds warps leaves it mostly idle with one warp per
+// matrix; cutting the candidates into segments gives about 8 warp tasks per resident
+// warp.  Segments of fewer than 256 candidates cost more in set-up (the rounds'
+// tables) than they spread.
+uint32_t ksys_segment(const canon_ctx *c, uint64_t n, uint32_t np, uint32_t rounds) {
+    if (c->ksys_seg == CANON_KSYS_WHOLE || !n || !np || !rounds)
+        return 0;
+    const uint64_t total = ksys_candidates(np, rounds);
+    uint64_t seg;
+    if (c->ksys_seg) {
+        seg = ((uint64_t)c->ksys_seg + 31u) & ~31ull;
+    } else {
+        const uint64_t resident = (uint64_t)(c->num_sms > 0 ? c->num_sms : 1) * 64u;
+        seg = total * n / (8u * resident);
+        seg &= ~31ull;
+        if (seg < 256)
+            seg = 256;
+    }
+    return seg >= total ? 0u : (uint32_t)seg;
+}
 
 // The largest batch of matrices with `words` 64-bit words (BIBD) or `bytes` bytes
 // (k-systems) each that one canon_submit_* call can queue on an empty context.

@@ -19,6 +19,21 @@ struct canon_ctx {
     uint8_t *h_bytes = nullptr;
     uint32_t n_bitems = 0, n_kitems = 0, n_words = 0, n_bytes = 0;
     uint32_t max_bytes = 0;
+    // what the queued batches need, kept at submit so that canon_sync reads no item:
+    // widest incidence shape, whether every incidence item takes the two-pass check,
+    // whether any item stores automorphisms
+    uint32_t q_max_b = 0, q_max_v = 0;
+    bool q_two_pass = true, q_want_auts = false;
+    // the queued input is copied to the GPU at submit; a call that borrows the device
+    // staging in between (canon_canonize_bibd) makes canon_sync copy it all again
+    bool q_reupload = false;
+    // k-system items queued: widest players and filled rounds (the segmented check's size)
+    uint32_t q_ks_np = 0, q_ks_nr = 0;
+    // candidates per warp task of the k-system check (canon_set_ksys_segment):
+    // 0 = chosen per launch, CANON_KSYS_WHOLE = one warp per matrix
+    uint32_t ksys_seg = 0;
+    canon::KsysSeg *d_kseg = nullptr;
+    size_t kseg_cap = 0;
     // device buffers
     canon::Item *d_bitems = nullptr, *d_kitems = nullptr;
     uint64_t *d_words = nullptr;
@@ -45,3 +60,9 @@ struct canon_ctx {
     float last_ms = 0.f;
     uint64_t launches = 0;
 };
+
+namespace canon {
+// candidates per warp task for a k-system check of n items of np players and
+// `rounds` rounds (0 = one warp per matrix)
+uint32_t ksys_segment(const canon_ctx *c, uint64_t n, uint32_t np, uint32_t rounds);
+}  // namespace canon

@@ -135,5 +135,26 @@ cudaError_t launch_mixed_check(const Item *d_bitems, uint32_t nb, const Item *d_
                                uint64_t max_trials, unsigned *d_ticket, int num_sms, cudaStream_t s,
                                uint32_t max_b = 63, uint32_t max_v = 16);
 cudaError_t ksys_upload_tables();
+// per-item state of the segmented k-system check: the first rejection as
+// (candidate << 32 | player index), all ones while none; automorphisms counted;
+// ill-formed rounds
+struct KsysSeg {
+    unsigned long long key;
+    unsigned n_aut;
+    unsigned bad;
+};
+// the k-system check with every item's candidates split into segments of seg_cands
+// (a multiple of 32) taken by different warps; d_state holds n_items + 1 entries;
+// total_max = the most candidates of any item.  Automorphisms are not stored.
+cudaError_t launch_ksys_check_split(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes, Outputs out,
+                                   uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
+                                   cudaStream_t s);
+// candidates of one k-system check: ng! * 2^ng * rounds
+inline uint64_t ksys_candidates(uint32_t np, uint32_t rounds) {
+    uint64_t f = 1;
+    for (uint32_t i = 2; i <= np / 2; ++i)
+        f *= i;
+    return (f << (np / 2)) * rounds;
+}
 
 }  // namespace canon

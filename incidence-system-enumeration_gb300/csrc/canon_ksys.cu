@@ -38,6 +38,103 @@ __global__ void __launch_bounds__(KTPB) ksys_kernel(const Item *__restrict__ ite
     }
 }
 
+// Every item's state: no rejection yet (key = all ones), no automorphism, well formed.
+__global__ void ksys_seg_init_kernel(KsysSeg *state, uint32_t n_items) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += gridDim.x * blockDim.x)
+        state[i] = KsysSeg{~0ull, 0u, 0u};
+}
+
+__device__ __forceinline__ unsigned long long volatile_key(const unsigned long long *p) {
+    return *reinterpret_cast<const volatile unsigned long long *>(p);
+}
+
+// The check of a batch with every matrix's candidates split into segments: the
+// unit of work is one (segment, item) pair, taken in segment-major order from a
+// 64-bit work counter, so a level of a few hundred matrices whose canonical members
+// try all ng! * 2^ng * rounds relabelings still fills the GPU.  Every segment's
+// warp publishes a rejection as the key (candidate << 32 | player index) with an
+// atomic minimum, and skips chunks that start after the smallest key seen: every
+// candidate before the first rejecting one is still evaluated, so the verdict,
+// m_playerIndex, the relabelings tried and |Aut| are those of the one-warp check.
+__global__ void __launch_bounds__(KTPB) ksys_seg_kernel(const Item *__restrict__ items, uint32_t n_items,
+                                                        const uint8_t *__restrict__ bytes, uint32_t seg_cands,
+                                                        uint64_t n_units, KsysSeg *state,
+                                                        unsigned long long *ticket) {
+    __shared__ uint64_t s_seq[KW][16], s_part[KW][16], s_pair[KW][16];
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0)
+            t = atomicAdd(ticket, 1ull);
+        t = __shfl_sync(0xFFFFFFFFu, t, 0);
+        if (t >= n_units)
+            break;
+        const uint32_t it = (uint32_t)(t % n_items);
+        const uint32_t seg = (uint32_t)(t / n_items);
+        const Item item = items[it];
+        const unsigned np = item.ncols, nr = item.nrows, ng = np >> 1;
+        KsysSeg &st = state[it];
+        const uint64_t start = (uint64_t)seg * seg_cands;
+        // past this item's candidates (a smaller shape than the launch's widest)
+        if (seg && np >= 4 && np <= KS_NPMAX && start >= (uint64_t)(c_fact[ng] << ng) * nr)
+            continue;
+        // rejected before this segment
+        if ((volatile_key(&st.key) >> 32) < start)
+            continue;
+        bool consecutive = false;
+        const bool ok = load_item(item, bytes, s_seq[warp], s_part[warp], s_pair[warp], lane, &consecutive);
+        if (!ok) {
+            if (lane == 0 && seg == 0)
+                st.bad = 1u;
+            continue;
+        }
+        const uint64_t total = (uint64_t)(c_fact[ng] << ng) * nr;
+        const uint64_t end = start + seg_cands < total ? start + seg_cands : total;
+        const int pidx0 = (int)(nr * np) - 2 - 1;
+        unsigned n_aut = 0;
+        for (uint64_t base = start; base < end; base += 32u) {
+            if ((volatile_key(&st.key) >> 32) < base)
+                break;
+            const unsigned c = (unsigned)base + lane;
+            Cand o;
+            o.res = 1;
+            if (c < end)
+                eval_candidate(c, np, ng, nr, s_seq[warp], s_part[warp], s_pair[warp], consecutive, o);
+            const unsigned rej = __ballot_sync(0xFFFFFFFFu, c < end && o.res < 0);
+            unsigned aut = __ballot_sync(0xFFFFFFFFu, c < end && o.res == 0);
+            if (rej) {
+                const unsigned fl = __ffs(rej) - 1u;
+                if (lane == fl) {
+                    const int pi = player_index_of(o, np, s_seq[warp], pidx0);
+                    atomicMin(&st.key, ((unsigned long long)c << 32) | (unsigned)pi);
+                }
+                break;   // the automorphisms of a rejected matrix are not reported
+            }
+            n_aut += __popc(aut);
+        }
+        if (lane == 0 && n_aut)
+            atomicAdd(&st.n_aut, n_aut);
+    }
+}
+
+// The outputs of the segmented check, one thread per item.
+__global__ void ksys_seg_finish_kernel(const Item *__restrict__ items, uint32_t n_items, const KsysSeg *state,
+                                       Outputs out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += gridDim.x * blockDim.x) {
+        const Item item = items[i];
+        const KsysSeg st = state[i];
+        const unsigned np = item.ncols, nr = item.nrows, ng = np >> 1;
+        const bool ok = !st.bad && item.kind == KIND_KSYS && np >= 4 && np <= KS_NPMAX && !(np & 1u) && nr >= 1 &&
+                        nr < np;
+        const bool canonical = ok && st.key == ~0ull;
+        const uint64_t total = ok ? (uint64_t)(c_fact[ng] << ng) * nr : 0;
+        // candidate 0 (the identity) is not compared
+        const uint64_t cands = !ok ? 0 : canonical ? total - 1 : (st.key >> 32);
+        const int pidx = canonical || !ok ? (int)(nr * np) - 2 - 1 : (int)(uint32_t)st.key;
+        write_item(out, item.out_idx, ok, canonical, false, pidx, st.n_aut, cands, false, np);
+    }
+}
+
 // One persistent kernel over a mixed batch (k-systems and incidence matrices of
 // any shapes): every warp first takes k-system items from the first work counter,
 // one warp per matrix, and then incidence matrices from the second, one thread
@@ -177,6 +274,47 @@ cudaError_t launch_ksys_check(const Item *d_items, uint32_t n_items, const uint8
     if (grid > need)
         grid = need;
     ksys_kernel<<<grid, ksys::KTPB, 0, s>>>(d_items, n_items, d_bytes, out, tk);
+    return cudaGetLastError();
+}
+
+// seg_cands: candidates per segment (a multiple of 32); total_max: the most
+// candidates of any item (ng! * 2^ng * rounds), which sets the segments per item
+cudaError_t launch_ksys_check_split(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes, Outputs out,
+                                   uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
+                                   cudaStream_t s) {
+    if (!n_items)
+        return cudaSuccess;
+    if (seg_cands < 32 || (seg_cands & 31u))
+        return cudaErrorInvalidValue;
+    const uint64_t n_seg = (total_max + seg_cands - 1) / seg_cands;
+    // the work counter after the items' states (which the init kernel sets)
+    cudaError_t e = cudaMemsetAsync(d_state + n_items, 0, sizeof(KsysSeg), s);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ksys_seg_kernel, ksys::KTPB, 0);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        per_sm = 1;
+    const uint64_t units = n_seg * n_items;
+    uint64_t grid = (uint64_t)per_sm * (num_sms > 0 ? num_sms : 1);
+    const uint64_t need = (units + ksys::KW - 1) / ksys::KW;
+    if (grid > need)
+        grid = need;
+    int gi = (int)((n_items + 255) / 256);
+    if (gi > 4 * num_sms)
+        gi = 4 * (num_sms > 0 ? num_sms : 1);
+    ksys_seg_init_kernel<<<gi, 256, 0, s>>>(d_state, n_items);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    unsigned long long *ticket = reinterpret_cast<unsigned long long *>(d_state + n_items);
+    ksys_seg_kernel<<<(int)grid, ksys::KTPB, 0, s>>>(d_items, n_items, d_bytes, seg_cands, units, d_state, ticket);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    ksys_seg_finish_kernel<<<gi, 256, 0, s>>>(d_items, n_items, d_state, out);
     return cudaGetLastError();
 }
 

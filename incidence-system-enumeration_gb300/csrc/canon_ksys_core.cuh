@@ -141,13 +141,15 @@ __device__ int player_index_of(const Cand &o, unsigned np, const uint64_t *seq, 
     return pi < current ? pi : current;
 }
 
-// cnvCheckNew() of one item by one warp (all 32 lanes call it together).
-__device__ void check_item_warp(const Item &item, const uint8_t *__restrict__ bytes, Outputs out,
-                                uint64_t *seq, uint64_t *part, uint64_t *pair, unsigned lane) {
-    const unsigned np = item.ncols, nr = item.nrows, ng = np >> 1;
-    const unsigned oi = item.out_idx;
+// Loads one item's rounds into the warp's tables (all 32 lanes call it together):
+// seq = position -> player, part = player -> partner per round, pair = for every
+// player the round (+1) in which it meets each partner.  Returns whether the rounds
+// are well formed; *consecutive = round i pairs player 0 with i+1 (every canonical
+// matrix does), which allows the fast comparison path.
+__device__ bool load_item(const Item &item, const uint8_t *__restrict__ bytes, uint64_t *seq, uint64_t *part,
+                          uint64_t *pair, unsigned lane, bool *consecutive) {
+    const unsigned np = item.ncols, nr = item.nrows;
     bool ok = item.kind == KIND_KSYS && np >= 4 && np <= KS_NPMAX && !(np & 1u) && nr >= 1 && nr < np;
-    // load rounds: position -> player (seq) and player -> partner (part)
     if (ok && lane < nr) {
         const uint8_t *row = bytes + item.data_off + lane * np;
         uint64_t sq = 0, pt = 0, seen = 0;
@@ -173,9 +175,7 @@ __device__ void check_item_warp(const Item &item, const uint8_t *__restrict__ by
         part[lane] = pt;
     }
     ok = __all_sync(0xFFFFFFFFu, ok);
-    // fast path when round i pairs player 0 with i+1 (every canonical matrix does)
-    const bool consecutive =
-        __all_sync(0xFFFFFFFFu, !(ok && lane < nr) || nib_get(part[lane], 0) == lane + 1u);
+    *consecutive = __all_sync(0xFFFFFFFFu, !(ok && lane < nr) || nib_get(part[lane], 0) == lane + 1u);
     __syncwarp();
     if (ok && lane < np) {
         uint64_t pr = 0;
@@ -189,6 +189,33 @@ __device__ void check_item_warp(const Item &item, const uint8_t *__restrict__ by
     }
     ok = __all_sync(0xFFFFFFFFu, ok);
     __syncwarp();
+    return ok;
+}
+
+// The outputs of one k-system item (one thread writes them).
+__device__ __forceinline__ void write_item(const Outputs &out, unsigned oi, bool ok, bool canonical, bool overflow,
+                                           int pidx, uint64_t n_aut, uint64_t cands, bool save, unsigned np) {
+    out.canonical[oi] = canonical ? 1 : 0;
+    out.status[oi] = ok ? (overflow ? ST_PERM_OVF : 0) : ST_BADINPUT;
+    out.reject_row[oi] = 0xFF;
+    out.row_to_change[oi] = 0xFF;
+    out.player_index[oi] = pidx;
+    uint4 *w = reinterpret_cast<uint4 *>(out.witness + (size_t)oi * 16u);
+    *w = make_uint4(~0u, ~0u, ~0u, ~0u);
+    out.aut[2 * (size_t)oi] = canonical ? n_aut : 0;
+    out.aut[2 * (size_t)oi + 1] = 0;
+    out.trials[oi] = cands;
+    out.n_auts[oi] = (uint16_t)(save ? (n_aut < out.aut_cap ? n_aut : out.aut_cap) : 0);
+    out.len_aut[oi] = (uint8_t)np;
+}
+
+// cnvCheckNew() of one item by one warp (all 32 lanes call it together).
+__device__ void check_item_warp(const Item &item, const uint8_t *__restrict__ bytes, Outputs out,
+                                uint64_t *seq, uint64_t *part, uint64_t *pair, unsigned lane) {
+    const unsigned np = item.ncols, nr = item.nrows, ng = np >> 1;
+    const unsigned oi = item.out_idx;
+    bool consecutive = false;
+    bool ok = load_item(item, bytes, seq, part, pair, lane, &consecutive);
 
     int pidx = (int)(nr * np) - 2 - 1;      // cnvCheckNew(): nrows*numPlayers - groupSize - 1
     uint64_t n_aut = 0, cands = 0;
@@ -233,20 +260,8 @@ __device__ void check_item_warp(const Item &item, const uint8_t *__restrict__ by
         if (save && n_aut > out.aut_cap)
             overflow = true;
     }
-    if (lane == 0) {
-        out.canonical[oi] = canonical ? 1 : 0;
-        out.status[oi] = ok ? (overflow ? ST_PERM_OVF : 0) : ST_BADINPUT;
-        out.reject_row[oi] = 0xFF;
-        out.row_to_change[oi] = 0xFF;
-        out.player_index[oi] = pidx;
-        uint4 *w = reinterpret_cast<uint4 *>(out.witness + (size_t)oi * 16u);
-        *w = make_uint4(~0u, ~0u, ~0u, ~0u);
-        out.aut[2 * (size_t)oi] = canonical ? n_aut : 0;
-        out.aut[2 * (size_t)oi + 1] = 0;
-        out.trials[oi] = cands;
-        out.n_auts[oi] = (uint16_t)(save ? (n_aut < out.aut_cap ? n_aut : out.aut_cap) : 0);
-        out.len_aut[oi] = (uint8_t)np;
-    }
+    if (lane == 0)
+        write_item(out, oi, ok, canonical, overflow, pidx, n_aut, cands, save, np);
 }
 
 }  // namespace

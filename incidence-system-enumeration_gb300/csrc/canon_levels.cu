@@ -752,6 +752,7 @@ extern "C" int canon_enumerate_ksys(canon_ctx *c, uint32_t np, canon_design_cb c
     DevBuf<canon::Item> items;
     DevBuf<unsigned> ticket;
     DevBuf<unsigned long long> tsum;
+    DevBuf<canon::KsysSeg> kseg;
     cudaEvent_t e0 = nullptr, e1 = nullptr, g0 = nullptr, g1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -872,9 +873,15 @@ extern "C" int canon_enumerate_ksys(canon_ctx *c, uint32_t np, canon_design_cb c
             o.len_aut = len_aut.p;
             o.auts = nullptr;
             o.aut_cap = 0;
+            // one warp per matrix, or the candidates of every matrix split over warps
+            const uint32_t seg = canon::ksys_segment(c, ns, np, m);
+            if (e == cudaSuccess && seg)
+                e = kseg.ensure(ns + 1);
             cudaEventRecord(e0, s);
             if (e == cudaSuccess)
-                e = canon::launch_ksys_check(items.p, (uint32_t)ns, cand.p, o, ticket.p, c->num_sms, s);
+                e = seg ? canon::launch_ksys_check_split(items.p, (uint32_t)ns, cand.p, o, seg,
+                                                         canon::ksys_candidates(np, m), kseg.p, c->num_sms, s)
+                        : canon::launch_ksys_check(items.p, (uint32_t)ns, cand.p, o, ticket.p, c->num_sms, s);
             cudaEventRecord(e1, s);
             // 4: the canonical ones into the next level
             if (e == cudaSuccess)

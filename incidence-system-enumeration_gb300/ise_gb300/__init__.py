@@ -59,7 +59,7 @@ HEADER_SYMBOLS = [
     "canon_label_first_rows", "canon_mlp_forward", "canon_mlp_grad", "canon_mlp_train",
     "canon_design_properties", "canon_report_bibd", "canon_ksys_cycles", "canon_report_ksys",
     "canon_tune_bibd", "canon_generate_partial_bibd", "canon_generate_partial_ksys", "canon_lexmax_nodes_bibd",
-    "canon_measure_int_peak", "canon_canonize_ksys_binary",
+    "canon_measure_int_peak", "canon_canonize_ksys_binary", "canon_set_ksys_segment",
 ]
 # the reference's plugin (k-Factorization/Utils/Include/CDTools.h:9-11)
 PLUGIN_SYMBOLS = ["createCanonizer", "releaseCanonizer", "runCanonizer"]
@@ -79,6 +79,8 @@ class Cfg(ctypes.Structure):
 
 
 OPT_AUT_PRUNE = 0x1
+OPT_VERDICT_SYNC = 0x2    # canon_sync returns only canonical + status
+KSYS_WHOLE = 0xFFFFFFFF   # canon_set_ksys_segment: one warp per matrix
 
 
 class BibdBatch(ctypes.Structure):
@@ -191,6 +193,7 @@ def load_library(path=LIB_PATH):
     L.canon_mlp_grad.argtypes = [vp, u64, vp, vp, fp, fp, fp]
     L.canon_mlp_train.argtypes = [vp, u64, vp, vp, u32, u32, ctypes.c_float, fp, fp]
     L.canon_set_ordering.argtypes = [vp, ctypes.POINTER(MlpWeights)]
+    L.canon_set_ksys_segment.argtypes = [vp, u32]
     u8p, sz = ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t
     L.canon_tune_bibd.argtypes = [vp, u32, u32, u32, u32, vp, ctypes.POINTER(TuneResult)]
     L.canon_design_properties.argtypes = [vp, u32, u32, u32, u64p, u8p, u8p]
@@ -543,6 +546,11 @@ class Context:
         self._check(self.lib.canon_mlp_train(self.h, n, d_x, d_labels, epochs, batch, lr,
                                              _ptr(params, ctypes.c_float), _ptr(losses, ctypes.c_float)))
         return params, losses
+
+    def set_ksys_segment(self, cands):
+        """Candidates per warp task of the k-system check: 0 = chosen per launch,
+        KSYS_WHOLE = one warp per matrix (canon_set_ksys_segment)."""
+        self._check(self.lib.canon_set_ksys_segment(self.h, cands))
 
     def set_ordering(self, params):
         """Install (or with None remove) the learned first-row order from flat FP32 params."""

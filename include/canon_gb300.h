@@ -105,6 +105,11 @@ typedef struct {
  * one automorphism search per parent of the shallow levels, whose latency outweighs the
  * saving on the families measured; hence an option. */
 #define CANON_OPT_AUT_PRUNE 0x1u
+/* canon_sync copies back only `canonical` and `status`, the two arrays a caller that
+ * keeps the canonical matrices of a level reads (Enumerator.cpp:446-447 keeps a
+ * partial matrix when TestCanonicity() returns true): 2 bytes per item instead of
+ * 51.  The other result arrays are not updated and their contents are undefined. */
+#define CANON_OPT_VERDICT_SYNC 0x2u
 
 /* BIBD / incidence-system batch: n matrices of b columns (b <= 63), v rows each
  * (v <= 16), row j of matrix i at rows[i*v + j] with bit c = column c.
@@ -170,6 +175,15 @@ int canon_submit_bibd(canon_ctx *ctx, const canon_bibd_batch *batch);
 int canon_submit_ksys(canon_ctx *ctx, const canon_ksys_batch *batch);
 /* Copy the queued input to the GPU, run the checks, wait, expose the results. */
 int canon_sync(canon_ctx *ctx, canon_results *out);
+/* Work split of the k-system check (cnvCheckNew): the candidates of a matrix
+ * (ng! * 2^ng * rounds relabelings) are cut into segments of `cands` candidates
+ * (rounded up to a multiple of 32) that different warps take, so that a batch of a
+ * few hundred matrices fills the GPU.  0 (the default) chooses the segment per launch
+ * from the batch size; CANON_KSYS_WHOLE keeps one warp per matrix.  Every output is
+ * the same either way.  Batches that store automorphisms (CANON_SAVE_AUTS) and mixed
+ * batches always run one warp per matrix. */
+#define CANON_KSYS_WHOLE 0xFFFFFFFFu
+int canon_set_ksys_segment(canon_ctx *ctx, uint32_t cands);
 /* Install (or with NULL remove) the learned ordering network. */
 int canon_set_ordering(canon_ctx *ctx, const canon_mlp_weights *w);
 

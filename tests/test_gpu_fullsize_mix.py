@@ -35,6 +35,14 @@ def test_config3_full_mix_sample_matches_oracle():
     finally:
         ctx.close()
     assert r["n"] == n and not r["status"].any()
+    # the verdict-only sync (CANON_OPT_VERDICT_SYNC) returns the same verdicts
+    ctx = G.Context(max_items=n + 16, max_words=16 * n, aut_cap=1, options=G.OPT_VERDICT_SYNC)
+    try:
+        workloads.submit_mix(ctx, batches)
+        rv = ctx.sync(raw=True)
+    finally:
+        ctx.close()
+    assert np.array_equal(rv["canonical"], r["canonical"]) and np.array_equal(rv["status"], r["status"])
     off = 0
     with cf.ThreadPoolExecutor(os.cpu_count() or 1) as ex:
         for bt in batches:

@@ -303,3 +303,28 @@ def test_mixed_batch_one_persistent_launch(ctx):
         o = oracle.ksys_test(M[:k])
         assert bool(r["canonical"][i]) == o["canonical"] and int(r["player_index"][i]) == o["player_index"], i
         i += 1
+
+
+def test_queue_survives_a_refused_batch_and_a_canonisation(ctx):
+    """Batches are copied to the GPU when they are queued: a batch refused for a bad
+    row count leaves the queue as it was, and canon_canonize_bibd (which borrows the
+    device staging) between submit and sync makes the sync copy the queue again."""
+    sts = cases.load_sts15()
+    rng = np.random.default_rng(5)
+    mats = [sts[int(rng.integers(80))][0][rng.permutation(15)][:, rng.permutation(35)] for _ in range(12)]
+    rows = np.stack([G.pack_rows(M) for M in mats])
+    nr = np.full(12, 15, np.uint8)
+    ref = compare_bibd(ctx, mats, G.COMPLETE | G.RAW, 15, 35)
+    ctx.submit_bibd(rows[:6], 15, 35, G.COMPLETE | G.RAW, nr[:6])
+    bad = nr[6:].copy()
+    bad[3] = 16
+    with pytest.raises(G.CanonError):
+        ctx.submit_bibd(rows[6:], 15, 35, G.COMPLETE | G.RAW, bad)
+    ctx.submit_bibd(rows[6:], 15, 35, G.COMPLETE | G.RAW, nr[6:])
+    canon_rows, _ = ctx.canonize_bibd(rows[:4], 15, 35)
+    assert canon_rows.shape[0] == 4
+    r = ctx.sync()
+    assert r["n"] == 12
+    assert np.array_equal(r["canonical"], ref["canonical"])
+    assert np.array_equal(r["witness"], ref["witness"])
+    assert r["aut"] == ref["aut"]
