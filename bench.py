@@ -386,7 +386,10 @@ def run_enum(args):
     kind, params, desc = ENUM_WORKLOADS[args.workload]
     ctx = G.Context(max_items=1 << 20)
     runs = []
-    for _ in range(args.warmup + args.steps):
+    l0 = None
+    for i in range(args.warmup + args.steps):
+        if i == args.warmup:
+            l0 = ctx.kernel_launches()
         if kind == "bibd":
             found, st = ctx.enumerate_bibd(*params)
         else:
@@ -394,6 +397,7 @@ def run_enum(args):
         runs.append((len(found), st.checks, st.seconds, st.kernel_ms, st.batches,
                      [int(x) for x in st.level_checks], [round(float(x), 3) for x in st.level_kernel_ms],
                      st.gen_seconds, int(st.trials)))
+    launches = ctx.kernel_launches() - l0
     timed = runs[args.warmup:]
     secs = sum(r[2] for r in timed)
     checks = sum(r[1] for r in timed)
@@ -420,7 +424,7 @@ def run_enum(args):
                                              "level_checks": timed[0][5], "level_kernel_ms": timed[-1][6]},
             "checks_per_s": checks / secs, "kernel_ms_per_step": sum(r[3] for r in timed) / args.steps,
             "gen_ms_per_step": 1e3 * sum(r[7] for r in timed) / args.steps,
-            "cpu_baseline": cpu}
+            "cpu_baseline": cpu, "gpu_launches": launches}
     if kind == "ksys":
         # relabelings the checks tried (cnvCheckNew candidates), the k-system check's unit of work
         line["relabelings_tried_per_step"] = timed[0][8]

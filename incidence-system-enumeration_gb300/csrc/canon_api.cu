@@ -217,6 +217,9 @@ canon_ctx *canon_create(const canon_cfg *cfg) {
     if (!c->cfg.max_trials)
         c->cfg.max_trials = 1ull << 28;
     c->max_bytes = c->cfg.max_words * 8u;
+    // level capacity of the captured k-system enumeration: the context's item
+    // capacity, at most 64K matrices (it grows when a level does not fit)
+    c->ksys_graph_cap = std::min<uint64_t>(std::max<uint64_t>(c->cfg.max_items, 256), 1ull << 16);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= c->cfg.device || c->cfg.device < 0) {
         c->err = "no CUDA device";
@@ -272,6 +275,10 @@ void canon_destroy(canon_ctx *c) {
         cudaFree(c->d_split_parts);
         cudaFree(c->d_split_stop);
         cudaFree(c->d_kseg);
+    }
+    if (c && c->ksys_graph) {
+        cudaSetDevice(c->device);
+        canon::ksys_graph_release(c);
     }
     if (!c)
         return;
@@ -1205,23 +1212,14 @@ namespace canon {
 // Candidates per warp task of a k-system check.  A matrix whose rounds are all
 // canonical tries every one of its ng! * 2^ng * rounds relabelings, so a batch of
 // fewer matrices than the GPU holds warps leaves it mostly idle with one warp per
-// matrix; cutting the candidates into segments gives about 8 warp tasks per resident
-// warp.  Segments of fewer than 256 candidates cost more in set-up (the rounds'
-// tables) than they spread.
+// matrix; ksys_auto_segment cuts the candidates into segments.
 uint32_t ksys_segment(const canon_ctx *c, uint64_t n, uint32_t np, uint32_t rounds) {
     if (c->ksys_seg == CANON_KSYS_WHOLE || !n || !np || !rounds)
         return 0;
     const uint64_t total = ksys_candidates(np, rounds);
-    uint64_t seg;
-    if (c->ksys_seg) {
-        seg = ((uint64_t)c->ksys_seg + 31u) & ~31ull;
-    } else {
-        const uint64_t resident = (uint64_t)(c->num_sms > 0 ? c->num_sms : 1) * 64u;
-        seg = total * n / (8u * resident);
-        seg &= ~31ull;
-        if (seg < 256)
-            seg = 256;
-    }
+    const uint64_t seg = c->ksys_seg ? (((uint64_t)c->ksys_seg + 31u) & ~31ull)
+                                     : ksys_auto_segment(n, total, (uint32_t)(c->num_sms > 0 ? c->num_sms : 1) *
+                                                                       KSYS_RESIDENT_WARPS_PER_SM);
     return seg >= total ? 0u : (uint32_t)seg;
 }
 

@@ -34,6 +34,9 @@ struct canon_ctx {
     uint32_t ksys_seg = 0;
     canon::KsysSeg *d_kseg = nullptr;
     size_t kseg_cap = 0;
+    // the captured k-system enumeration (canon_levels.cu) and its level capacity
+    void *ksys_graph = nullptr;
+    uint64_t ksys_graph_cap = 1ull << 16;
     // device buffers
     canon::Item *d_bitems = nullptr, *d_kitems = nullptr;
     uint64_t *d_words = nullptr;
@@ -65,4 +68,6 @@ namespace canon {
 // candidates per warp task for a k-system check of n items of np players and
 // `rounds` rounds (0 = one warp per matrix)
 uint32_t ksys_segment(const canon_ctx *c, uint64_t n, uint32_t np, uint32_t rounds);
+// frees the captured k-system enumeration of a context
+void ksys_graph_release(canon_ctx *c);
 }  // namespace canon

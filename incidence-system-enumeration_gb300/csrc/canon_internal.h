@@ -144,11 +144,27 @@ struct KsysSeg {
     unsigned bad;
 };
 // the k-system check with every item's candidates split into segments of seg_cands
-// (a multiple of 32) taken by different warps; d_state holds n_items + 1 entries;
-// total_max = the most candidates of any item.  Automorphisms are not stored.
+// (a multiple of 32; 0 = chosen on the device by ksys_auto_segment) taken by different
+// warps; d_state holds n_items + 1 entries (the last is the work counter); total_max =
+// the most candidates of any item; d_n (optional) = the item count in device memory
+// (at most n_items).  Automorphisms are not stored.
 cudaError_t launch_ksys_check_split(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes, Outputs out,
                                    uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
-                                   cudaStream_t s);
+                                   cudaStream_t s, const uint64_t *d_n = nullptr);
+// warps of the segmented k-system kernel resident on one SM (128-thread blocks)
+constexpr uint32_t KSYS_RESIDENT_WARPS_PER_SM = 64;
+// Candidates per segment for n items of at most `total` candidates each: about 8
+// warp tasks per resident warp, segments of at least 256 candidates (fewer cost more
+// in set-up, the rounds' tables, than they spread); a segment that covers the whole
+// item is one warp per matrix.  The same rule on the host and on the device.
+__host__ __device__ inline uint32_t ksys_auto_segment(uint64_t n, uint64_t total, uint32_t resident_warps) {
+    uint64_t seg = total * n / (8ull * (resident_warps ? resident_warps : 1));
+    seg &= ~31ull;
+    if (seg < 256)
+        seg = 256;
+    const uint64_t whole = (total + 31) & ~31ull;
+    return (uint32_t)(seg < whole ? seg : whole);
+}
 // candidates of one k-system check: ng! * 2^ng * rounds
 inline uint64_t ksys_candidates(uint32_t np, uint32_t rounds) {
     uint64_t f = 1;

@@ -38,9 +38,25 @@ __global__ void __launch_bounds__(KTPB) ksys_kernel(const Item *__restrict__ ite
     }
 }
 
+// The size of a segmented launch: the items (from device memory when d_n is given,
+// as a captured enumeration level holds its size there) and the candidates per
+// segment (0 = the automatic choice for that many items).
+struct SegSize {
+    uint32_t n;
+    uint32_t seg;
+};
+__device__ __forceinline__ SegSize seg_size(uint32_t n_items, const uint64_t *d_n, uint32_t seg_cands,
+                                            uint64_t total_max, uint32_t resident_warps) {
+    SegSize z;
+    z.n = d_n ? (uint32_t)*d_n : n_items;
+    z.seg = seg_cands ? seg_cands : ksys_auto_segment(z.n, total_max, resident_warps);
+    return z;
+}
+
 // Every item's state: no rejection yet (key = all ones), no automorphism, well formed.
-__global__ void ksys_seg_init_kernel(KsysSeg *state, uint32_t n_items) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += gridDim.x * blockDim.x)
+__global__ void ksys_seg_init_kernel(KsysSeg *state, uint32_t n_items, const uint64_t *d_n) {
+    const uint32_t n = d_n ? (uint32_t)*d_n : n_items;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         state[i] = KsysSeg{~0ull, 0u, 0u};
 }
 
@@ -57,11 +73,14 @@ __device__ __forceinline__ unsigned long long volatile_key(const unsigned long l
 // candidate before the first rejecting one is still evaluated, so the verdict,
 // m_playerIndex, the relabelings tried and |Aut| are those of the one-warp check.
 __global__ void __launch_bounds__(KTPB) ksys_seg_kernel(const Item *__restrict__ items, uint32_t n_items,
-                                                        const uint8_t *__restrict__ bytes, uint32_t seg_cands,
-                                                        uint64_t n_units, KsysSeg *state,
+                                                        const uint64_t *d_n, const uint8_t *__restrict__ bytes,
+                                                        uint32_t seg_cands, uint64_t total_max,
+                                                        uint32_t resident_warps, KsysSeg *state,
                                                         unsigned long long *ticket) {
     __shared__ uint64_t s_seq[KW][16], s_part[KW][16], s_pair[KW][16];
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const SegSize z = seg_size(n_items, d_n, seg_cands, total_max, resident_warps);
+    const uint64_t n_units = z.n ? ((total_max + z.seg - 1) / z.seg) * z.n : 0;
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0)
@@ -69,12 +88,12 @@ __global__ void __launch_bounds__(KTPB) ksys_seg_kernel(const Item *__restrict__
         t = __shfl_sync(0xFFFFFFFFu, t, 0);
         if (t >= n_units)
             break;
-        const uint32_t it = (uint32_t)(t % n_items);
-        const uint32_t seg = (uint32_t)(t / n_items);
+        const uint32_t it = (uint32_t)(t % z.n);
+        const uint32_t seg = (uint32_t)(t / z.n);
         const Item item = items[it];
         const unsigned np = item.ncols, nr = item.nrows, ng = np >> 1;
         KsysSeg &st = state[it];
-        const uint64_t start = (uint64_t)seg * seg_cands;
+        const uint64_t start = (uint64_t)seg * z.seg;
         // past this item's candidates (a smaller shape than the launch's widest)
         if (seg && np >= 4 && np <= KS_NPMAX && start >= (uint64_t)(c_fact[ng] << ng) * nr)
             continue;
@@ -89,7 +108,7 @@ __global__ void __launch_bounds__(KTPB) ksys_seg_kernel(const Item *__restrict__
             continue;
         }
         const uint64_t total = (uint64_t)(c_fact[ng] << ng) * nr;
-        const uint64_t end = start + seg_cands < total ? start + seg_cands : total;
+        const uint64_t end = start + z.seg < total ? start + z.seg : total;
         const int pidx0 = (int)(nr * np) - 2 - 1;
         unsigned n_aut = 0;
         for (uint64_t base = start; base < end; base += 32u) {
@@ -118,9 +137,10 @@ __global__ void __launch_bounds__(KTPB) ksys_seg_kernel(const Item *__restrict__
 }
 
 // The outputs of the segmented check, one thread per item.
-__global__ void ksys_seg_finish_kernel(const Item *__restrict__ items, uint32_t n_items, const KsysSeg *state,
-                                       Outputs out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += gridDim.x * blockDim.x) {
+__global__ void ksys_seg_finish_kernel(const Item *__restrict__ items, uint32_t n_items, const uint64_t *d_n,
+                                       const KsysSeg *state, Outputs out) {
+    const uint32_t n = d_n ? (uint32_t)*d_n : n_items;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const Item item = items[i];
         const KsysSeg st = state[i];
         const unsigned np = item.ncols, nr = item.nrows, ng = np >> 1;
@@ -277,17 +297,18 @@ cudaError_t launch_ksys_check(const Item *d_items, uint32_t n_items, const uint8
     return cudaGetLastError();
 }
 
-// seg_cands: candidates per segment (a multiple of 32); total_max: the most
-// candidates of any item (ng! * 2^ng * rounds), which sets the segments per item
+// seg_cands: candidates per segment (a multiple of 32, or 0 = chosen on the device
+// from the item count); total_max: the most candidates of any item (ng! * 2^ng *
+// rounds), which sets the segments per item.  d_n (optional): the item count in
+// device memory, at most n_items, which then only sizes the grids; the work counter
+// is d_state[n_items].
 cudaError_t launch_ksys_check_split(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes, Outputs out,
                                    uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
-                                   cudaStream_t s) {
+                                   cudaStream_t s, const uint64_t *d_n) {
     if (!n_items)
         return cudaSuccess;
-    if (seg_cands < 32 || (seg_cands & 31u))
+    if (seg_cands & 31u)
         return cudaErrorInvalidValue;
-    const uint64_t n_seg = (total_max + seg_cands - 1) / seg_cands;
-    // the work counter after the items' states (which the init kernel sets)
     cudaError_t e = cudaMemsetAsync(d_state + n_items, 0, sizeof(KsysSeg), s);
     if (e != cudaSuccess)
         return e;
@@ -297,25 +318,28 @@ cudaError_t launch_ksys_check_split(const Item *d_items, uint32_t n_items, const
         return e;
     if (per_sm < 1)
         per_sm = 1;
-    const uint64_t units = n_seg * n_items;
-    uint64_t grid = (uint64_t)per_sm * (num_sms > 0 ? num_sms : 1);
-    const uint64_t need = (units + ksys::KW - 1) / ksys::KW;
-    if (grid > need)
-        grid = need;
+    const int sms = num_sms > 0 ? num_sms : 1;
+    uint64_t grid = (uint64_t)per_sm * sms;
+    if (!d_n && seg_cands) {
+        const uint64_t units = ((total_max + seg_cands - 1) / seg_cands) * n_items;
+        const uint64_t need = (units + ksys::KW - 1) / ksys::KW;
+        if (grid > need)
+            grid = need;
+    }
     int gi = (int)((n_items + 255) / 256);
-    if (gi > 4 * num_sms)
-        gi = 4 * (num_sms > 0 ? num_sms : 1);
-    ksys_seg_init_kernel<<<gi, 256, 0, s>>>(d_state, n_items);
+    if (gi > 4 * sms)
+        gi = 4 * sms;
+    ksys_seg_init_kernel<<<gi, 256, 0, s>>>(d_state, n_items, d_n);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
     unsigned long long *ticket = reinterpret_cast<unsigned long long *>(d_state + n_items);
-    ksys_seg_kernel<<<(int)grid, ksys::KTPB, 0, s>>>(d_items, n_items, d_bytes, seg_cands, units, d_state, ticket);
+    ksys_seg_kernel<<<(int)grid, ksys::KTPB, 0, s>>>(d_items, n_items, d_n, d_bytes, seg_cands, total_max,
+                                                     (uint32_t)(sms * KSYS_RESIDENT_WARPS_PER_SM), d_state, ticket);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;
-    ksys_seg_finish_kernel<<<gi, 256, 0, s>>>(d_items, n_items, d_state, out);
+    ksys_seg_finish_kernel<<<gi, 256, 0, s>>>(d_items, n_items, d_n, d_state, out);
     return cudaGetLastError();
 }
-
 }  // namespace canon

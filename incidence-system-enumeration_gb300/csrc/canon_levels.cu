@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(SCAN_TPB) tile_sums_kernel(const T *in, uint64
 }
 
 // pass 2 (one block): exclusive scan of the tile sums in place; sums[ntiles] = total
-__global__ void __launch_bounds__(SCAN_TPB) scan_sums_kernel(uint64_t *sums, uint32_t ntiles) {
+__device__ void scan_sums_body(uint64_t *sums, uint32_t ntiles) {
     uint64_t carry = 0;
     for (uint32_t b0 = 0; b0 < ntiles; b0 += SCAN_TPB) {
         const uint32_t i = b0 + threadIdx.x;
@@ -208,6 +208,10 @@ __global__ void __launch_bounds__(SCAN_TPB) scan_sums_kernel(uint64_t *sums, uin
     }
     if (threadIdx.x == 0)
         sums[ntiles] = carry;
+}
+
+__global__ void __launch_bounds__(SCAN_TPB) scan_sums_kernel(uint64_t *sums, uint32_t ntiles) {
+    scan_sums_body(sums, ntiles);
 }
 
 // pass 3: exclusive offsets of every input; out[n] = total
@@ -268,6 +272,65 @@ cudaError_t exclusive_scan(const T *in, uint64_t n, uint64_t *out, DevBuf<uint64
         if (e != cudaSuccess)
             return e;
     }
+    return cudaGetLastError();
+}
+
+// The exclusive scan of `*d_n` inputs (the count in device memory, at most cap):
+// out[i] for i < n and out[n] = the total.  Grids are sized by cap; tiles past the
+// count do nothing.  sums holds cap / SCAN_TILE + 2 words.
+template <typename T>
+__global__ void __launch_bounds__(SCAN_TPB) tile_sums_dev_kernel(const T *in, const uint64_t *d_n, uint64_t *sums) {
+    const uint64_t n = *d_n;
+    if ((uint64_t)blockIdx.x * SCAN_TILE >= n)
+        return;
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_PER_THREAD;
+    uint64_t s = 0;
+    for (int j = 0; j < SCAN_PER_THREAD; ++j)
+        if (base + j < n)
+            s += in[base + j];
+    uint64_t total;
+    block_exclusive_scan(s, &total);
+    if (threadIdx.x == 0)
+        sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_TPB) scan_sums_dev_kernel(uint64_t *sums, const uint64_t *d_n) {
+    scan_sums_body(sums, (uint32_t)((*d_n + SCAN_TILE - 1) / SCAN_TILE));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(SCAN_TPB) tile_scan_dev_kernel(const T *in, const uint64_t *d_n,
+                                                                 const uint64_t *sums, uint64_t *out) {
+    const uint64_t n = *d_n;
+    const uint32_t ntiles = (uint32_t)((n + SCAN_TILE - 1) / SCAN_TILE);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        out[n] = sums[ntiles];
+    if (blockIdx.x >= ntiles)
+        return;
+    const uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_PER_THREAD;
+    uint64_t v[SCAN_PER_THREAD];
+    uint64_t s = 0;
+    for (int j = 0; j < SCAN_PER_THREAD; ++j) {
+        v[j] = (base + j < n) ? (uint64_t)in[base + j] : 0;
+        s += v[j];
+    }
+    uint64_t total;
+    uint64_t run = sums[blockIdx.x] + block_exclusive_scan(s, &total);
+    for (int j = 0; j < SCAN_PER_THREAD; ++j) {
+        if (base + j < n)
+            out[base + j] = run;
+        run += v[j];
+    }
+}
+
+template <typename T>
+cudaError_t exclusive_scan_dev(const T *in, const uint64_t *d_n, uint64_t cap, uint64_t *out, uint64_t *sums,
+                               cudaStream_t s, int *kernels) {
+    const uint32_t tiles = (uint32_t)((cap + SCAN_TILE - 1) / SCAN_TILE);
+    tile_sums_dev_kernel<T><<<tiles ? tiles : 1, SCAN_TPB, 0, s>>>(in, d_n, sums);
+    scan_sums_dev_kernel<<<1, SCAN_TPB, 0, s>>>(sums, d_n);
+    tile_scan_dev_kernel<T><<<tiles ? tiles : 1, SCAN_TPB, 0, s>>>(in, d_n, sums, out);
+    *kernels += 3;
     return cudaGetLastError();
 }
 
@@ -359,7 +422,11 @@ void parallel_ranges(uint64_t n, F fn) {
 }
 
 // ---- k-system rounds on the device ----------------------------------------
-__global__ void ksys_count_kernel(int np, const uint8_t *parents, uint32_t n_par, int d, uint32_t *counts) {
+// d_npar (optional): the parent count in device memory (a captured level)
+__global__ void ksys_count_kernel(int np, const uint8_t *parents, uint32_t n_par, int d, uint32_t *counts,
+                                  const uint64_t *d_npar = nullptr) {
+    if (d_npar)
+        n_par = (uint32_t)*d_npar;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_par; p += stride)
         counts[p] = canon::ksys_children(np, parents + (size_t)p * d * np, d, nullptr);
@@ -367,7 +434,10 @@ __global__ void ksys_count_kernel(int np, const uint8_t *parents, uint32_t n_par
 
 // the children of parents [p0, p1) at offsets[p] - offsets[p0], and one work item each
 __global__ void ksys_emit_kernel(int np, const uint8_t *parents, uint32_t p0, uint32_t p1, int d,
-                                 const uint64_t *offsets, uint8_t *out, canon::Item *items) {
+                                 const uint64_t *offsets, uint8_t *out, canon::Item *items,
+                                 const uint64_t *d_npar = nullptr) {
+    if (d_npar)
+        p1 = (uint32_t)*d_npar;
     const uint64_t base = offsets[p0];
     const uint32_t m = (uint32_t)d + 1;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -392,7 +462,9 @@ __global__ void ksys_emit_kernel(int np, const uint8_t *parents, uint32_t p0, ui
 __global__ void ksys_compact_kernel(uint64_t n_cand, uint32_t bytes, const uint8_t *cand, const uint8_t *canonical,
                                     const uint8_t *status, const uint64_t *aut, const uint64_t *trials,
                                     const uint64_t *offs, uint8_t *dst, uint64_t *aut_dst, unsigned *bad,
-                                    unsigned long long *trials_sum) {
+                                    unsigned long long *trials_sum, const uint64_t *d_ncand = nullptr) {
+    if (d_ncand)
+        n_cand = *d_ncand;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     unsigned long long tsum = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_cand; i += stride) {
@@ -413,6 +485,294 @@ __global__ void ksys_compact_kernel(uint64_t n_cand, uint32_t bytes, const uint8
         tsum += __shfl_down_sync(0xFFFFFFFFu, tsum, off);
     if ((threadIdx.x & 31u) == 0 && tsum)
         atomicAdd(trials_sum, tsum);
+}
+
+// ---- the k-system enumeration as one captured CUDA graph -------------------
+// Every level's size stays in device memory (KsCtl): the kernels of a level read it
+// there, so the whole enumeration -- per level the round generator, the scan, the
+// segmented check and the compaction -- is captured once and replayed with one
+// launch and one wait.  Level buffers are sized for `cap` parents and candidates; a
+// level beyond that raises `overflow`, empties the rest of the run, and the host
+// enumerates again level by level with buffers that grow.
+struct KsCtl {
+    uint64_t n_par;                       // parents of the level in progress
+    uint64_t n_cand;                      // its candidates
+    uint64_t level_checks[16];
+    unsigned long long stamp[16][3];      // globaltimer: level start, candidates written, checked
+    unsigned long long trials;            // relabelings tried by all checks
+    unsigned levels;                      // levels with parents
+    unsigned overflow;
+    unsigned bad;                         // a check reported a bad status
+    unsigned pad;
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// round 0 = (0 1)(2 3)... as the only parent of the first level
+__global__ void ksg_start_kernel(KsCtl *ctl, uint8_t *lev, int np) {
+    if (threadIdx.x < (unsigned)np)
+        lev[threadIdx.x] = (uint8_t)threadIdx.x;
+    if (threadIdx.x == 0)
+        ctl->n_par = 1;
+}
+
+__global__ void ksg_begin_kernel(KsCtl *ctl, int level) {
+    ctl->stamp[level][0] = global_ns();
+    if (ctl->n_par)
+        ++ctl->levels;
+}
+
+// the level's candidates: offs[n_par]; beyond the buffers, the run stops here
+__global__ void ksg_cand_kernel(KsCtl *ctl, const uint64_t *offs, uint64_t cap, int level) {
+    uint64_t n = offs[ctl->n_par];
+    if (n > cap) {
+        ctl->overflow = 1u;
+        n = 0;
+        ctl->n_par = 0;
+    }
+    ctl->n_cand = n;
+    ctl->level_checks[level] = n;
+}
+
+__global__ void ksg_stamp_kernel(KsCtl *ctl, int level, int k) { ctl->stamp[level][k] = global_ns(); }
+
+// the next level's parents: the canonical candidates
+__global__ void ksg_next_kernel(KsCtl *ctl, const uint64_t *coffs, uint64_t cap) {
+    uint64_t n = coffs[ctl->n_cand];
+    if (n > cap) {
+        ctl->overflow = 1u;
+        n = 0;
+    }
+    ctl->n_par = n;
+}
+
+struct KsysGraph {
+    uint32_t np = 0, seg = 0;
+    uint64_t cap = 0;
+    int kernels = 0;
+    cudaGraphExec_t exec = nullptr;
+    DevBuf<uint8_t> lev[2], cand, can, status, rrow, rtc, wit, len_aut;
+    DevBuf<uint64_t> doffs, coffs, sums, aut, aut_out, trials;
+    DevBuf<uint32_t> counts;
+    DevBuf<int32_t> pidx;
+    DevBuf<uint16_t> n_auts;
+    DevBuf<canon::Item> items;
+    DevBuf<canon::KsysSeg> kseg;
+    DevBuf<KsCtl> ctl;
+    ~KsysGraph() {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+    }
+};
+
+// Allocates the buffers and captures the enumeration of K_np with level buffers of
+// `cap` matrices; seg = the segment rule (0 = chosen per level on the device).
+cudaError_t ksys_graph_build(canon_ctx *c, KsysGraph &g, uint32_t np, uint64_t cap, uint32_t seg) {
+    const uint32_t rounds = np - 1;
+    const size_t mbytes = (size_t)rounds * np;     // the largest matrix
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i)
+        e = g.lev[i].ensure(cap * mbytes);
+    if (e == cudaSuccess) e = g.cand.ensure(cap * mbytes);
+    if (e == cudaSuccess) e = g.can.ensure(cap);
+    if (e == cudaSuccess) e = g.status.ensure(cap);
+    if (e == cudaSuccess) e = g.rrow.ensure(cap);
+    if (e == cudaSuccess) e = g.rtc.ensure(cap);
+    if (e == cudaSuccess) e = g.wit.ensure(cap * 16);
+    if (e == cudaSuccess) e = g.len_aut.ensure(cap);
+    if (e == cudaSuccess) e = g.doffs.ensure(cap + 1);
+    if (e == cudaSuccess) e = g.coffs.ensure(cap + 1);
+    if (e == cudaSuccess) e = g.sums.ensure(cap / SCAN_TILE + 2);
+    if (e == cudaSuccess) e = g.aut.ensure(cap * 2);
+    if (e == cudaSuccess) e = g.aut_out.ensure(cap * 2);
+    if (e == cudaSuccess) e = g.trials.ensure(cap);
+    if (e == cudaSuccess) e = g.counts.ensure(cap);
+    if (e == cudaSuccess) e = g.pidx.ensure(cap);
+    if (e == cudaSuccess) e = g.n_auts.ensure(cap);
+    if (e == cudaSuccess) e = g.items.ensure(cap);
+    if (e == cudaSuccess) e = g.kseg.ensure(cap + 1);
+    if (e == cudaSuccess) e = g.ctl.ensure(1);
+    if (e != cudaSuccess)
+        return e;
+    const int sms = c->num_sms > 0 ? c->num_sms : 1;
+    int gg = (int)((cap + 127) / 128);
+    if (gg > 4 * sms)
+        gg = 4 * sms;
+    int gc = (int)((cap + 255) / 256);
+    if (gc > 4 * sms)
+        gc = 4 * sms;
+    cudaStream_t s = c->stream;
+    int kernels = 0;
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess)
+        return e;
+    KsCtl *ctl = g.ctl.p;
+    e = cudaMemsetAsync(ctl, 0, sizeof(KsCtl), s);
+    if (e == cudaSuccess) {
+        ksg_start_kernel<<<1, 32, 0, s>>>(ctl, g.lev[1].p, (int)np);
+        ++kernels;
+        e = cudaGetLastError();
+    }
+    // parents with n rounds live in lev[n & 1]
+    for (uint32_t n = 1; n < rounds && e == cudaSuccess; ++n) {
+        const uint32_t m = n + 1;
+        const bool complete = m == rounds;
+        const uint8_t *par = g.lev[n & 1].p;
+        uint8_t *dst = g.lev[m & 1].p;
+        ksg_begin_kernel<<<1, 1, 0, s>>>(ctl, (int)m - 1);
+        ksys_count_kernel<<<gg, 128, 0, s>>>((int)np, par, 0, (int)n, g.counts.p, &ctl->n_par);
+        kernels += 2;
+        e = exclusive_scan_dev(g.counts.p, &ctl->n_par, cap, g.doffs.p, g.sums.p, s, &kernels);
+        if (e != cudaSuccess)
+            break;
+        ksg_cand_kernel<<<1, 1, 0, s>>>(ctl, g.doffs.p, cap, (int)m - 1);
+        ksys_emit_kernel<<<gg, 128, 0, s>>>((int)np, par, 0, 0, (int)n, g.doffs.p, g.cand.p, g.items.p,
+                                             &ctl->n_par);
+        ksg_stamp_kernel<<<1, 1, 0, s>>>(ctl, (int)m - 1, 1);
+        kernels += 3;
+        canon::Outputs o{};
+        o.canonical = g.can.p;
+        o.status = g.status.p;
+        o.reject_row = g.rrow.p;
+        o.row_to_change = g.rtc.p;
+        o.player_index = g.pidx.p;
+        o.witness = g.wit.p;
+        o.aut = g.aut.p;
+        o.trials = g.trials.p;
+        o.n_auts = g.n_auts.p;
+        o.len_aut = g.len_aut.p;
+        e = canon::launch_ksys_check_split(g.items.p, (uint32_t)cap, g.cand.p, o, seg,
+                                           canon::ksys_candidates(np, m), g.kseg.p, c->num_sms, s, &ctl->n_cand);
+        kernels += 3;
+        if (e != cudaSuccess)
+            break;
+        ksg_stamp_kernel<<<1, 1, 0, s>>>(ctl, (int)m - 1, 2);
+        ++kernels;
+        e = exclusive_scan_dev(g.can.p, &ctl->n_cand, cap, g.coffs.p, g.sums.p, s, &kernels);
+        if (e != cudaSuccess)
+            break;
+        ksys_compact_kernel<<<gc, 256, 0, s>>>(0, (uint32_t)(m * np), g.cand.p, g.can.p, g.status.p, g.aut.p,
+                                               g.trials.p, g.coffs.p, dst, complete ? g.aut_out.p : nullptr,
+                                               &ctl->bad, &ctl->trials, &ctl->n_cand);
+        ksg_next_kernel<<<1, 1, 0, s>>>(ctl, g.coffs.p, cap);
+        kernels += 2;
+        e = cudaGetLastError();
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+    if (e == cudaSuccess)
+        e = e2;
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&g.exec, graph, 0);
+    if (graph)
+        cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        g.exec = nullptr;
+        return e;
+    }
+    g.np = np;
+    g.cap = cap;
+    g.seg = seg;
+    g.kernels = kernels;
+    return cudaSuccess;
+}
+
+}  // namespace
+
+namespace canon {
+void ksys_graph_release(canon_ctx *c) {
+    delete static_cast<KsysGraph *>(c->ksys_graph);
+    c->ksys_graph = nullptr;
+}
+}  // namespace canon
+
+namespace {
+
+// One enumeration of K_np through the captured graph.  Returns CANON_OK with
+// *ran = false when a level outgrew the buffers (the caller enumerates level by
+// level, and the next graph is built 4x larger).
+int ksys_enumerate_graph(canon_ctx *c, uint32_t np, canon_design_cb cb, void *user, canon_enum_stats &st,
+                         bool *ran) {
+    *ran = false;
+    // the segment rule baked into the graph: a fixed size, one segment per matrix, or per level on the device
+    const uint32_t seg = c->ksys_seg == CANON_KSYS_WHOLE ? 0xFFFFFFE0u
+                                                         : (c->ksys_seg ? ((c->ksys_seg + 31u) & ~31u) : 0u);
+    KsysGraph *g = static_cast<KsysGraph *>(c->ksys_graph);
+    if (!g || g->np != np || g->cap != c->ksys_graph_cap || g->seg != seg || !g->exec) {
+        canon::ksys_graph_release(c);
+        g = new KsysGraph();
+        c->ksys_graph = g;
+        const cudaError_t e = ksys_graph_build(c, *g, np, c->ksys_graph_cap, seg);
+        if (e != cudaSuccess) {
+            canon::ksys_graph_release(c);
+            c->err = std::string("enumerate k-systems: graph capture: ") + cudaGetErrorString(e);
+            return e == cudaErrorMemoryAllocation ? CANON_ENOMEM : CANON_ECUDA;
+        }
+    }
+    cudaStream_t s = c->stream;
+    KsCtl h{};
+    cudaError_t e = cudaGraphLaunch(g->exec, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&h, g->ctl.p, sizeof(KsCtl), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        c->err = std::string("enumerate k-systems: graph: ") + cudaGetErrorString(e);
+        return CANON_ECUDA;
+    }
+    c->launches += g->kernels;
+    if (h.overflow) {
+        if (c->ksys_graph_cap < (1ull << 24))
+            c->ksys_graph_cap *= 4;
+        canon::ksys_graph_release(c);
+        return CANON_OK;
+    }
+    *ran = true;
+    const uint32_t rounds = np - 1;
+    for (uint32_t m = 2; m <= rounds; ++m) {
+        const uint64_t nc = h.level_checks[m - 1];
+        if (!nc && !h.stamp[m - 1][2])
+            continue;
+        st.checks += nc;
+        st.level_checks[m - 1] = nc;
+        const double gen = (double)(h.stamp[m - 1][1] - h.stamp[m - 1][0]) * 1e-9;
+        const double chk = (double)(h.stamp[m - 1][2] - h.stamp[m - 1][1]) * 1e-6;
+        st.gen_seconds += gen;
+        st.level_kernel_ms[m - 1] = chk;
+        st.kernel_ms += chk;
+    }
+    st.levels = h.levels;
+    st.batches = h.levels;
+    st.trials = h.trials;
+    if (h.bad) {
+        c->err = "enumerate k-systems: a check reported a bad status";
+        return CANON_ETIMEOUT;
+    }
+    const uint64_t n_final = h.n_par;
+    if (n_final) {
+        const size_t bytes = (size_t)rounds * np;
+        std::vector<uint8_t> mats((size_t)n_final * bytes);
+        std::vector<uint64_t> auts((size_t)n_final * 2);
+        e = cudaMemcpyAsync(mats.data(), g->lev[rounds & 1].p, mats.size(), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(auts.data(), g->aut_out.p, auts.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            c->err = std::string("enumerate k-systems: designs: ") + cudaGetErrorString(e);
+            return CANON_ECUDA;
+        }
+        st.designs = n_final;
+        if (cb)
+            for (uint64_t i = 0; i < n_final; ++i)
+                cb(user, mats.data() + i * bytes, rounds, np, auts[2 * i], auts[2 * i + 1]);
+    }
+    return CANON_OK;
 }
 
 }  // namespace
@@ -744,6 +1104,17 @@ extern "C" int canon_enumerate_ksys(canon_ctx *c, uint32_t np, canon_design_cb c
     cudaSetDevice(c->device);
     cudaStream_t s = c->stream;
     canon_enum_stats st{};
+    if (!(c->cfg.options & CANON_OPT_NO_GRAPH)) {
+        bool ran = false;
+        const int rc = ksys_enumerate_graph(c, np, cb, user, st, &ran);
+        if (rc != CANON_OK || ran) {
+            st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (stats)
+                *stats = st;
+            return rc;
+        }
+        st = canon_enum_stats{};   // a level outgrew the graph's buffers: level by level below
+    }
     DevBuf<uint8_t> lev, next, cand, can, status, rrow, rtc, wit, len_aut;
     DevBuf<uint64_t> doffs, coffs, sums, aut, aut_out, trials;
     DevBuf<uint32_t> dcounts;

@@ -81,6 +81,7 @@ class Cfg(ctypes.Structure):
 OPT_AUT_PRUNE = 0x1
 OPT_VERDICT_SYNC = 0x2    # canon_sync returns only canonical + status
 KSYS_WHOLE = 0xFFFFFFFF   # canon_set_ksys_segment: one warp per matrix
+OPT_NO_GRAPH = 0x4        # canon_enumerate_ksys level by level instead of its captured graph
 
 
 class BibdBatch(ctypes.Structure):

@@ -110,6 +110,9 @@ typedef struct {
  * partial matrix when TestCanonicity() returns true): 2 bytes per item instead of
  * 51.  The other result arrays are not updated and their contents are undefined. */
 #define CANON_OPT_VERDICT_SYNC 0x2u
+/* canon_enumerate_ksys runs level by level with host-sized launches (reading every
+ * level's size back) instead of replaying its captured CUDA graph.  Same output. */
+#define CANON_OPT_NO_GRAPH 0x4u
 
 /* BIBD / incidence-system batch: n matrices of b columns (b <= 63), v rows each
  * (v <= 16), row j of matrix i at rows[i*v + j] with bit c = column c.

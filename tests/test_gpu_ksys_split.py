@@ -79,3 +79,36 @@ def test_k10_enumeration_is_the_same_under_every_split(ctx):
         ctx.set_ksys_segment(0)
     assert len(runs[0][0]) == 396
     assert runs[1] == runs[0] and runs[2] == runs[0]
+
+
+def _enum(ctx, np_):
+    found, st = ctx.enumerate_ksys(np_)
+    return [(R.tobytes(), a) for R, a in found], int(st.trials), int(st.checks), list(st.level_checks)
+
+
+def test_captured_graph_enumeration_equals_level_by_level():
+    """canon_enumerate_ksys replays one captured CUDA graph (level sizes in device
+    memory); CANON_OPT_NO_GRAPH runs level by level.  Same designs in the same order,
+    same relabelings tried and per-level checks, for K6, K8 and K10; a context whose
+    item capacity is below K10's largest level (4,092) overflows the graph's buffers,
+    falls back to the level-by-level run, and replays a 4x larger graph next time."""
+    plain = G.Context(max_items=1 << 16, aut_cap=4, options=G.OPT_NO_GRAPH)
+    graph = G.Context(max_items=1 << 16, aut_cap=4)
+    small = G.Context(max_items=1024, aut_cap=4)
+    try:
+        for np_ in (6, 8, 10):
+            ref = _enum(plain, np_)
+            assert _enum(graph, np_) == ref, np_
+            assert _enum(graph, np_) == ref, np_          # the cached graph, replayed
+        ref10 = _enum(plain, 10)
+        assert len(ref10[0]) == 396
+        l0 = small.kernel_launches()
+        assert _enum(small, 10) == ref10                  # overflow: level by level
+        l1 = small.kernel_launches()
+        assert _enum(small, 10) == ref10                  # 4,096 fits: the graph
+        l2 = small.kernel_launches()
+        assert l1 - l0 != l2 - l1
+    finally:
+        plain.close()
+        graph.close()
+        small.close()
