@@ -242,6 +242,7 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
                     finish(ST_BADINPUT);
                     continue;
                 }
+                st.w = conv_row_weight(sm, v);
                 eval = true;        // the root: no arrangement step
                 break;
             }
@@ -273,8 +274,10 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
         const uint64_t bnd = hb ? R_(st.i) : 0ull;
-        const int state = full ? eval_node_uniform<BCAP>(sm, st.i, b, b, tied, arr, hb, bnd)
-                               : eval_node_uniform(sm, st.i, b, b, tied, arr, hb, bnd);
+        // count planes for the heaviest row among the lanes stepping together
+        const unsigned w = __reduce_max_sync(__activemask(), st.w);
+        const int state = full ? eval_node_planes<BCAP>(sm, w, st.i, b, b, tied, arr, hb, bnd)
+                               : eval_node_planes(sm, w, st.i, b, b, tied, arr, hb, bnd);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }
@@ -337,6 +340,7 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
                 }
                 for (unsigned c = b; c < bt; ++c)
                     CM_(c) = 0;
+                st.w = conv_row_weight(sm, n);
                 eval = true;
                 break;
             }
@@ -368,8 +372,9 @@ __global__ void __launch_bounds__(TPB) bibd_items_conv_kernel(const Item *__rest
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
         const uint64_t bnd = hb ? R_(st.i) : 0ull;
-        const int state = full ? eval_node_uniform<BCAP>(sm, st.i, b, bt, tied, arr, hb, bnd)
-                               : eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, bnd);
+        const unsigned w = __reduce_max_sync(__activemask(), st.w);
+        const int state = full ? eval_node_planes<BCAP>(sm, w, st.i, b, bt, tied, arr, hb, bnd)
+                               : eval_node_planes(sm, w, st.i, b, bt, tied, arr, hb, bnd);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             finish(0);
     }

@@ -45,9 +45,14 @@ namespace {
 // every orbit, the first orbit whose counts differ decides, which is the first
 // position where the two rows differ (a per-orbit comparison inside the loop
 // measured 1.13x slower).
-template <unsigned FB = 0, typename S>
+// NP: bit planes of the count (3, 4 or 6).  A row's count inside one orbit is at most
+// its weight, so NP = 3 is exact when no row of the matrix has more than 7 ones (STS(15):
+// 7) and NP = 4 up to 15 (BIBD(16,24,9,6,3): 9); fewer planes shorten the carry chain
+// of every column and the plane tests of every orbit end.
+template <unsigned FB = 0, unsigned NP = 6, typename S>
 __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, unsigned bt, unsigned &tied,
                                                  uint64_t &arr, bool have_bound, uint64_t bound) {
+    static_assert(NP == 3 || NP == 4 || NP == 6, "3, 4 or 6 count planes");
     if (FB) {
         b = FB;
         bt = FB;
@@ -57,27 +62,35 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
     const uint64_t ends = (lvl >> 1) | (~0ull << (b - 1));
     unsigned t0 = tied;
     uint64_t a = 0;
-    unsigned p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, p5 = 0;
+    unsigned pl[NP];
+#pragma unroll
+    for (unsigned k = 0; k < NP; ++k)
+        pl[k] = 0;
     unsigned s = 0;
 #pragma unroll(FB ? FB : 1)
     for (unsigned p = 0; p < bt; ++p) {
         unsigned carry = (unsigned)CM_(p) & t0, t;
-        t = p0 & carry; p0 ^= carry; carry = t;
-        t = p1 & carry; p1 ^= carry; carry = t;
-        t = p2 & carry; p2 ^= carry; carry = t;
-        t = p3 & carry; p3 ^= carry; carry = t;
-        t = p4 & carry; p4 ^= carry; carry = t;
-        p5 ^= carry;
+#pragma unroll
+        for (unsigned k = 0; k + 1 < NP; ++k) {
+            t = pl[k] & carry;
+            pl[k] ^= carry;
+            carry = t;
+        }
+        pl[NP - 1] ^= carry;
         if ((ends >> p) & 1u) {
             unsigned cstar = 0;
-            t = t0 & p5; if (t) { t0 = t; cstar |= 32u; }
-            t = t0 & p4; if (t) { t0 = t; cstar |= 16u; }
-            t = t0 & p3; if (t) { t0 = t; cstar |= 8u; }
-            t = t0 & p2; if (t) { t0 = t; cstar |= 4u; }
-            t = t0 & p1; if (t) { t0 = t; cstar |= 2u; }
-            t = t0 & p0; if (t) { t0 = t; cstar |= 1u; }
+#pragma unroll
+            for (int k = (int)NP - 1; k >= 0; --k) {
+                t = t0 & pl[k];
+                if (t) {
+                    t0 = t;
+                    cstar |= 1u << k;
+                }
+            }
             a |= ((1ull << cstar) - 1ull) << s;
-            p0 = p1 = p2 = p3 = p4 = p5 = 0;
+#pragma unroll
+            for (unsigned k = 0; k < NP; ++k)
+                pl[k] = 0;
             s = p + 1;
         }
     }
@@ -89,6 +102,28 @@ __device__ __forceinline__ int eval_node_uniform(S sm, unsigned lv, unsigned b, 
     tied = t0;
     arr = a;
     return state;
+}
+
+// the greatest row weight of the n rows in R_() (sets the count planes of a node step)
+template <typename S>
+__device__ __forceinline__ unsigned conv_row_weight(S sm, unsigned n) {
+    unsigned w = 0;
+    for (unsigned r = 0; r < n; ++r) {
+        const unsigned c = (unsigned)__popcll(R_(r));
+        w = c > w ? c : w;
+    }
+    return w;
+}
+
+// the node evaluation with the fewest count planes that hold weight w
+template <unsigned FB = 0, typename S>
+__device__ __forceinline__ int eval_node_planes(S sm, unsigned w, unsigned lv, unsigned b, unsigned bt,
+                                                unsigned &tied, uint64_t &arr, bool have_bound, uint64_t bound) {
+    if (w <= 7)
+        return eval_node_uniform<FB, 3>(sm, lv, b, bt, tied, arr, have_bound, bound);
+    if (w <= 15)
+        return eval_node_uniform<FB, 4>(sm, lv, b, bt, tied, arr, have_bound, bound);
+    return eval_node_uniform<FB, 6>(sm, lv, b, bt, tied, arr, have_bound, bound);
 }
 
 // the columns of level lv+1 after row x was taken at level lv: inside every orbit of
@@ -131,6 +166,7 @@ struct ConvState {
     uint64_t nmask1;
     bool improved, timeout, rejected;
     bool verdict_only;      // stop at the first greater node (M rejected; no |Aut|)
+    unsigned w;             // the greatest row weight (conv_row_weight): the count planes
 };
 
 // a fresh search of the n rows in R_(); restart_after, b and verdict_only are the caller's

@@ -109,6 +109,7 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
     ConvState st;
     conv_start(st, n, order0);
     st.b = b;
+    st.w = conv_row_weight(sm, n);     // the count planes, as the kernels choose them
     st.restart_after = mode == 0 ? ~0ull : (mode == 1 ? RESTART_AFTER : 0);
     st.verdict_only = mode == 3;
     int ref_lv = -1;
@@ -132,10 +133,10 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
         const uint64_t bnd = hb ? R_(st.i) : 0ull;
-        const int state = fb == 35   ? eval_node_uniform<35>(sm, st.i, b, bt, tied, arr, hb, bnd)
-                          : fb == 40 ? eval_node_uniform<40>(sm, st.i, b, bt, tied, arr, hb, bnd)
-                          : fb == 64 ? eval_node_uniform<64>(sm, st.i, b, bt, tied, arr, hb, bnd)
-                                     : eval_node_uniform(sm, st.i, b, bt, tied, arr, hb, bnd);
+        const int state = fb == 35   ? eval_node_planes<35>(sm, st.w, st.i, b, bt, tied, arr, hb, bnd)
+                          : fb == 40 ? eval_node_planes<40>(sm, st.w, st.i, b, bt, tied, arr, hb, bnd)
+                          : fb == 64 ? eval_node_planes<64>(sm, st.w, st.i, b, bt, tied, arr, hb, bnd)
+                                     : eval_node_planes(sm, st.w, st.i, b, bt, tied, arr, hb, bnd);
         if (!conv_after_eval(sm, st, state, tied, arr, b))
             break;
         if (!conv_next(sm, st, ref_lv, ref_x))

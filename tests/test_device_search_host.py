@@ -359,3 +359,26 @@ def test_converged_layout_walks_the_same_tree(host):
                                                ctypes.c_uint64(0xFEDCBA9876543210), ctypes.byref(leaves),
                                                ctypes.byref(nodes), ctypes.byref(imp), 0) == 0
                 assert (leaves.value, nodes.value, imp.value) == a, (params, k)
+
+
+def test_converged_layout_with_four_and_six_count_planes(host):
+    """The node step counts with 3, 4 or 6 bit planes by the matrix's greatest row
+    weight (<= 7, <= 15, more).  Heavier rows take the 4- and 6-plane paths: the
+    BIBD(9,18,8,4,3) designs (weight 8) and their prefixes, and random 0/1 matrices of
+    weights around 12 and 20, must walk the same tree as max_search()."""
+    rng = np.random.default_rng(78)
+    for M, _ in cases.bibd_designs(9, 18, 8, 4, 3):
+        X = cases.permute_normalize(M, rng)
+        r = np.ascontiguousarray(G.pack_rows(X), np.uint64)
+        for k in (3, 6, 9):
+            a, m = _conv_vs_max(host, np.ascontiguousarray(r[:k]), k, 18)
+            assert a == m, k
+    for v, b, dens in ((10, 24, 0.5), (8, 40, 0.5), (6, 63, 0.45)):
+        for _ in range(6):
+            X = (rng.random((v, b)) < dens).astype(np.uint8)
+            X[:, 0] = 1                      # no empty matrix
+            r = np.ascontiguousarray(G.pack_rows(X), np.uint64)
+            w = int(X.sum(axis=1).max())
+            assert w > 7
+            a, m = _conv_vs_max(host, r, v, b)
+            assert a == m, (v, b, w)
