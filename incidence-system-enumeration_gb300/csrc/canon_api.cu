@@ -149,9 +149,28 @@ cudaError_t ensure_scratch(canon_ctx *c, size_t bytes) {
     return e;
 }
 
+// the forward pass of the installed weights: on tcgen05 (16-byte aligned rows), or the
+// warp-level mma.sync path (CANON_OPT_MLP_WARP_MMA, or unaligned buffers)
 cudaError_t mlp_forward_installed(canon_ctx *c, long n, const void *x, float *y, void *h1, void *h2, cudaStream_t s) {
+    const auto a16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+    if (!(c->cfg.options & CANON_OPT_MLP_WARP_MMA) && c->d_tc_err && a16(x) && a16(h1) && a16(h2))
+        return canon::mlp::forward_tc(n, x, c->d_w1, c->d_mlp + P_B1, c->d_w2, c->d_mlp + P_B2, c->d_w3,
+                                      c->d_mlp + P_B3, y, h1, h2, c->d_tc_err, c->num_sms, s);
     return canon::mlp::forward(n, x, c->d_w1, c->d_mlp + P_B1, c->d_w2, c->d_mlp + P_B2, c->d_w3, c->d_mlp + P_B3, y,
                                h1, h2, c->num_sms, s);
+}
+
+// after the stream is synchronised: did a tensor-core forward pass give up waiting?
+// (the flag is cleared)
+bool tc_timed_out(canon_ctx *c) {
+    if (!c->d_tc_err)
+        return false;
+    unsigned f = 0;
+    if (cudaMemcpy(&f, c->d_tc_err, sizeof(f), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return true;
+    if (f)
+        cudaMemset(c->d_tc_err, 0, sizeof(f));
+    return f != 0;
 }
 
 // orders of the first-row candidates for n matrices (chunked: features, scores, sort)
@@ -256,6 +275,10 @@ canon_ctx *canon_create(const canon_cfg *cfg) {
     if (e == cudaSuccess)
         e = dev_alloc(&c->d_ticket, 2);
     if (e == cudaSuccess)
+        e = dev_alloc(&c->d_tc_err, 1);
+    if (e == cudaSuccess)
+        e = cudaMemset(c->d_tc_err, 0, sizeof(unsigned));
+    if (e == cudaSuccess)
         e = alloc_outputs(c->d_out, n, c->cfg.aut_cap, true);
     if (e == cudaSuccess)
         e = alloc_outputs(c->h_out, n, c->cfg.aut_cap, false);
@@ -287,7 +310,7 @@ void canon_destroy(canon_ctx *c) {
         cudaStreamSynchronize(c->stream);
     free_outputs(c->d_out, true);
     free_outputs(c->h_out, false);
-    void *dptrs[] = {c->d_bitems, c->d_kitems, c->d_words, c->d_bytes, c->d_ticket, c->d_mlp, c->d_w1, c->d_w2,
+    void *dptrs[] = {c->d_bitems, c->d_kitems, c->d_words, c->d_bytes, c->d_ticket, c->d_tc_err, c->d_mlp, c->d_w1, c->d_w2,
                      c->d_w2t, c->d_w3, c->d_adam_m, c->d_adam_v, c->d_grad, c->d_loss, c->d_scratch,
                      c->d_orders};
     for (void *p : dptrs)
@@ -1081,6 +1104,8 @@ int canon_mlp_forward(canon_ctx *c, uint64_t n, const void *d_x, const float *pa
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
     ++c->launches;
+    if (e == cudaSuccess && tc_timed_out(c))
+        return fail(c, CANON_ETIMEOUT, "forward: a wait for the tensor cores timed out");
     return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "forward");
 }
 
@@ -1090,12 +1115,14 @@ static cudaError_t mlp_grad_pass(canon_ctx *c, long n, const void *d_x, const fl
     cudaError_t e = ensure_scratch(c, (size_t)n * 4 + act * 2 * 2 + (size_t)n * 4 + act * 4 * 2 + 1024);
     if (e != cudaSuccess)
         return e;
+    // the BF16 activations first: 256-byte rows, so both start 16-byte aligned (the
+    // tensor-core forward stores them 16 bytes at a time)
     char *base = static_cast<char *>(c->d_scratch);
-    float *logit = reinterpret_cast<float *>(base);
-    void *h1 = base + (size_t)n * 4;
-    void *h2 = base + (size_t)n * 4 + act * 2;
-    float *dy = reinterpret_cast<float *>(base + (size_t)n * 4 + act * 4);
-    float *dh2 = reinterpret_cast<float *>(base + (size_t)n * 8 + act * 4);
+    void *h1 = base;
+    void *h2 = base + act * 2;
+    float *logit = reinterpret_cast<float *>(base + act * 4);
+    float *dy = logit + n;
+    float *dh2 = reinterpret_cast<float *>(base + act * 4 + (size_t)n * 8);
     float *dh1 = dh2 + act;
     cudaStream_t s = c->stream;
     e = cudaMemsetAsync(c->d_grad, 0, canon::mlp::N_PARAMS * 4, s);
@@ -1128,6 +1155,8 @@ int canon_mlp_grad(canon_ctx *c, uint64_t n, const void *d_x, const float *d_lab
         e = cudaStreamSynchronize(c->stream);
     if (loss)
         *loss = l / (float)n;
+    if (e == cudaSuccess && tc_timed_out(c))
+        return fail(c, CANON_ETIMEOUT, "grad: a wait for the tensor cores timed out");
     return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "grad");
 }
 
@@ -1169,6 +1198,8 @@ int canon_mlp_train(canon_ctx *c, uint64_t n, const void *d_x, const float *d_la
     e = cudaMemcpyAsync(params, c->d_mlp, canon::mlp::N_PARAMS * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess && tc_timed_out(c))
+        return fail(c, CANON_ETIMEOUT, "train: a wait for the tensor cores timed out");
     return e == cudaSuccess ? CANON_OK : cuda_fail(c, e, "train");
 }
 

@@ -42,6 +42,7 @@ struct canon_ctx {
     uint64_t *d_words = nullptr;
     uint8_t *d_bytes = nullptr;
     unsigned *d_ticket = nullptr;      // work-stealing counters (2 words)
+    unsigned *d_tc_err = nullptr;      // raised when a tensor-core forward pass gave up waiting
     canon::Outputs d_out{}, h_out{};
     std::vector<uint8_t> item_kind;   // per out_idx
     // learned order: installed weights (device) and lazily grown scratch

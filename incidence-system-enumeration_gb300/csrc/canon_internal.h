@@ -105,6 +105,11 @@ namespace mlp {
 constexpr int N_PARAMS = 128 * 64 + 128 + 128 * 128 + 128 + 128 + 1;
 cudaError_t forward(long n, const void *x, const void *w1, const float *b1, const void *w2, const float *b2,
                     const void *w3, const float *b3, float *y, void *h1, void *h2, int num_sms, cudaStream_t s);
+// the same forward pass on tcgen05 (x 16-byte aligned); *err is raised if a wait for
+// the tensor cores timed out
+cudaError_t forward_tc(long n, const void *x, const void *w1, const float *b1, const void *w2, const float *b2,
+                       const void *w3, const float *b3, float *y, void *h1, void *h2, unsigned *err, int num_sms,
+                       cudaStream_t s);
 cudaError_t backward(long n, const float *logit, const float *label, const void *h1, const void *h2,
                      const void *w3, const void *w2t, float *dy, float *dh2, float *dh1, float *loss,
                      int num_sms, cudaStream_t s);

@@ -1,10 +1,11 @@
 // canon_mlp.cu -- the learned search order: a BF16 MLP 64 -> 128 -> 128 -> 1 that
 // scores every row of a matrix as the first row of the canonical labeling.
 //
-// Inference and the forward pass of training run on the tensor cores
-// (mma.sync m16n8k16, BF16 operands, FP32 accumulation), one warp per 16 rows, the
-// weights staged once per block in shared memory; the hidden activations stay in
-// registers and feed the next layer as A fragments.  The backward pass propagates through the same layers (the hidden
+// Inference and the forward pass of training run on the 5th-generation tensor cores
+// (tcgen05.mma, BF16 operands, FP32 accumulators in tensor memory, 128 rows per CTA:
+// mlp_forward_tc_kernel).  The earlier warp-level path (mma.sync m16n8k16, one warp per
+// 16 rows, the hidden activations kept in registers as A fragments) stays as the
+// context option CANON_OPT_MLP_WARP_MMA.  The backward pass propagates through the same layers (the hidden
 // gradient dH1 = dH2 * W2 also on the tensor cores), the weight gradients are
 // tiled FP32 reductions over the batch, and Adam keeps FP32 master weights from
 // which the BF16 copies are refreshed after every step.  No counterpart in the
@@ -157,6 +158,260 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(long n, const __nv_bfl
             if (r0 + g + 8 < n)
                 y[r0 + g + 8] = part1 + wg.b3[0];
         }
+    }
+}
+
+// ---- the forward pass on the 5th-generation tensor cores -------------------
+// One CTA (4 warps) takes 128 rows at a time.  Both layers are tcgen05.mma
+// (kind::f16: BF16 operands, FP32 accumulators in tensor memory) issued by one
+// thread: D1[128 x 128] = X[128 x 64] W1^T, then D2[128 x 128] = H1[128 x 128] W2^T.
+// The operands sit in shared memory in the K-major layout without swizzle: 8-row x
+// 16-byte core matrices, the core matrices along K 128 bytes apart (leading byte
+// offset) and the 8-row groups (K/8) x 128 bytes apart (stride byte offset).  Each
+// thread owns one row of the accumulators (tensor-memory lane = row): it reads its
+// row with tcgen05.ld, adds the bias, applies the ReLU and rounds to BF16 -- H1 goes
+// back to shared memory as layer 2's A operand, H2 meets w3 in a per-thread dot
+// product.  W1 and W2 are staged once per CTA.  Every wait for the tensor cores is
+// bounded by time: past it the kernel raises *err, stops, frees its tensor memory
+// and returns.
+constexpr int TC_ROWS = 128;
+constexpr uint32_t TC_TMEM_COLS = 256;                  // D1 in columns 0-127, D2 in 128-255
+constexpr uint32_t TC_W1 = 0, TC_W2 = TC_W1 + HID * IN * 2, TC_X = TC_W2 + HID * HID * 2,
+                   TC_H1 = TC_X + TC_ROWS * IN * 2, TC_PAR = TC_H1 + TC_ROWS * HID * 2,
+                   TC_BAR = TC_PAR + 3 * HID * 4, TC_END = TC_BAR + 16;
+constexpr size_t TC_SMEM = TC_END + 1024;               // + the alignment of the base to 1 KB
+// instruction descriptor, kind::f16: FP32 accumulator (bit 4), BF16 A (bits 7-9 = 1) and
+// B (bits 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit 17, M >> 4 at bit 24
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(HID >> 3) << 17) |
+                              ((uint32_t)(TC_ROWS >> 4) << 24);
+constexpr unsigned long long TC_WAIT_NS = 1000000000ull;   // 1 s: far beyond any tile's MMAs
+
+// byte offset of the 16-byte chunk (row r, K elements 8*k8 .. 8*k8+7) of a K-major tile
+// whose rows hold kdim elements
+__device__ __forceinline__ uint32_t core_off(int r, int k8, int kdim) {
+    return (uint32_t)((r >> 3) * (kdim / 8) * 128 + k8 * 128 + (r & 7) * 16);
+}
+
+// shared-memory matrix descriptor: start, leading and stride byte offsets (>> 4), the
+// descriptor version (1 at bit 46), no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ unsigned long long tc_now() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// waits for the phase of the given parity of the barrier; false after TC_WAIT_NS
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity) {
+    const unsigned long long t0 = tc_now();
+    for (;;) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok)
+            return true;
+        if (tc_now() - t0 > TC_WAIT_NS)
+            return false;
+    }
+}
+
+// 32 consecutive FP32 accumulator columns of this thread's row (the warp's 32 lanes)
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&f)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i)
+        f[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void async_proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __nv_bfloat16 *__restrict__ x,
+                                                                MlpDev wg, float *__restrict__ y,
+                                                                __nv_bfloat16 *__restrict__ h1out,
+                                                                __nv_bfloat16 *__restrict__ h2out, unsigned *err) {
+    extern __shared__ __align__(16) unsigned char tc_smem_raw[];
+    const uint32_t raw = (uint32_t)__cvta_generic_to_shared(tc_smem_raw);
+    const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
+    unsigned char *sm = tc_smem_raw + pad;
+    const uint32_t sbase = raw + pad;
+    float *sb1 = reinterpret_cast<float *>(sm + TC_PAR), *sb2 = sb1 + HID, *sw3 = sb2 + HID;
+    const uint32_t bar = sbase + TC_BAR;
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(sm + TC_BAR + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // tensor memory: one warp allocates (and at the end frees) the accumulator columns
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + TC_BAR + 8),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // the weights (K-major core-matrix layout) and the biases, once
+    for (int i = tid; i < HID * (IN / 8); i += blockDim.x) {
+        const int r = i / (IN / 8), k8 = i % (IN / 8);
+        *reinterpret_cast<uint4 *>(sm + TC_W1 + core_off(r, k8, IN)) =
+            *reinterpret_cast<const uint4 *>(wg.w1 + r * IN + k8 * 8);
+    }
+    for (int i = tid; i < HID * (HID / 8); i += blockDim.x) {
+        const int r = i / (HID / 8), k8 = i % (HID / 8);
+        *reinterpret_cast<uint4 *>(sm + TC_W2 + core_off(r, k8, HID)) =
+            *reinterpret_cast<const uint4 *>(wg.w2 + r * HID + k8 * 8);
+    }
+    for (int i = tid; i < HID; i += blockDim.x) {
+        sb1[i] = wg.b1[i];
+        sb2[i] = wg.b2[i];
+        sw3[i] = __bfloat162float(wg.w3[i]);
+    }
+    async_proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t d1 = tmem, d2 = tmem + HID;
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;    // this warp's 32 tensor-memory lanes
+    const float b3 = wg.b3[0];
+    uint32_t phase = 0;
+    bool failed = false;
+    const long tiles = (n + TC_ROWS - 1) / TC_ROWS;
+    for (long tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const long r0 = tile * TC_ROWS;
+        // X tile: 128 rows x 8 chunks of 16 bytes (rows past n are zero)
+        for (int i = tid; i < TC_ROWS * (IN / 8); i += blockDim.x) {
+            const int r = i / (IN / 8), k8 = i % (IN / 8);
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (r0 + r < n)
+                v = *reinterpret_cast<const uint4 *>(x + (r0 + r) * IN + k8 * 8);
+            *reinterpret_cast<uint4 *>(sm + TC_X + core_off(r, k8, IN)) = v;
+        }
+        async_proxy_fence();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < IN / 16; ++ks)
+                tc_mma(d1, tc_desc(sbase + TC_X + ks * 256, 128, (IN / 8) * 128),
+                       tc_desc(sbase + TC_W1 + ks * 256, 128, (IN / 8) * 128), ks > 0);
+            tc_commit(bar);
+        }
+        bool ok = tc_wait(bar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        tc_fence_after();
+        // layer-1 epilogue: H1 = relu(D1 + b1) in BF16, this thread's row
+        const int row = 32 * warp + lane;
+        const long grow = r0 + row;
+#pragma unroll 1
+        for (int c = 0; c < HID / 32; ++c) {
+            float f[32];
+            tc_ld32(d1 + lane_base + 32 * c, f);
+            uint32_t pk[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int col = 32 * c + 2 * j;
+                pk[j] = pack_bf16(fmaxf(f[2 * j] + sb1[col], 0.f), fmaxf(f[2 * j + 1] + sb1[col + 1], 0.f));
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint4 v = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+                *reinterpret_cast<uint4 *>(sm + TC_H1 + core_off(row, 4 * c + q, HID)) = v;
+                if (h1out && grow < n)
+                    *reinterpret_cast<uint4 *>(h1out + grow * HID + (4 * c + q) * 8) = v;
+            }
+        }
+        tc_fence_before();
+        async_proxy_fence();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < HID / 16; ++ks)
+                tc_mma(d2, tc_desc(sbase + TC_H1 + ks * 256, 128, (HID / 8) * 128),
+                       tc_desc(sbase + TC_W2 + ks * 256, 128, (HID / 8) * 128), ks > 0);
+            tc_commit(bar);
+        }
+        ok = tc_wait(bar, phase);
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        tc_fence_after();
+        // layer-2 epilogue: H2 = relu(D2 + b2) in BF16, and the logit H2 . w3 + b3
+        float acc = 0.f;
+#pragma unroll 1
+        for (int c = 0; c < HID / 32; ++c) {
+            float f[32];
+            tc_ld32(d2 + lane_base + 32 * c, f);
+            uint32_t pk[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int col = 32 * c + 2 * j;
+                pk[j] = pack_bf16(fmaxf(f[2 * j] + sb2[col], 0.f), fmaxf(f[2 * j + 1] + sb2[col + 1], 0.f));
+                acc += bf_lo(pk[j]) * sw3[col] + bf_hi(pk[j]) * sw3[col + 1];
+            }
+            if (h2out && grow < n) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    *reinterpret_cast<uint4 *>(h2out + grow * HID + (4 * c + q) * 8) =
+                        make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+            }
+        }
+        if (grow < n)
+            y[grow] = acc + b3;
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (failed) {
+        if (tid == 0)
+            atomicExch(err, 1u);
+        // the MMAs the barrier waited for: once more, bounded, before their columns are freed
+        (void)tc_wait(bar, phase ^ 1u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS)
+                     : "memory");
     }
 }
 
@@ -435,6 +690,27 @@ cudaError_t forward(long n, const void *x, const void *w1, const float *b1, cons
         return e;
     mlp_forward_kernel<<<(int)grid, 128, FWD_SMEM, s>>>(n, (const __nv_bfloat16 *)x, w, y, (__nv_bfloat16 *)h1,
                                                          (__nv_bfloat16 *)h2);
+    return cudaGetLastError();
+}
+
+cudaError_t forward_tc(long n, const void *x, const void *w1, const float *b1, const void *w2, const float *b2,
+                       const void *w3, const float *b3, float *y, void *h1, void *h2, unsigned *err, int num_sms,
+                       cudaStream_t s) {
+    if (n <= 0)
+        return cudaSuccess;
+    MlpDev w{(const __nv_bfloat16 *)w1, b1, (const __nv_bfloat16 *)w2, b2, (const __nv_bfloat16 *)w3, b3};
+    const long tiles = (n + TC_ROWS - 1) / TC_ROWS;
+    // a persistent grid, two CTAs per SM (shared memory allows two; their 2 x 256 tensor-memory
+    // columns are the SM's 512, so an allocation never waits)
+    long grid = 2L * (num_sms > 0 ? num_sms : 1);
+    if (grid > tiles)
+        grid = tiles;
+    const cudaError_t e =
+        cudaFuncSetAttribute(mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
+    if (e != cudaSuccess)
+        return e;
+    mlp_forward_tc_kernel<<<(int)grid, 128, TC_SMEM, s>>>(n, (const __nv_bfloat16 *)x, w, y, (__nv_bfloat16 *)h1,
+                                                          (__nv_bfloat16 *)h2, err);
     return cudaGetLastError();
 }
 

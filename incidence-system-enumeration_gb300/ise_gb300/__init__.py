@@ -82,6 +82,7 @@ OPT_AUT_PRUNE = 0x1
 OPT_VERDICT_SYNC = 0x2    # canon_sync returns only canonical + status
 KSYS_WHOLE = 0xFFFFFFFF   # canon_set_ksys_segment: one warp per matrix
 OPT_NO_GRAPH = 0x4        # canon_enumerate_ksys level by level instead of its captured graph
+OPT_MLP_WARP_MMA = 0x8    # the MLP forward on mma.sync instead of tcgen05
 
 
 class BibdBatch(ctypes.Structure):

@@ -200,3 +200,46 @@ def test_config4_eval_batch_learned_order_matches_oracle():
     assert not st.any()
     import cases
     cases.compare_sts_sample(rows, can, wit.reshape(n, 16), aut.view(np.uint64).reshape(n, 2), range(0, n, 512))
+
+
+def test_tensor_core_forward_matches_the_warp_mma_path(data):
+    """The forward pass on tcgen05 (FP32 accumulators in tensor memory, 128 rows per
+    CTA) against the warp-level mma.sync path on the same BF16 inputs: logits within
+    BF16 rounding of the hidden layers, on sizes that end inside a 128-row tile; and
+    the training gradients of both paths agree."""
+    X, t = data
+    p = G.init_mlp_params(21)
+    p[8192:8320] = 0.05
+    tc = G.Context(max_items=1 << 12, aut_cap=4)
+    mm = G.Context(max_items=1 << 12, aut_cap=4, options=G.OPT_MLP_WARP_MMA)
+    try:
+        for n in (1, 127, 128, 129, 1000):
+            ys = []
+            for c in (tc, mm):
+                dx = to_device(c, G.to_bf16_bits(X[:n]))
+                dy = c.alloc(4 * n)
+                try:
+                    c.mlp_forward(n, dx, p, dy)
+                    ys.append(c.d2h(np.zeros(n, np.float32), dy))
+                finally:
+                    c.free(dx)
+                    c.free(dy)
+            d = np.abs(ys[0] - ys[1])
+            assert d.max() < 2e-2 and np.median(d) < 1e-3, (n, d.max(), np.median(d))
+            _, _, _, _, _, yr = ref_forward(p, X[:n])
+            assert np.allclose(ys[0], yr, rtol=2e-2, atol=2e-2), n
+        gs = []
+        for c in (tc, mm):
+            dx = to_device(c, G.to_bf16_bits(X))
+            dt = to_device(c, t)
+            try:
+                gs.append(c.mlp_grad(len(X), dx, dt, p))
+            finally:
+                c.free(dx)
+                c.free(dt)
+        (g0, l0), (g1, l1) = gs
+        assert abs(l0 - l1) < 1e-3
+        assert np.abs(g0 - g1).max() < 5e-3 * max(1.0, np.abs(g1).max())
+    finally:
+        tc.close()
+        mm.close()
