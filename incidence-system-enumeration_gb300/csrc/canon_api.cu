@@ -149,11 +149,12 @@ cudaError_t ensure_scratch(canon_ctx *c, size_t bytes) {
     return e;
 }
 
-// the forward pass of the installed weights: on tcgen05 (16-byte aligned rows), or the
-// warp-level mma.sync path (CANON_OPT_MLP_WARP_MMA, or unaligned buffers)
+// the forward pass of the installed weights: on tcgen05 (at least one 128-row tile,
+// 16-byte aligned rows), or the warp-level mma.sync path (CANON_OPT_MLP_WARP_MMA,
+// fewer rows, or unaligned buffers)
 cudaError_t mlp_forward_installed(canon_ctx *c, long n, const void *x, float *y, void *h1, void *h2, cudaStream_t s) {
     const auto a16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
-    if (!(c->cfg.options & CANON_OPT_MLP_WARP_MMA) && c->d_tc_err && a16(x) && a16(h1) && a16(h2))
+    if (!(c->cfg.options & CANON_OPT_MLP_WARP_MMA) && c->d_tc_err && n >= 128 && a16(x) && a16(h1) && a16(h2))
         return canon::mlp::forward_tc(n, x, c->d_w1, c->d_mlp + P_B1, c->d_w2, c->d_mlp + P_B2, c->d_w3,
                                       c->d_mlp + P_B3, y, h1, h2, c->d_tc_err, c->num_sms, s);
     return canon::mlp::forward(n, x, c->d_w1, c->d_mlp + P_B1, c->d_w2, c->d_mlp + P_B2, c->d_w3, c->d_mlp + P_B3, y,

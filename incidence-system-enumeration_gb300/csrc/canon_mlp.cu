@@ -10,7 +10,9 @@
 // tiled FP32 reductions over the batch, and Adam keeps FP32 master weights from
 // which the BF16 copies are refreshed after every step.  No counterpart in the
 // reference.
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include "canon_internal.h"
 
@@ -165,9 +167,13 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(long n, const __nv_bfl
 // One CTA (4 warps) takes 128 rows at a time.  Both layers are tcgen05.mma
 // (kind::f16: BF16 operands, FP32 accumulators in tensor memory) issued by one
 // thread: D1[128 x 128] = X[128 x 64] W1^T, then D2[128 x 128] = H1[128 x 128] W2^T.
-// The operands sit in shared memory in the K-major layout without swizzle: 8-row x
-// 16-byte core matrices, the core matrices along K 128 bytes apart (leading byte
-// offset) and the 8-row groups (K/8) x 128 bytes apart (stride byte offset).  Each
+// The operands sit in shared memory in the K-major layout without swizzle, as 8-row x
+// 16-byte core matrices.  X arrives by TMA (cp.async.bulk.tensor): eight boxes of 128
+// rows x 8 elements, each 2 KB with its rows 16 bytes apart, so the core matrices of
+// an 8-row group are 128 bytes apart (stride byte offset) and those along K 2 KB apart
+// (leading byte offset); the next tile's X is requested as soon as this tile's first
+// MMAs are done, and arrives while the rest of the tile runs.  W1, W2 and H1 use
+// 8-row groups (K/8) x 128 bytes apart and K neighbours 128 bytes apart.  Each
 // thread owns one row of the accumulators (tensor-memory lane = row): it reads its
 // row with tcgen05.ld, adds the bias, applies the ReLU and rounds to BF16 -- H1 goes
 // back to shared memory as layer 2's A operand, H2 meets w3 in a per-thread dot
@@ -178,7 +184,9 @@ constexpr int TC_ROWS = 128;
 constexpr uint32_t TC_TMEM_COLS = 256;                  // D1 in columns 0-127, D2 in 128-255
 constexpr uint32_t TC_W1 = 0, TC_W2 = TC_W1 + HID * IN * 2, TC_X = TC_W2 + HID * HID * 2,
                    TC_H1 = TC_X + TC_ROWS * IN * 2, TC_PAR = TC_H1 + TC_ROWS * HID * 2,
-                   TC_BAR = TC_PAR + 3 * HID * 4, TC_END = TC_BAR + 16;
+                   TC_BAR = TC_PAR + 3 * HID * 4, TC_END = TC_BAR + 32;
+// in the barrier block: the MMA barrier at +0, the tensor-memory address at +8, the TMA barrier at +16
+constexpr uint32_t TC_X_CHUNK = TC_ROWS * 16;           // one TMA box: 128 rows x 16 bytes
 constexpr size_t TC_SMEM = TC_END + 1024;               // + the alignment of the base to 1 KB
 // instruction descriptor, kind::f16: FP32 accumulator (bit 4), BF16 A (bits 7-9 = 1) and
 // B (bits 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bit 17, M >> 4 at bit 24
@@ -257,7 +265,21 @@ __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence:
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void async_proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-__global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __nv_bfloat16 *__restrict__ x,
+// the X rows [row0, row0 + 128) as eight TMA boxes (columns 8k .. 8k+7 each) into the
+// tile, all counted on the TMA barrier; rows past the tensor's end arrive as zeros
+__device__ __forceinline__ void tc_load_x(const CUtensorMap *tmap, uint32_t dst, uint32_t bar, long row0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(TC_ROWS * IN * 2)
+                 : "memory");
+#pragma unroll
+    for (int k8 = 0; k8 < IN / 8; ++k8)
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+            "[%4];" ::"r"(dst + k8 * TC_X_CHUNK),
+            "l"(reinterpret_cast<uint64_t>(tmap)), "r"(8 * k8), "r"((int)row0), "r"(bar)
+            : "memory");
+}
+
+__global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __grid_constant__ CUtensorMap xmap,
                                                                 MlpDev wg, float *__restrict__ y,
                                                                 __nv_bfloat16 *__restrict__ h1out,
                                                                 __nv_bfloat16 *__restrict__ h2out, unsigned *err) {
@@ -267,7 +289,7 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __
     unsigned char *sm = tc_smem_raw + pad;
     const uint32_t sbase = raw + pad;
     float *sb1 = reinterpret_cast<float *>(sm + TC_PAR), *sb2 = sb1 + HID, *sw3 = sb2 + HID;
-    const uint32_t bar = sbase + TC_BAR;
+    const uint32_t bar = sbase + TC_BAR, tbar = sbase + TC_BAR + 16;
     uint32_t *s_tmem = reinterpret_cast<uint32_t *>(sm + TC_BAR + 8);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -278,9 +300,14 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    const long tiles = (n + TC_ROWS - 1) / TC_ROWS;
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tbar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // the first tile's X, while the weights are staged
+        if ((long)blockIdx.x < tiles)
+            tc_load_x(&xmap, sbase + TC_X, tbar, (long)blockIdx.x * TC_ROWS);
     }
     // the weights (K-major core-matrix layout) and the biases, once
     for (int i = tid; i < HID * (IN / 8); i += blockDim.x) {
@@ -306,34 +333,42 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __
     const uint32_t d1 = tmem, d2 = tmem + HID;
     const uint32_t lane_base = (uint32_t)(32 * warp) << 16;    // this warp's 32 tensor-memory lanes
     const float b3 = wg.b3[0];
-    uint32_t phase = 0;
-    bool failed = false;
-    const long tiles = (n + TC_ROWS - 1) / TC_ROWS;
+    // the parity each barrier completes next; what is in flight and the parity it completes on
+    uint32_t phase = 0, tphase = 0, mma_parity = 0, x_parity = 0;
+    bool failed = false, x_pending = (long)blockIdx.x < tiles, mma_pending = false;
     for (long tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
         const long r0 = tile * TC_ROWS;
-        // X tile: 128 rows x 8 chunks of 16 bytes (rows past n are zero)
-        for (int i = tid; i < TC_ROWS * (IN / 8); i += blockDim.x) {
-            const int r = i / (IN / 8), k8 = i % (IN / 8);
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (r0 + r < n)
-                v = *reinterpret_cast<const uint4 *>(x + (r0 + r) * IN + k8 * 8);
-            *reinterpret_cast<uint4 *>(sm + TC_X + core_off(r, k8, IN)) = v;
+        // this tile's X (requested one tile earlier)
+        x_parity = tphase;
+        bool ok = tc_wait(tbar, tphase);
+        tphase ^= 1u;
+        x_pending = !ok;
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
         }
-        async_proxy_fence();
-        __syncthreads();
         if (tid == 0) {
             tc_fence_after();
 #pragma unroll
             for (int ks = 0; ks < IN / 16; ++ks)
-                tc_mma(d1, tc_desc(sbase + TC_X + ks * 256, 128, (IN / 8) * 128),
+                tc_mma(d1, tc_desc(sbase + TC_X + ks * 2 * TC_X_CHUNK, TC_X_CHUNK, 128),
                        tc_desc(sbase + TC_W1 + ks * 256, 128, (IN / 8) * 128), ks > 0);
             tc_commit(bar);
         }
-        bool ok = tc_wait(bar, phase);
+        mma_parity = phase;
+        ok = tc_wait(bar, phase);
         phase ^= 1u;
+        mma_pending = !ok;
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
+        }
+        // the X tile is read: request the next one now
+        if (tile + gridDim.x < tiles) {
+            if (tid == 0)
+                tc_load_x(&xmap, sbase + TC_X, tbar, (tile + gridDim.x) * TC_ROWS);
+            x_pending = true;
+            x_parity = tphase;
         }
         tc_fence_after();
         // layer-1 epilogue: H1 = relu(D1 + b1) in BF16, this thread's row
@@ -368,8 +403,10 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __
                        tc_desc(sbase + TC_W2 + ks * 256, 128, (HID / 8) * 128), ks > 0);
             tc_commit(bar);
         }
+        mma_parity = phase;
         ok = tc_wait(bar, phase);
         phase ^= 1u;
+        mma_pending = !ok;
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
@@ -403,8 +440,12 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __
     if (failed) {
         if (tid == 0)
             atomicExch(err, 1u);
-        // the MMAs the barrier waited for: once more, bounded, before their columns are freed
-        (void)tc_wait(bar, phase ^ 1u);
+        // what is still in flight (the MMAs the barrier waited for, a requested X tile):
+        // once more, bounded, before the tensor memory and the shared memory are given up
+        if (mma_pending)
+            (void)tc_wait(bar, mma_parity);
+        if (x_pending)
+            (void)tc_wait(tbar, x_parity);
     }
     tc_fence_before();
     __syncthreads();
@@ -705,12 +746,33 @@ cudaError_t forward_tc(long n, const void *x, const void *w1, const float *b1, c
     long grid = 2L * (num_sms > 0 ? num_sms : 1);
     if (grid > tiles)
         grid = tiles;
+    // X as a 2-D tensor (64 BF16 columns, n rows of 128 bytes) read in boxes of 8 x 128
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess)
+            return e;
+        if (q != cudaDriverEntryPointSuccess || !fn)
+            return cudaErrorSymbolNotFound;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    CUtensorMap xmap;
+    const cuuint64_t dims[2] = {(cuuint64_t)IN, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {(cuuint64_t)IN * 2};
+    const cuuint32_t box[2] = {8, (cuuint32_t)TC_ROWS};
+    const cuuint32_t estr[2] = {1, 1};
+    if (encode(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(x), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
     const cudaError_t e =
         cudaFuncSetAttribute(mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
     if (e != cudaSuccess)
         return e;
-    mlp_forward_tc_kernel<<<(int)grid, 128, TC_SMEM, s>>>(n, (const __nv_bfloat16 *)x, w, y, (__nv_bfloat16 *)h1,
-                                                          (__nv_bfloat16 *)h2, err);
+    mlp_forward_tc_kernel<<<(int)grid, 128, TC_SMEM, s>>>(n, xmap, w, y, (__nv_bfloat16 *)h1, (__nv_bfloat16 *)h2,
+                                                          err);
     return cudaGetLastError();
 }
 

@@ -203,20 +203,23 @@ def test_config4_eval_batch_learned_order_matches_oracle():
 
 
 def test_tensor_core_forward_matches_the_warp_mma_path(data):
-    """The forward pass on tcgen05 (FP32 accumulators in tensor memory, 128 rows per
-    CTA) against the warp-level mma.sync path on the same BF16 inputs: logits within
-    BF16 rounding of the hidden layers, on sizes that end inside a 128-row tile; and
-    the training gradients of both paths agree."""
+    """The forward pass on tcgen05 (X by TMA, FP32 accumulators in tensor memory, 128
+    rows per CTA) against the warp-level mma.sync path on the same BF16 inputs: logits
+    within BF16 rounding of the hidden layers, on sizes that end inside a 128-row tile
+    (batches under 128 rows take the warp-level path in both contexts); and the
+    training gradients of both paths agree."""
     X, t = data
+    XL = np.random.default_rng(22).random((4095, 64)).astype(np.float32)
     p = G.init_mlp_params(21)
     p[8192:8320] = 0.05
     tc = G.Context(max_items=1 << 12, aut_cap=4)
     mm = G.Context(max_items=1 << 12, aut_cap=4, options=G.OPT_MLP_WARP_MMA)
     try:
-        for n in (1, 127, 128, 129, 1000):
+        for n in (1, 127, 128, 129, 1000, 4095):
+            assert n <= len(XL)
             ys = []
             for c in (tc, mm):
-                dx = to_device(c, G.to_bf16_bits(X[:n]))
+                dx = to_device(c, G.to_bf16_bits(XL[:n]))
                 dy = c.alloc(4 * n)
                 try:
                     c.mlp_forward(n, dx, p, dy)
@@ -226,7 +229,7 @@ def test_tensor_core_forward_matches_the_warp_mma_path(data):
                     c.free(dy)
             d = np.abs(ys[0] - ys[1])
             assert d.max() < 2e-2 and np.median(d) < 1e-3, (n, d.max(), np.median(d))
-            _, _, _, _, _, yr = ref_forward(p, X[:n])
+            _, _, _, _, _, yr = ref_forward(p, XL[:n])
             assert np.allclose(ys[0], yr, rtol=2e-2, atol=2e-2), n
         gs = []
         for c in (tc, mm):
