@@ -129,21 +129,45 @@ __device__ __forceinline__ int eval_node_planes(S sm, unsigned w, unsigned lv, u
 // the columns of level lv+1 after row x was taken at level lv: inside every orbit of
 // level lv, the columns with a 1 in row x first (one pass, a write pointer per orbit);
 // bt: the columns walked (columns past the matrix's own hold no 1 and never move)
+// With FB > 0 the column masks are loaded RD columns ahead of their turn: a swap at
+// column p writes only positions w <= p, never a column still to come, so the early
+// loads read what the in-order pass would, and their latency overlaps the swaps instead
+// of following each one (the compiler cannot see that w <= p and would keep every load
+// behind the stores before it).
+constexpr unsigned RD = 4;
 template <unsigned FB = 0, typename S>
 __device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, unsigned bt) {
-    if (FB)
-        bt = FB;
     const uint64_t starts = L_(lv);
     unsigned w = 0;
-#pragma unroll(FB ? FB : 1)
-    for (unsigned p = 0; p < bt; ++p) {
-        if ((starts >> p) & 1u)
-            w = p;
-        const uint16_t c = CM_(p);
-        if ((c >> x) & 1u) {
-            CM_(p) = CM_(w);
-            CM_(w) = c;
-            ++w;
+    if constexpr (FB > 0) {
+        static_assert(FB >= RD, "the look-ahead fits the columns");
+        uint16_t ahead[RD];
+#pragma unroll
+        for (unsigned q = 0; q < RD; ++q)
+            ahead[q] = CM_(q);
+#pragma unroll
+        for (unsigned p = 0; p < FB; ++p) {
+            if ((starts >> p) & 1u)
+                w = p;
+            const uint16_t c = ahead[p % RD];
+            if (p + RD < FB)
+                ahead[p % RD] = CM_(p + RD);
+            if ((c >> x) & 1u) {
+                CM_(p) = CM_(w);
+                CM_(w) = c;
+                ++w;
+            }
+        }
+    } else {
+        for (unsigned p = 0; p < bt; ++p) {
+            if ((starts >> p) & 1u)
+                w = p;
+            const uint16_t c = CM_(p);
+            if ((c >> x) & 1u) {
+                CM_(p) = CM_(w);
+                CM_(w) = c;
+                ++w;
+            }
         }
     }
 }
