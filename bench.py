@@ -396,7 +396,7 @@ def run_enum(args):
             found, st = ctx.enumerate_ksys(*params)
         runs.append((len(found), st.checks, st.seconds, st.kernel_ms, st.batches,
                      [int(x) for x in st.level_checks], [round(float(x), 3) for x in st.level_kernel_ms],
-                     st.gen_seconds, int(st.trials)))
+                     st.gen_seconds, int(st.trials), [round(float(x), 3) for x in st.level_gen_ms]))
     launches = ctx.kernel_launches() - l0
     timed = runs[args.warmup:]
     secs = sum(r[2] for r in timed)
@@ -421,7 +421,8 @@ def run_enum(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 bit rows / u8",
             "data": "exhaustive", "config": {"workload": desc, "designs": timed[0][0],
                                              "checks_per_step": timed[0][1], "batches_per_step": timed[0][4],
-                                             "level_checks": timed[0][5], "level_kernel_ms": timed[-1][6]},
+                                             "level_checks": timed[0][5], "level_kernel_ms": timed[-1][6],
+                                             "level_gen_ms": timed[-1][9]},
             "checks_per_s": checks / secs, "kernel_ms_per_step": sum(r[3] for r in timed) / args.steps,
             "gen_ms_per_step": 1e3 * sum(r[7] for r in timed) / args.steps,
             "cpu_baseline": cpu, "gpu_launches": launches}
