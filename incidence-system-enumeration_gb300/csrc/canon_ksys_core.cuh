@@ -35,25 +35,21 @@ __device__ __forceinline__ void eval_candidate(unsigned c, unsigned np, unsigned
     const unsigned t = qd & ((1u << ng) - 1u);
     const unsigned h = qd >> ng;
     const uint8_t *a = c_heap + (c_heap_off[ng] + h) * 6u;
-    // trmk: positions of round d -> labels (cnvCheckKm, cnv.cpp:168-185)
-    uint64_t trmk = 0;
-    for (unsigned i = 0; i < ng; ++i) {
-        const unsigned tg = (t >> (ng - 1u - i)) & 1u;
-        const unsigned base = 2u * a[i];
-        trmk = nib_set(trmk, 2u * i, base + tg);
-        trmk = nib_set(trmk, 2u * i + 1u, base + 1u - tg);
-    }
-    uint64_t ttr = 0;
+    // the relabeling (player -> label) and its inverse, pair by pair of round d: the
+    // players of its i-th pair get label 2a[i] + t_i and the other label of that group,
+    // in the order the in-group bit says (cnvCheckKm, cnv.cpp:168-185)
     const uint64_t sd = seq[d];
-    for (unsigned p = 0; p < np; ++p)
-        ttr = nib_set(ttr, nib_get(sd, p), nib_get(trmk, p));
+    uint64_t ttr = 0, inv = 0;
+    for (unsigned i = 0; i < ng; ++i) {
+        const unsigned lab = 2u * a[i] + ((t >> (ng - 1u - i)) & 1u);
+        const unsigned p0 = nib_get(sd, 2u * i), p1 = nib_get(sd, 2u * i + 1u);
+        ttr |= ((uint64_t)lab << (4u * p0)) | ((uint64_t)(lab ^ 1u) << (4u * p1));
+        inv |= ((uint64_t)p0 << (4u * lab)) | ((uint64_t)p1 << (4u * (lab ^ 1u)));
+    }
     o.ttr = ttr;
     o.res = 0;
     if (c == 0)
         return;   // the identity is registered without a comparison (cnv.cpp:85-89)
-    uint64_t inv = 0;
-    for (unsigned x = 0; x < np; ++x)
-        inv = nib_set(inv, nib_get(ttr, x), x);
     o.inv = inv;
     const unsigned u = nib_get(inv, 0);
     // second entries (partner of label 0) of the relabelled rounds; the sorted
@@ -79,19 +75,30 @@ __device__ __forceinline__ void eval_candidate(unsigned c, unsigned np, unsigned
         }
         const unsigned r = nib_get(pair[u], w) - 1u;
         const uint64_t pr = part[r];
-        uint64_t q = 0;
-        for (unsigned x = 0; x < np; ++x)
-            q = nib_set(q, nib_get(ttr, x), nib_get(ttr, nib_get(pr, x)));
         const uint64_t orig = part[i];
-        if (q == orig) {
+        // the relabelled round r against round i, label by label (q[y] = the label of the
+        // partner of the player labelled y): rounds in canonical pair order compare like
+        // their partner tables, so the first label whose partner differs decides, and
+        // most relabelings differ within the first labels
+        int cmp = 0;
+        for (unsigned y = 0; y < np; ++y) {
+            const unsigned qy = nib_get(ttr, nib_get(pr, nib_get(inv, y)));
+            const unsigned oy = nib_get(orig, y);
+            if (qy != oy) {
+                cmp = qy < oy ? -1 : 1;
+                break;
+            }
+        }
+        if (!cmp) {
             if (daymax < r)
                 daymax = r;
             continue;
         }
-        // rounds in canonical pair order compare like their partner tables: the
-        // first player whose partner differs decides
-        const unsigned x0 = (unsigned)(__ffsll((long long)(q ^ orig)) - 1) >> 2;
-        if (nib_get(q, x0) < nib_get(orig, x0)) {
+        if (cmp < 0) {
+            // the whole relabelled round, for the player index of the rejection
+            uint64_t q = 0;
+            for (unsigned x = 0; x < np; ++x)
+                q = nib_set(q, nib_get(ttr, x), nib_get(ttr, nib_get(pr, x)));
             o.res = -1;
             o.row = i;
             o.src = r;
