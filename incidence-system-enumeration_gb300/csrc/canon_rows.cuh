@@ -172,9 +172,15 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
     uint32_t count = 0;
     int q = 0;
     left[0] = (uint8_t)d.r;
-    bool enter = true;
+    // The walk is a state machine that takes one step per iteration -- set up an orbit,
+    // try one value, back up one orbit, or test a leaf -- so that the threads of a warp,
+    // which walk different parents, stay in step instead of each looping over its own
+    // run of rejected values.  The children come in the order of the plain depth-first
+    // walk.
+    enum : int { ENTER = 0, TRY = 1, BACK = 2 };
+    int state = ENTER;
     for (;;) {
-        if (enter) {
+        if (state == ENTER) {
             if (q == norb) {
                 bool ok = left[q] == 0 && lamb.w[0] == B64 && lamb.w[1] == B64;
                 // the swap test against every row i >= 1 (the orbits of level i are
@@ -248,7 +254,7 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
                 up64.sub(mq, hi[q]);
                 up64.w[0] += B64;
                 up64.w[1] += B64;
-                enter = false;
+                state = TRY;
                 continue;
             }
             mq = spread16(ones[q]);
@@ -276,55 +282,56 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
             up64.sub(mq, hi[q]);
             up64.w[0] += B64;
             up64.w[1] += B64;
-        }
-        // undo the value applied at level q, then try the next one
-        if (x[q] != 0xFF) {
-            lamb.add(mq, x[q]);
-            x[q] = 0xFF;
-        }
-        bool moved = false;
-        while (nxt[q] > mn[q]) {
-            const int xv = --nxt[q];
-            Bytes16 l = lamb;
-            l.sub(mq, (unsigned)xv);
-            // per row, with the 1s left after this orbit (left'), the capacities of the
-            // later orbits (ca', cn') and their parts that meet row i (RC', RN'):
-            //   RN' <= lam' <= RC'                  (byte high bits of a and bb)
-            //   RC' - lam' <= ca' - left'           (the 1s outside row i's orbits fit)
-            //   lam' - RN' <= left' - cn'           (and fill what must be filled)
-            const int lf1 = left[q] - xv;
-            const uint64_t k2 = ONE8 * (uint64_t)(ca - hi[q] - lf1) | HIB;
-            const uint64_t k3 = ONE8 * (uint64_t)(lf1 - (cn - lo[q])) | HIB;
-            uint64_t g = HIB;
-#pragma unroll
-            for (int w = 0; w < 2; ++w) {
-                const uint64_t a = (up64.w[w] | HIB) - l.w[w];      // 128 + RC' - lam'
-                const uint64_t bb = (l.w[w] | HIB) - lo64.w[w];     // 128 + lam' - RN'
-                g &= a & bb & (k2 - (a & LOW7)) & (k3 - (bb & LOW7));
-            }
-            if (g != HIB)
-                continue;
-            lamb = l;
-            x[q] = (uint8_t)xv;
-            left[q + 1] = (uint8_t)(left[q] - xv);
-            // still equal to row n-1: its value on the orbit taken everywhere
-            const bool prev1 = (ones[q] >> (n - 1)) & 1u;
-            if (((tied >> q) & 1u) && xv == (prev1 ? len[q] : 0))
-                tied |= 1ull << (q + 1);
-            else
-                tied &= ~(1ull << (q + 1));
-            moved = true;
-            break;
-        }
-        if (moved) {
-            ca -= hi[q];
-            cn -= lo[q];
-            rc.sub(mq, hi[q]);
-            rn.sub(mq, lo[q]);
-            ++q;
-            enter = true;
+            state = TRY;
             continue;
         }
+        if (state == TRY) {
+            // undo the value applied at level q, then try the next one
+            if (x[q] != 0xFF) {
+                lamb.add(mq, x[q]);
+                x[q] = 0xFF;
+            }
+            if (nxt[q] > mn[q]) {
+                const int xv = --nxt[q];
+                Bytes16 l = lamb;
+                l.sub(mq, (unsigned)xv);
+                // per row, with the 1s left after this orbit (left'), the capacities of the
+                // later orbits (ca', cn') and their parts that meet row i (RC', RN'):
+                //   RN' <= lam' <= RC'                  (byte high bits of a and bb)
+                //   RC' - lam' <= ca' - left'           (the 1s outside row i's orbits fit)
+                //   lam' - RN' <= left' - cn'           (and fill what must be filled)
+                const int lf1 = left[q] - xv;
+                const uint64_t k2 = ONE8 * (uint64_t)(ca - hi[q] - lf1) | HIB;
+                const uint64_t k3 = ONE8 * (uint64_t)(lf1 - (cn - lo[q])) | HIB;
+                uint64_t g = HIB;
+#pragma unroll
+                for (int w = 0; w < 2; ++w) {
+                    const uint64_t a = (up64.w[w] | HIB) - l.w[w];      // 128 + RC' - lam'
+                    const uint64_t bb = (l.w[w] | HIB) - lo64.w[w];     // 128 + lam' - RN'
+                    g &= a & bb & (k2 - (a & LOW7)) & (k3 - (bb & LOW7));
+                }
+                if (g == HIB) {
+                    lamb = l;
+                    x[q] = (uint8_t)xv;
+                    left[q + 1] = (uint8_t)(left[q] - xv);
+                    // still equal to row n-1: its value on the orbit taken everywhere
+                    const bool prev1 = (ones[q] >> (n - 1)) & 1u;
+                    if (((tied >> q) & 1u) && xv == (prev1 ? len[q] : 0))
+                        tied |= 1ull << (q + 1);
+                    else
+                        tied &= ~(1ull << (q + 1));
+                    ca -= hi[q];
+                    cn -= lo[q];
+                    rc.sub(mq, hi[q]);
+                    rn.sub(mq, lo[q]);
+                    ++q;
+                    state = ENTER;
+                }
+                continue;
+            }
+            state = BACK;
+        }
+        // no value left at orbit q: back up one orbit
         if (q == 0)
             break;
         --q;
@@ -341,7 +348,7 @@ CANON_HD uint32_t children(const Params &d, const uint64_t *parent, int n, uint6
         up64.sub(mq, hi[q]);
         up64.w[0] += B64;
         up64.w[1] += B64;
-        enter = false;
+        state = TRY;
     }
     return count;
 }
