@@ -1116,23 +1116,30 @@ static cudaError_t mlp_grad_pass(canon_ctx *c, long n, const void *d_x, const fl
     cudaError_t e = ensure_scratch(c, (size_t)n * 4 + act * 2 * 2 + (size_t)n * 4 + act * 4 * 2 + 1024);
     if (e != cudaSuccess)
         return e;
-    // the BF16 activations first: 256-byte rows, so both start 16-byte aligned (the
-    // tensor-core forward stores them 16 bytes at a time)
+    // the per-row arrays of 128 values first (256- or 512-byte rows), so every one starts
+    // 16-byte aligned (the tensor-core passes move them 16 bytes at a time), then the
+    // per-row scalars
     char *base = static_cast<char *>(c->d_scratch);
     void *h1 = base;
     void *h2 = base + act * 2;
-    float *logit = reinterpret_cast<float *>(base + act * 4);
-    float *dy = logit + n;
-    float *dh2 = reinterpret_cast<float *>(base + act * 4 + (size_t)n * 8);
+    float *dh2 = reinterpret_cast<float *>(base + act * 4);
     float *dh1 = dh2 + act;
+    float *logit = dh1 + act;
+    float *dy = logit + n;
     cudaStream_t s = c->stream;
     e = cudaMemsetAsync(c->d_grad, 0, canon::mlp::N_PARAMS * 4, s);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(c->d_loss, 0, 4, s);
     if (e == cudaSuccess)
         e = mlp_forward_installed(c, n, d_x, logit, h1, h2, s);
-    if (e == cudaSuccess)
-        e = canon::mlp::backward(n, logit, d_labels, h1, h2, c->d_w3, c->d_w2t, dy, dh2, dh1, c->d_loss, c->num_sms, s);
+    if (e == cudaSuccess) {
+        if (!(c->cfg.options & CANON_OPT_MLP_WARP_MMA) && c->d_tc_err && n >= 128)
+            e = canon::mlp::backward_tc(n, logit, d_labels, h1, h2, c->d_w3, c->d_w2t, dy, dh2, dh1, c->d_loss,
+                                        c->d_tc_err, c->num_sms, s);
+        else
+            e = canon::mlp::backward(n, logit, d_labels, h1, h2, c->d_w3, c->d_w2t, dy, dh2, dh1, c->d_loss,
+                                     c->num_sms, s);
+    }
     if (e == cudaSuccess)
         e = canon::mlp::weight_grads(n, dh1, dh2, dy, d_x, h1, h2, c->d_grad, c->num_sms, s);
     c->launches += 6;

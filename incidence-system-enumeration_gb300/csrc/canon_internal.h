@@ -110,6 +110,10 @@ cudaError_t forward(long n, const void *x, const void *w1, const float *b1, cons
 cudaError_t forward_tc(long n, const void *x, const void *w1, const float *b1, const void *w2, const float *b2,
                        const void *w3, const float *b3, float *y, void *h1, void *h2, unsigned *err, int num_sms,
                        cudaStream_t s);
+// the backward pass with dH1 = dH2 W2 on tcgen05 (h1, h2, dh1, dh2 16-byte aligned)
+cudaError_t backward_tc(long n, const float *logit, const float *label, const void *h1, const void *h2,
+                        const void *w3, const void *w2t, float *dy, float *dh2, float *dh1, float *loss,
+                        unsigned *err, int num_sms, cudaStream_t s);
 cudaError_t backward(long n, const float *logit, const float *label, const void *h1, const void *h2,
                      const void *w3, const void *w2t, float *dy, float *dh2, float *dh1, float *loss,
                      int num_sms, cudaStream_t s);

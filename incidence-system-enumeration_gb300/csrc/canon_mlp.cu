@@ -456,6 +456,162 @@ __global__ void __launch_bounds__(128, 1) mlp_forward_tc_kernel(long n, const __
     }
 }
 
+// The backward pass on tcgen05, 128 rows per CTA, one row per thread: dy and the BCE loss
+// of the row, dH2 = dy w3 [H2 > 0] (FP32 to global memory for the weight gradients, BF16
+// into shared memory as the A operand), then dH1 = (dH2 W2) [H1 > 0] as 8 MMAs of
+// 128 x 128 x 16 into 128 tensor-memory columns, with W2 transposed ([in][out], K-major
+// for B) staged once per CTA.  The same operand layouts, descriptors and bounded waits as
+// mlp_forward_tc_kernel.
+constexpr uint32_t TB_W2T = 0, TB_A = TB_W2T + HID * HID * 2, TB_W3 = TB_A + TC_ROWS * HID * 2,
+                   TB_BAR = TB_W3 + HID * 4, TB_END = TB_BAR + 16;
+constexpr size_t TB_SMEM = TB_END + 1024;
+constexpr uint32_t TB_TMEM_COLS = 128;
+
+__global__ void __launch_bounds__(128, 1) mlp_backward_tc_kernel(long n, const float *__restrict__ logit,
+                                                                 const float *__restrict__ label,
+                                                                 const __nv_bfloat16 *__restrict__ h1,
+                                                                 const __nv_bfloat16 *__restrict__ h2,
+                                                                 const __nv_bfloat16 *__restrict__ w3,
+                                                                 const __nv_bfloat16 *__restrict__ w2t,
+                                                                 float *__restrict__ dy, float *__restrict__ dh2,
+                                                                 float *__restrict__ dh1, float *__restrict__ loss_sum,
+                                                                 unsigned *err) {
+    extern __shared__ __align__(16) unsigned char tb_smem_raw[];
+    const uint32_t raw = (uint32_t)__cvta_generic_to_shared(tb_smem_raw);
+    const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
+    unsigned char *sm = tb_smem_raw + pad;
+    const uint32_t sbase = raw + pad;
+    float *sw3 = reinterpret_cast<float *>(sm + TB_W3);
+    const uint32_t bar = sbase + TB_BAR;
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(sm + TB_BAR + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + TB_BAR + 8),
+                     "r"(TB_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int i = tid; i < HID * (HID / 8); i += blockDim.x) {
+        const int r = i / (HID / 8), k8 = i % (HID / 8);
+        *reinterpret_cast<uint4 *>(sm + TB_W2T + core_off(r, k8, HID)) =
+            *reinterpret_cast<const uint4 *>(w2t + r * HID + k8 * 8);
+    }
+    for (int i = tid; i < HID; i += blockDim.x)
+        sw3[i] = __bfloat162float(w3[i]);
+    async_proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    const float inv_n = 1.f / (float)n;
+    uint32_t phase = 0, mma_parity = 0;
+    bool failed = false, mma_pending = false;
+    const long tiles = (n + TC_ROWS - 1) / TC_ROWS;
+    for (long tile = blockIdx.x; tile < tiles && !failed; tile += gridDim.x) {
+        const int row = 32 * warp + lane;
+        const long r = tile * TC_ROWS + row;
+        const bool in = r < n;
+        // dy and the loss of this row (rows past n contribute nothing)
+        float d = 0.f, l = 0.f;
+        if (in) {
+            const float z = logit[r], t = label[r];
+            d = (1.f / (1.f + __expf(-z)) - t) * inv_n;
+            l = fmaxf(z, 0.f) - z * t + log1pf(__expf(-fabsf(z)));
+            dy[r] = d;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            l += __shfl_xor_sync(0xFFFFFFFFu, l, o);
+        if (lane == 0 && l != 0.f)
+            atomicAdd(loss_sum, l);
+        // dH2 of this row: FP32 out, BF16 into the A tile
+#pragma unroll 1
+        for (int k8 = 0; k8 < HID / 8; ++k8) {
+            uint4 hv = make_uint4(0u, 0u, 0u, 0u);
+            if (in)
+                hv = *reinterpret_cast<const uint4 *>(h2 + r * HID + k8 * 8);
+            const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+            float g[8];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = k8 * 8 + 2 * j;
+                g[2 * j] = bf_lo(hw[j]) > 0.f ? d * sw3[c] : 0.f;
+                g[2 * j + 1] = bf_hi(hw[j]) > 0.f ? d * sw3[c + 1] : 0.f;
+            }
+            if (in) {
+                float4 *dst = reinterpret_cast<float4 *>(dh2 + r * HID + k8 * 8);
+                dst[0] = make_float4(g[0], g[1], g[2], g[3]);
+                dst[1] = make_float4(g[4], g[5], g[6], g[7]);
+            }
+            *reinterpret_cast<uint4 *>(sm + TB_A + core_off(row, k8, HID)) =
+                make_uint4(pack_bf16(g[0], g[1]), pack_bf16(g[2], g[3]), pack_bf16(g[4], g[5]),
+                           pack_bf16(g[6], g[7]));
+        }
+        tc_fence_before();
+        async_proxy_fence();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < HID / 16; ++ks)
+                tc_mma(tmem, tc_desc(sbase + TB_A + ks * 256, 128, (HID / 8) * 128),
+                       tc_desc(sbase + TB_W2T + ks * 256, 128, (HID / 8) * 128), ks > 0);
+            tc_commit(bar);
+        }
+        mma_parity = phase;
+        const bool ok = tc_wait(bar, phase);
+        phase ^= 1u;
+        mma_pending = !ok;
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        tc_fence_after();
+        // dH1 = (dH2 W2) [H1 > 0]
+#pragma unroll 1
+        for (int c = 0; c < HID / 32; ++c) {
+            float f[32];
+            tc_ld32(tmem + lane_base + 32 * c, f);
+            if (in) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint4 hv = *reinterpret_cast<const uint4 *>(h1 + r * HID + 32 * c + 8 * q);
+                    const uint32_t hw[4] = {hv.x, hv.y, hv.z, hv.w};
+                    float o[8];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        o[2 * j] = bf_lo(hw[j]) > 0.f ? f[8 * q + 2 * j] : 0.f;
+                        o[2 * j + 1] = bf_hi(hw[j]) > 0.f ? f[8 * q + 2 * j + 1] : 0.f;
+                    }
+                    float4 *dst = reinterpret_cast<float4 *>(dh1 + r * HID + 32 * c + 8 * q);
+                    dst[0] = make_float4(o[0], o[1], o[2], o[3]);
+                    dst[1] = make_float4(o[4], o[5], o[6], o[7]);
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (failed) {
+        if (tid == 0)
+            atomicExch(err, 1u);
+        if (mma_pending)
+            (void)tc_wait(bar, mma_parity);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TB_TMEM_COLS)
+                     : "memory");
+    }
+}
+
 // Backward of the binary cross-entropy on the logits: dy, dH2 = dy w3 [H2 > 0]
 // and dH1 = (dH2 W2) [H1 > 0] (tensor cores; w2t is W2 transposed, [in][out]).
 __global__ void mlp_backward_kernel(long n, const float *__restrict__ logit, const float *__restrict__ label,
@@ -773,6 +929,26 @@ cudaError_t forward_tc(long n, const void *x, const void *w1, const float *b1, c
         return e;
     mlp_forward_tc_kernel<<<(int)grid, 128, TC_SMEM, s>>>(n, xmap, w, y, (__nv_bfloat16 *)h1, (__nv_bfloat16 *)h2,
                                                           err);
+    return cudaGetLastError();
+}
+
+cudaError_t backward_tc(long n, const float *logit, const float *label, const void *h1, const void *h2,
+                        const void *w3, const void *w2t, float *dy, float *dh2, float *dh1, float *loss,
+                        unsigned *err, int num_sms, cudaStream_t s) {
+    if (n <= 0)
+        return cudaSuccess;
+    const long tiles = (n + TC_ROWS - 1) / TC_ROWS;
+    // three CTAs fit an SM by shared memory (66 KB each); 3 x 128 tensor-memory columns
+    long grid = 3L * (num_sms > 0 ? num_sms : 1);
+    if (grid > tiles)
+        grid = tiles;
+    const cudaError_t e =
+        cudaFuncSetAttribute(mlp_backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TB_SMEM);
+    if (e != cudaSuccess)
+        return e;
+    mlp_backward_tc_kernel<<<(int)grid, 128, TB_SMEM, s>>>(n, logit, label, (const __nv_bfloat16 *)h1,
+                                                           (const __nv_bfloat16 *)h2, (const __nv_bfloat16 *)w3,
+                                                           (const __nv_bfloat16 *)w2t, dy, dh2, dh1, loss, err);
     return cudaGetLastError();
 }
 
