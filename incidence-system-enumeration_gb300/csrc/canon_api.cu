@@ -1140,8 +1140,13 @@ static cudaError_t mlp_grad_pass(canon_ctx *c, long n, const void *d_x, const fl
             e = canon::mlp::backward(n, logit, d_labels, h1, h2, c->d_w3, c->d_w2t, dy, dh2, dh1, c->d_loss,
                                      c->num_sms, s);
     }
-    if (e == cudaSuccess)
-        e = canon::mlp::weight_grads(n, dh1, dh2, dy, d_x, h1, h2, c->d_grad, c->num_sms, s);
+    if (e == cudaSuccess) {
+        if (!(c->cfg.options & CANON_OPT_MLP_WARP_MMA) && c->d_tc_err && n >= 128 &&
+            ((uintptr_t)d_x & 15u) == 0)
+            e = canon::mlp::weight_grads_tc(n, dh1, dh2, dy, d_x, h1, h2, c->d_grad, c->d_tc_err, c->num_sms, s);
+        else
+            e = canon::mlp::weight_grads(n, dh1, dh2, dy, d_x, h1, h2, c->d_grad, c->num_sms, s);
+    }
     c->launches += 6;
     return e;
 }

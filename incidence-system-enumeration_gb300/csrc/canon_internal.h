@@ -119,6 +119,10 @@ cudaError_t backward(long n, const float *logit, const float *label, const void 
                      int num_sms, cudaStream_t s);
 cudaError_t weight_grads(long n, const float *dh1, const float *dh2, const float *dy, const void *x,
                          const void *h1, const void *h2, float *grad, int num_sms, cudaStream_t s);
+// the same weight gradients as GEMMs over the batch rows on tcgen05 (dh1, dh2 16-byte aligned)
+cudaError_t weight_grads_tc(long n, const float *dh1, const float *dh2, const float *dy, const void *x,
+                            const void *h1, const void *h2, float *grad, unsigned *err, int num_sms,
+                            cudaStream_t s);
 cudaError_t adam(int count, float *p, const float *grad, float *m, float *v, float lr, int step, void *w1,
                  void *w2, void *w2t, void *w3, cudaStream_t s);
 cudaError_t features(uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *rows, void *feat,

@@ -612,6 +612,160 @@ __global__ void __launch_bounds__(128, 1) mlp_backward_tc_kernel(long n, const f
     }
 }
 
+// Weight gradients on tcgen05: G[o][i] = sum over rows of dh[row][o] * act[row][i], the
+// batch rows being the contraction.  A CTA takes 128-row K tiles in turn and accumulates in
+// tensor memory; each thread stages its row transposed into the K-major core-matrix layout
+// (A[o][row] = BF16 of dh, B[i][row] = act), so the operands are those of the forward pass
+// with the rows as K.  B gets a row of ones (the valid rows) after its IN activation rows, so
+// column IN of the product is the bias gradient sum dh[row][o]; 15 zero rows pad N to a
+// multiple of 16.  At the end every CTA adds its 128 x (IN + 1) partial sums to the FP32
+// gradient.  Shared memory is padded so that at most two CTAs share an SM: two 256-column
+// tensor-memory allocations never wait.
+template <int IN>
+struct WgLayout {
+    static constexpr int NB = IN + 16;                               // B rows
+    static constexpr uint32_t A = 0, B = TC_ROWS * HID * 2, BAR = B + NB * TC_ROWS * 2, END = BAR + 16;
+    static constexpr size_t SMEM = 100 * 1024 + 1024;                // two CTAs per SM at most
+    static_assert(END + 1024 <= SMEM, "tiles fit");
+    // kind::f16, FP32 accumulator, BF16 A and B, K-major, N = NB, M = 128
+    static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(NB >> 3) << 17) |
+                                      ((uint32_t)(TC_ROWS >> 4) << 24);
+};
+constexpr uint32_t WG_TMEM_COLS = 256;
+
+template <int IN>
+__global__ void __launch_bounds__(128, 1) weight_grad_tc_kernel(long n, const float *__restrict__ dh,
+                                                                const __nv_bfloat16 *__restrict__ act,
+                                                                float *__restrict__ gw, float *__restrict__ gb,
+                                                                unsigned *err) {
+    using L = WgLayout<IN>;
+    extern __shared__ __align__(16) unsigned char wg_smem_raw[];
+    const uint32_t raw = (uint32_t)__cvta_generic_to_shared(wg_smem_raw);
+    const uint32_t pad = ((raw + 1023u) & ~1023u) - raw;
+    unsigned char *sm = wg_smem_raw + pad;
+    const uint32_t sbase = raw + pad;
+    const uint32_t bar = sbase + L::BAR;
+    uint32_t *s_tmem = reinterpret_cast<uint32_t *>(sm + L::BAR + 8);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long tiles = (n + TC_ROWS - 1) / TC_ROWS;
+    if ((long)blockIdx.x >= tiles)
+        return;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + L::BAR + 8),
+                     "r"(WG_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // B rows IN + 1 .. NB - 1 stay zero
+    for (int i = tid; i < (L::NB - IN - 1) * (TC_ROWS / 8); i += blockDim.x) {
+        const int r = IN + 1 + i / (TC_ROWS / 8), k8 = i % (TC_ROWS / 8);
+        *reinterpret_cast<uint4 *>(sm + L::B + core_off(r, k8, TC_ROWS)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *s_tmem;
+    // this thread's place along K in every tile: K-chunk tid / 8, element tid % 8
+    const uint32_t kofs = (uint32_t)(tid >> 3) * 128u + (uint32_t)(tid & 7) * 2u;
+    uint32_t phase = 0, mma_parity = 0;
+    bool failed = false, mma_pending = false, first = true;
+    for (long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const long r = tile * TC_ROWS + tid;
+        const bool in = r < n;
+        // A[o][k] = dh[r][o]
+#pragma unroll 1
+        for (int o8 = 0; o8 < HID / 8; ++o8) {
+            float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+            if (in) {
+                v0 = *reinterpret_cast<const float4 *>(dh + r * HID + o8 * 8);
+                v1 = *reinterpret_cast<const float4 *>(dh + r * HID + o8 * 8 + 4);
+            }
+            const float v[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+            unsigned char *dst = sm + L::A + (uint32_t)o8 * (HID / 8) * 128u + kofs;
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                *reinterpret_cast<__nv_bfloat16 *>(dst + j * 16) = __float2bfloat16_rn(v[j]);
+        }
+        // B[i][k] = act[r][i], and the row of ones
+#pragma unroll 1
+        for (int i8 = 0; i8 < IN / 8; ++i8) {
+            uint4 a = make_uint4(0u, 0u, 0u, 0u);
+            if (in)
+                a = *reinterpret_cast<const uint4 *>(act + r * IN + i8 * 8);
+            const uint32_t w[4] = {a.x, a.y, a.z, a.w};
+            unsigned char *dst = sm + L::B + (uint32_t)i8 * (TC_ROWS / 8) * 128u + kofs;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                *reinterpret_cast<uint16_t *>(dst + (2 * j) * 16) = (uint16_t)(w[j] & 0xFFFFu);
+                *reinterpret_cast<uint16_t *>(dst + (2 * j + 1) * 16) = (uint16_t)(w[j] >> 16);
+            }
+        }
+        *reinterpret_cast<__nv_bfloat16 *>(sm + L::B + (uint32_t)(IN / 8) * (TC_ROWS / 8) * 128u + kofs) =
+            __float2bfloat16_rn(in ? 1.f : 0.f);
+        tc_fence_before();
+        async_proxy_fence();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < TC_ROWS / 16; ++ks) {
+                const uint64_t ad = tc_desc(sbase + L::A + ks * 256, 128, (TC_ROWS / 8) * 128);
+                const uint64_t bd = tc_desc(sbase + L::B + ks * 256, 128, (TC_ROWS / 8) * 128);
+                const uint32_t acc = (!first || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(L::IDESC), "r"(acc));
+            }
+            tc_commit(bar);
+        }
+        first = false;
+        mma_parity = phase;
+        const bool ok = tc_wait(bar, phase);
+        phase ^= 1u;
+        mma_pending = !ok;
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+    }
+    if (!failed) {
+        tc_fence_after();
+        // row o = this thread's tensor-memory lane: add the partial sums
+        const int o = 32 * warp + lane;
+        const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+#pragma unroll 1
+        for (int c = 0; c < (L::NB + 31) / 32; ++c) {
+            float f[32];
+            tc_ld32(tmem + lane_base + 32 * c, f);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int i = 32 * c + j;
+                if (i < IN)
+                    atomicAdd(gw + o * IN + i, f[j]);
+                else if (i == IN)
+                    atomicAdd(gb + o, f[j]);
+            }
+        }
+    } else {
+        if (tid == 0)
+            atomicExch(err, 1u);
+        if (mma_pending)
+            (void)tc_wait(bar, mma_parity);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(WG_TMEM_COLS)
+                     : "memory");
+    }
+}
+
 // Backward of the binary cross-entropy on the logits: dy, dH2 = dy w3 [H2 > 0]
 // and dH1 = (dH2 W2) [H1 > 0] (tensor cores; w2t is W2 transposed, [in][out]).
 __global__ void mlp_backward_kernel(long n, const float *__restrict__ logit, const float *__restrict__ label,
@@ -985,6 +1139,35 @@ cudaError_t weight_grads(long n, const float *dh1, const float *dh2, const float
         og = 1;
     out_grad_kernel<<<og, HID, 0, s>>>(n, dy, (const __nv_bfloat16 *)h2, grad + B2, grad + W3);
     (void)B3;
+    return cudaGetLastError();
+}
+
+cudaError_t weight_grads_tc(long n, const float *dh1, const float *dh2, const float *dy, const void *x, const void *h1,
+                            const void *h2, float *grad, unsigned *err, int num_sms, cudaStream_t s) {
+    const int W1 = HID * IN, B1 = W1 + HID, W2 = B1 + HID * HID, B2 = W2 + HID, W3 = B2 + HID;
+    if (n <= 0)
+        return cudaSuccess;
+    const long tiles = (n + TC_ROWS - 1) / TC_ROWS;
+    long grid = 2L * (num_sms > 0 ? num_sms : 1);
+    if (grid > tiles)
+        grid = tiles;
+    cudaError_t e = cudaFuncSetAttribute(weight_grad_tc_kernel<IN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)WgLayout<IN>::SMEM);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(weight_grad_tc_kernel<HID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)WgLayout<HID>::SMEM);
+    if (e != cudaSuccess)
+        return e;
+    weight_grad_tc_kernel<IN><<<(int)grid, 128, WgLayout<IN>::SMEM, s>>>(n, dh1, (const __nv_bfloat16 *)x, grad,
+                                                                         grad + W1, err);
+    weight_grad_tc_kernel<HID><<<(int)grid, 128, WgLayout<HID>::SMEM, s>>>(n, dh2, (const __nv_bfloat16 *)h1,
+                                                                           grad + B1, grad + W2, err);
+    int og = (int)((n + 255) / 256);
+    if (og > 8 * num_sms)
+        og = 8 * num_sms;
+    if (og < 1)
+        og = 1;
+    out_grad_kernel<<<og, HID, 0, s>>>(n, dy, (const __nv_bfloat16 *)h2, grad + B2, grad + W3);
     return cudaGetLastError();
 }
 

@@ -113,8 +113,9 @@ typedef struct {
 /* canon_enumerate_ksys runs level by level with host-sized launches (reading every
  * level's size back) instead of replaying its captured CUDA graph.  Same output. */
 #define CANON_OPT_NO_GRAPH 0x4u
-/* The MLP's forward pass and the hidden-layer gradient of its backward pass run on the
- * warp-level mma.sync path instead of tcgen05 (the two agree to FP32 rounding). */
+/* The MLP's GEMMs (forward, the hidden-layer gradient, the weight gradients) run on the
+ * warp-level mma.sync and FP32 paths instead of tcgen05 (the results agree to BF16
+ * rounding of the operands). */
 #define CANON_OPT_MLP_WARP_MMA 0x8u
 
 /* BIBD / incidence-system batch: n matrices of b columns (b <= 63), v rows each
