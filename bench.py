@@ -341,7 +341,12 @@ def integer_roofline(ctx, args, n, flags, variant, d_rows, d_can, d_aut, d_st, f
     nodes = ctx.d2h(np.zeros(n, np.uint64), d_nodes)
     ctx.free(d_nodes)
     ops = float(nodes.sum()) * B * INT_OPS_PER_NODE_COLUMN
-    if variant in (G.VARIANT_TWO_PASS, G.VARIANT_CONVERGED):
+    conv_names = {G.VARIANT_CONVERGED: "bibd_conv_kernel<35, 15> (lex-max pass, converged layout)",
+                  G.VARIANT_CONVERGED_D2: "bibd_conv_kernel<35, 15, 2> (lex-max pass, converged layout, "
+                                          "loads staged 2 ahead)",
+                  G.VARIANT_CONVERGED_D8: "bibd_conv_kernel<35, 15, 8> (lex-max pass, converged layout, "
+                                          "loads staged 8 ahead)"}
+    if variant == G.VARIANT_TWO_PASS or variant in conv_names:
         # the first pass alone: without witness and trials outputs only it is launched
         ms = []
         for _ in range(2):
@@ -349,8 +354,7 @@ def integer_roofline(ctx, args, n, flags, variant, d_rows, d_can, d_aut, d_st, f
             ctx.check_bibd_device(n, V, B, flags, d_rows, d_can, None, d_aut, d_st)
             ctx.stream_sync()
             ms.append(ctx.last_kernel_ms())
-        kname = ("bibd_conv_kernel<35, 15> (lex-max pass, converged layout)" if variant == G.VARIANT_CONVERGED
-                 else "bibd_max_kernel<35, 15> (lex-max pass)")
+        kname = conv_names.get(variant, "bibd_max_kernel<35, 15> (lex-max pass)")
     else:
         ms = list(times)
         kname = "the one-pass check kernel"

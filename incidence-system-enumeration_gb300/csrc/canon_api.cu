@@ -726,7 +726,9 @@ cudaError_t run_variant(canon_ctx *c, int variant, uint32_t n, uint32_t v, uint3
     const bool ref = flags & (CANON_SAVE_AUTS | CANON_REFERENCE_ORDER);
     const bool two = !ref && (variant < 0 ? (flags & (CANON_AUT_CANON | CANON_FULL_AUT)) != 0
                                           : (variant == canon::VARIANT_TWO_PASS ||
-                                             variant == canon::VARIANT_CONVERGED));
+                                             variant == canon::VARIANT_CONVERGED ||
+                                             variant == canon::VARIANT_CONVERGED_D2 ||
+                                             variant == canon::VARIANT_CONVERGED_D8));
     c->launches += two ? ((d_witness16 || d_trials) ? 2 : 1) : 1;
     return canon::launch_bibd_check_uniform(n, v, b, flags, d_rows, d_canonical, d_witness16, d_aut, d_status,
                                             d_trials, c->cfg.max_trials, c->d_ticket, c->num_sms, s, orders,
@@ -794,7 +796,8 @@ int canon_tune_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t f
     const bool verdict = flags & CANON_VERDICT_ONLY;
     const bool want_aut = flags & (CANON_AUT_CANON | CANON_FULL_AUT);
     constexpr int NV = canon::N_VARIANTS;
-    bool applies[NV] = {true, !ref, verdict && !ref && !want_aut, !ref};
+    const bool small = v <= 15 && b <= 35;     // the instance the staging-depth variants exist for
+    bool applies[NV] = {true, !ref, verdict && !ref && !want_aut, !ref, !ref && small, !ref && small};
     // outputs of every variant, compared with the one-pass variant's on the host
     struct Out {
         uint8_t *can = nullptr, *wit = nullptr, *st = nullptr;
@@ -815,7 +818,9 @@ int canon_tune_bibd(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, uint32_t f
     std::vector<uint8_t> can0(n), st0(n), wit0(verdict ? 0 : (size_t)n * 16), can1(n), st1(n),
         wit1(verdict ? 0 : (size_t)n * 16);
     std::vector<uint64_t> aut0((size_t)n * 2), aut1((size_t)n * 2);
-    float ms[NV] = {-1.f, -1.f, -1.f, -1.f};
+    float ms[NV];
+    for (int k = 0; k < NV; ++k)
+        ms[k] = -1.f;
     int best = -1;
     for (int k = 0; k < NV && e == cudaSuccess; ++k) {
         if (!applies[k])

@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(256) int_peak_kernel(uint32_t iters, uint32_t 
 // the b columns with the same trip count in every lane.  A thread that finishes its
 // matrix takes the next one inside the control steps, so the lanes keep evaluating
 // nodes together until the batch runs out.
-template <int BCAP, int VCAP>
+template <int BCAP, int VCAP, unsigned RDEPTH = 4>
 __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32_t v, uint32_t b, uint32_t flags,
                                                         const uint64_t *__restrict__ rows, uint8_t *canonical,
                                                         uint64_t *aut, uint8_t *status, uint64_t max_nodes,
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
         const bool full = b == BCAP;
         if (ref_lv >= 0) {
             if (full)
-                refine_uniform<BCAP>(sm, (unsigned)ref_lv, ref_x, b);
+                refine_uniform<BCAP, RDEPTH>(sm, (unsigned)ref_lv, ref_x, b);
             else
                 refine_uniform(sm, (unsigned)ref_lv, ref_x, b);
         }
@@ -736,8 +736,10 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
         return cudaSuccess;
     const int need = (int)((n + TPB - 1) / TPB);
     const bool ref_order = flags & (F_SAVE_AUTS | F_REFERENCE_ORDER);
+    const bool depth_variant = variant == VARIANT_CONVERGED_D2 || variant == VARIANT_CONVERGED_D8;
     const bool two = !ref_order && (variant < 0 ? (flags & (F_AUT_CANON | F_FULL_AUT)) != 0
-                                                : (variant == VARIANT_TWO_PASS || variant == VARIANT_CONVERGED));
+                                                : (variant == VARIANT_TWO_PASS || variant == VARIANT_CONVERGED ||
+                                                   depth_variant));
     // the converged layout of the lex-max pass by default; the original one only when
     // the autotuner asks for it by name
     const bool conv = variant != VARIANT_TWO_PASS;
@@ -749,7 +751,14 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
         CANON_TRY(cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s));
         // the smallest instance that holds the shape
         const int shape = (v <= 15 && b <= 35) ? 0 : (b <= 40 ? 1 : 2);
-        const void *kfn = conv ? (shape == 0   ? (const void *)bibd_conv_kernel<35, 15>
+        // the staging depth of the arrangement's loads (2 / 4 / 8 columns ahead): the
+        // autotuner's variants, instantiated for the 15 x 35 instance
+        const unsigned depth = (shape == 0 && variant == VARIANT_CONVERGED_D2)   ? 2u
+                               : (shape == 0 && variant == VARIANT_CONVERGED_D8) ? 8u
+                                                                                 : 4u;
+        const void *kfn = conv ? (shape == 0   ? (depth == 2   ? (const void *)bibd_conv_kernel<35, 15, 2>
+                                                  : depth == 8 ? (const void *)bibd_conv_kernel<35, 15, 8>
+                                                               : (const void *)bibd_conv_kernel<35, 15>)
                                   : shape == 1 ? (const void *)bibd_conv_kernel<40, 16>
                                                : (const void *)bibd_conv_kernel<64, 16>)
                                : (shape == 0   ? (const void *)bibd_max_kernel<35, 15>
@@ -760,9 +769,16 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
 #define CANON_PASS1(K, BC, VC, ...)                                                                             \
     K<BC, VC><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status, max_trials, tk, d_orders, \
                                    nullptr __VA_ARGS__)
+#define CANON_PASS1D(BC, VC, RA, D)                                                                                \
+    bibd_conv_kernel<BC, VC, D><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, d_canonical, d_aut, d_status, max_trials, \
+                                                     tk, d_orders, nullptr, RA)
         if (conv) {
             const uint64_t ra = restart_nodes();
-            if (shape == 0)
+            if (shape == 0 && depth == 2)
+                CANON_PASS1D(35, 15, ra, 2);
+            else if (shape == 0 && depth == 8)
+                CANON_PASS1D(35, 15, ra, 8);
+            else if (shape == 0)
                 CANON_PASS1(bibd_conv_kernel, 35, 15, , ra);
             else if (shape == 1)
                 CANON_PASS1(bibd_conv_kernel, 40, 16, , ra);
@@ -777,6 +793,7 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
                 CANON_PASS1(bibd_max_kernel, 64, 16);
         }
 #undef CANON_PASS1
+#undef CANON_PASS1D
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess)
             return e;

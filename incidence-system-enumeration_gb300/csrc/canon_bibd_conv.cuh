@@ -129,13 +129,13 @@ __device__ __forceinline__ int eval_node_planes(S sm, unsigned w, unsigned lv, u
 // the columns of level lv+1 after row x was taken at level lv: inside every orbit of
 // level lv, the columns with a 1 in row x first (one pass, a write pointer per orbit);
 // bt: the columns walked (columns past the matrix's own hold no 1 and never move)
-// With FB > 0 the column masks are loaded RD columns ahead of their turn: a swap at
+// With FB > 0 the column masks are loaded RD columns ahead of their turn (RD, the
+// shared-memory staging depth, is a dimension of the autotuner: 2, 4 or 8): a swap at
 // column p writes only positions w <= p, never a column still to come, so the early
 // loads read what the in-order pass would, and their latency overlaps the swaps instead
 // of following each one (the compiler cannot see that w <= p and would keep every load
 // behind the stores before it).
-constexpr unsigned RD = 4;
-template <unsigned FB = 0, typename S>
+template <unsigned FB = 0, unsigned RD = 4, typename S>
 __device__ __forceinline__ void refine_uniform(S sm, unsigned lv, unsigned x, unsigned bt) {
     const uint64_t starts = L_(lv);
     unsigned w = 0;

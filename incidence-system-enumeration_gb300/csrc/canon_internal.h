@@ -64,7 +64,15 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
 // check variants with identical outputs (canon_tune_bibd): one pass, two passes,
 // the search split by first row (verdict only), two passes with the first pass in
 // the converged layout (canon_bibd_conv.cuh)
-enum : int { VARIANT_SINGLE = 0, VARIANT_TWO_PASS = 1, VARIANT_SPLIT = 2, VARIANT_CONVERGED = 3, N_VARIANTS = 4 };
+enum : int {
+    VARIANT_SINGLE = 0,
+    VARIANT_TWO_PASS = 1,
+    VARIANT_SPLIT = 2,
+    VARIANT_CONVERGED = 3,
+    VARIANT_CONVERGED_D2 = 4,   // the converged pass staging its column loads 2 (8) columns ahead
+    VARIANT_CONVERGED_D8 = 5,
+    N_VARIANTS = 6
+};
 // one share of a lex-max search split by first row (bibd_split_kernel)
 struct SplitPart {
     uint64_t leaves;

@@ -119,11 +119,14 @@ DESIGN_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint
 
 
 class TuneResult(ctypes.Structure):
-    _fields_ = [("variant", ctypes.c_int), ("ms", ctypes.c_float * 4)]
+    _fields_ = [("variant", ctypes.c_int), ("ms", ctypes.c_float * 6)]
 
 
 VARIANT_SINGLE, VARIANT_TWO_PASS, VARIANT_SPLIT, VARIANT_CONVERGED = 0, 1, 2, 3
-VARIANT_NAMES = ["one pass", "two passes", "split by first row", "two passes, converged lex-max pass"]
+VARIANT_CONVERGED_D2, VARIANT_CONVERGED_D8 = 4, 5
+VARIANT_NAMES = ["one pass", "two passes", "split by first row", "two passes, converged lex-max pass",
+                 "two passes, converged lex-max pass, loads staged 2 ahead",
+                 "two passes, converged lex-max pass, loads staged 8 ahead"]
 
 
 class MlpWeights(ctypes.Structure):

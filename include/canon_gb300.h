@@ -225,16 +225,21 @@ int canon_check_bibd_device(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, 
  *                          first row) (CANON_VERDICT_ONLY without |Aut| flags);
  *   CANON_VARIANT_CONVERGED two passes, the lex-max pass laid out so that the
  *                          threads of a warp evaluate their nodes together (one
- *                          pass over all columns per node and thread).
+ *                          pass over all columns per node and thread), its column
+ *                          loads staged 4 columns ahead;
+ *   CANON_VARIANT_CONVERGED_D2 / _D8 the same with the loads staged 2 / 8 columns
+ *                          ahead (the shared-memory staging depth; 15 x 35 shapes).
  * ms[i]: the variant's device time, -1 when it does not apply, -2 when its
  * outputs differed (never chosen). */
 #define CANON_VARIANT_SINGLE    0
 #define CANON_VARIANT_TWO_PASS  1
 #define CANON_VARIANT_SPLIT     2
 #define CANON_VARIANT_CONVERGED 3
+#define CANON_VARIANT_CONVERGED_D2 4
+#define CANON_VARIANT_CONVERGED_D8 5
 typedef struct {
     int   variant;      /* the variant kept */
-    float ms[4];
+    float ms[6];
 } canon_tune_result;
 int canon_tune_bibd(canon_ctx *ctx, uint32_t n, uint32_t v, uint32_t b, uint32_t flags, const uint64_t *d_rows,
                     canon_tune_result *out);

@@ -46,9 +46,10 @@ def test_tuned_variant_keeps_outputs(flags):
     ctx.h2d(d_rows, rows)
     variant, ms = ctx.tune_bibd(n, 15, 35, flags, d_rows)
     assert ms[0] > 0 and ms[1] > 0 and ms[3] > 0        # one pass and both two-pass layouts apply
+    assert ms[4] > 0 and ms[5] > 0                       # the staging depths 2 and 8 (15 x 35)
     assert (ms[2] > 0) == bool(flags & G.VERDICT_ONLY)   # the split search only for verdicts
     assert -2.0 not in ms                                # every variant matched the one-pass outputs
-    assert variant == min((k for k in range(4) if ms[k] > 0), key=lambda k: ms[k])
+    assert variant == min((k for k in range(6) if ms[k] > 0), key=lambda k: ms[k])
     got, _ = run(ctx, rows, flags)
     ctx.close()
     assert np.array_equal(got["canonical"], ref["canonical"]) and not got["status"].any()
