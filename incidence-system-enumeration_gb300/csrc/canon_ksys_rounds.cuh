@@ -19,9 +19,13 @@ namespace canon {
 // (k-Factorization/TripleSys/Source/TripleSys.cpp:487-775) restricted to the matchings
 // an orderly enumeration keeps; the children of a parent come in the order of the
 // depth-first walk (partners in increasing order).  dst == nullptr: count only.
+// second >= 0: only the rounds whose second pair (the lowest player after 0 and d+1)
+// takes partner `second` -- the walk of one parent split into independent parts by that
+// partner, which in increasing order give the parent's children in its order.
 constexpr int KS_MAXNP = 12;
 
-__host__ __device__ inline uint32_t ksys_children(int np, const uint8_t *parent, int d, uint8_t *dst) {
+__host__ __device__ inline uint32_t ksys_children(int np, const uint8_t *parent, int d, uint8_t *dst,
+                                                  int second = -1) {
     uint16_t used[KS_MAXNP];
     for (int a = 0; a < np; ++a)
         used[a] = 0;
@@ -49,6 +53,8 @@ __host__ __device__ inline uint32_t ksys_children(int np, const uint8_t *parent,
             if ((taken >> c) & 1u || ((used[a] >> c) & 1u))
                 continue;
             if (a == 0 && c != d + 1)
+                continue;
+            if (depth == 1 && second >= 0 && c != second)
                 continue;
             break;
         }

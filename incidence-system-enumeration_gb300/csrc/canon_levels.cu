@@ -422,28 +422,35 @@ void parallel_ranges(uint64_t n, F fn) {
 }
 
 // ---- k-system rounds on the device ----------------------------------------
-// d_npar (optional): the parent count in device memory (a captured level)
-__global__ void ksys_count_kernel(int np, const uint8_t *parents, uint32_t n_par, int d, uint32_t *counts,
-                                  const uint64_t *d_npar = nullptr) {
-    if (d_npar)
-        n_par = (uint32_t)*d_npar;
+// The walk of a level is split into units: unit u is parent u / np with the second pair's
+// partner u % np (ksys_children), so a parent's children are counted and written by np
+// threads, in its order.  d_nunits (optional): the unit count in device memory (a captured
+// level).
+__global__ void ksys_count_kernel(int np, const uint8_t *parents, uint32_t n_units, int d, uint32_t *counts,
+                                  const uint64_t *d_nunits = nullptr) {
+    if (d_nunits)
+        n_units = (uint32_t)*d_nunits;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n_par; p += stride)
-        counts[p] = canon::ksys_children(np, parents + (size_t)p * d * np, d, nullptr);
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n_units; u += stride) {
+        const uint32_t p = u / (uint32_t)np, sec = u % (uint32_t)np;
+        counts[u] = canon::ksys_children(np, parents + (size_t)p * d * np, d, nullptr, (int)sec);
+    }
 }
 
-// the children of parents [p0, p1) at offsets[p] - offsets[p0], and one work item each
-__global__ void ksys_emit_kernel(int np, const uint8_t *parents, uint32_t p0, uint32_t p1, int d,
+// the children of units [u0, u1) at offsets[u] - offsets[u0], and one work item each
+__global__ void ksys_emit_kernel(int np, const uint8_t *parents, uint32_t u0, uint32_t u1, int d,
                                  const uint64_t *offsets, uint8_t *out, canon::Item *items,
-                                 const uint64_t *d_npar = nullptr) {
-    if (d_npar)
-        p1 = (uint32_t)*d_npar;
-    const uint64_t base = offsets[p0];
+                                 const uint64_t *d_nunits = nullptr) {
+    if (d_nunits)
+        u1 = (uint32_t)*d_nunits;
+    const uint64_t base = offsets[u0];
     const uint32_t m = (uint32_t)d + 1;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x; p < p1; p += stride) {
-        const uint64_t o = offsets[p] - base;
-        const uint32_t cnt = canon::ksys_children(np, parents + (size_t)p * d * np, d, out + o * m * np);
+    for (uint32_t u = u0 + blockIdx.x * blockDim.x + threadIdx.x; u < u1; u += stride) {
+        const uint32_t p = u / (uint32_t)np, sec = u % (uint32_t)np;
+        const uint64_t o = offsets[u] - base;
+        const uint32_t cnt =
+            canon::ksys_children(np, parents + (size_t)p * d * np, d, out + o * m * np, (int)sec);
         for (uint32_t j = 0; j < cnt; ++j) {
             canon::Item it{};
             it.data_off = (uint32_t)((o + j) * m * np);
@@ -496,6 +503,7 @@ __global__ void ksys_compact_kernel(uint64_t n_cand, uint32_t bytes, const uint8
 // enumerates again level by level with buffers that grow.
 struct KsCtl {
     uint64_t n_par;                       // parents of the level in progress
+    uint64_t n_units;                     // their walk units (parents x np)
     uint64_t n_cand;                      // its candidates
     uint64_t level_checks[16];
     unsigned long long stamp[16][3];      // globaltimer: level start, candidates written, checked
@@ -520,19 +528,21 @@ __global__ void ksg_start_kernel(KsCtl *ctl, uint8_t *lev, int np) {
         ctl->n_par = 1;
 }
 
-__global__ void ksg_begin_kernel(KsCtl *ctl, int level) {
+__global__ void ksg_begin_kernel(KsCtl *ctl, int level, int np) {
     ctl->stamp[level][0] = global_ns();
+    ctl->n_units = ctl->n_par * (uint64_t)np;
     if (ctl->n_par)
         ++ctl->levels;
 }
 
-// the level's candidates: offs[n_par]; beyond the buffers, the run stops here
+// the level's candidates: offs[n_units]; beyond the buffers, the run stops here
 __global__ void ksg_cand_kernel(KsCtl *ctl, const uint64_t *offs, uint64_t cap, int level) {
-    uint64_t n = offs[ctl->n_par];
+    uint64_t n = offs[ctl->n_units];
     if (n > cap) {
         ctl->overflow = 1u;
         n = 0;
         ctl->n_par = 0;
+        ctl->n_units = 0;
     }
     ctl->n_cand = n;
     ctl->level_checks[level] = n;
@@ -584,13 +594,13 @@ cudaError_t ksys_graph_build(canon_ctx *c, KsysGraph &g, uint32_t np, uint64_t c
     if (e == cudaSuccess) e = g.rtc.ensure(cap);
     if (e == cudaSuccess) e = g.wit.ensure(cap * 16);
     if (e == cudaSuccess) e = g.len_aut.ensure(cap);
-    if (e == cudaSuccess) e = g.doffs.ensure(cap + 1);
+    if (e == cudaSuccess) e = g.doffs.ensure(cap * np + 1);
     if (e == cudaSuccess) e = g.coffs.ensure(cap + 1);
-    if (e == cudaSuccess) e = g.sums.ensure(cap / SCAN_TILE + 2);
+    if (e == cudaSuccess) e = g.sums.ensure(cap * np / SCAN_TILE + 2);
     if (e == cudaSuccess) e = g.aut.ensure(cap * 2);
     if (e == cudaSuccess) e = g.aut_out.ensure(cap * 2);
     if (e == cudaSuccess) e = g.trials.ensure(cap);
-    if (e == cudaSuccess) e = g.counts.ensure(cap);
+    if (e == cudaSuccess) e = g.counts.ensure(cap * np);
     if (e == cudaSuccess) e = g.pidx.ensure(cap);
     if (e == cudaSuccess) e = g.n_auts.ensure(cap);
     if (e == cudaSuccess) e = g.items.ensure(cap);
@@ -599,7 +609,7 @@ cudaError_t ksys_graph_build(canon_ctx *c, KsysGraph &g, uint32_t np, uint64_t c
     if (e != cudaSuccess)
         return e;
     const int sms = c->num_sms > 0 ? c->num_sms : 1;
-    int gg = (int)((cap + 127) / 128);
+    int gg = (int)((cap * np + 127) / 128);
     if (gg > 4 * sms)
         gg = 4 * sms;
     int gc = (int)((cap + 255) / 256);
@@ -623,15 +633,15 @@ cudaError_t ksys_graph_build(canon_ctx *c, KsysGraph &g, uint32_t np, uint64_t c
         const bool complete = m == rounds;
         const uint8_t *par = g.lev[n & 1].p;
         uint8_t *dst = g.lev[m & 1].p;
-        ksg_begin_kernel<<<1, 1, 0, s>>>(ctl, (int)m - 1);
-        ksys_count_kernel<<<gg, 128, 0, s>>>((int)np, par, 0, (int)n, g.counts.p, &ctl->n_par);
+        ksg_begin_kernel<<<1, 1, 0, s>>>(ctl, (int)m - 1, (int)np);
+        ksys_count_kernel<<<gg, 128, 0, s>>>((int)np, par, 0, (int)n, g.counts.p, &ctl->n_units);
         kernels += 2;
-        e = exclusive_scan_dev(g.counts.p, &ctl->n_par, cap, g.doffs.p, g.sums.p, s, &kernels);
+        e = exclusive_scan_dev(g.counts.p, &ctl->n_units, cap * np, g.doffs.p, g.sums.p, s, &kernels);
         if (e != cudaSuccess)
             break;
         ksg_cand_kernel<<<1, 1, 0, s>>>(ctl, g.doffs.p, cap, (int)m - 1);
         ksys_emit_kernel<<<gg, 128, 0, s>>>((int)np, par, 0, 0, (int)n, g.doffs.p, g.cand.p, g.items.p,
-                                             &ctl->n_par);
+                                             &ctl->n_units);
         ksg_stamp_kernel<<<1, 1, 0, s>>>(ctl, (int)m - 1, 1);
         kernels += 3;
         canon::Outputs o{};
@@ -1166,22 +1176,23 @@ extern "C" int canon_enumerate_ksys(canon_ctx *c, uint32_t np, canon_design_cb c
     while (n < rounds && n_par) {
         const uint32_t m = n + 1;
         const bool complete = m == rounds;
-        // 1: children per parent and their offsets (on the GPU)
-        e = dcounts.ensure(n_par);
+        // 1: children per walk unit (parent x second-pair partner) and their offsets (on the GPU)
+        const uint64_t n_units = n_par * np;
+        e = dcounts.ensure(n_units);
         if (e == cudaSuccess)
-            e = doffs.ensure(n_par + 1);
+            e = doffs.ensure(n_units + 1);
         if (e != cudaSuccess)
             return done(CANON_ENOMEM, "level buffers", e);
-        int g = (int)((n_par + 127) / 128);
+        int g = (int)((n_units + 127) / 128);
         if (g > grid_cap)
             g = grid_cap;
         cudaEventRecord(g0, s);
-        ksys_count_kernel<<<g, 128, 0, s>>>((int)np, lev.p, (uint32_t)n_par, (int)n, dcounts.p);
+        ksys_count_kernel<<<g, 128, 0, s>>>((int)np, lev.p, (uint32_t)n_units, (int)n, dcounts.p);
         e = cudaGetLastError();
         if (e == cudaSuccess)
-            e = exclusive_scan(dcounts.p, n_par, doffs.p, sums, s);
+            e = exclusive_scan(dcounts.p, n_units, doffs.p, sums, s);
         cudaEventRecord(g1, s);
-        std::vector<uint64_t> offs(n_par + 1);
+        std::vector<uint64_t> offs(n_units + 1);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(offs.data(), doffs.p, offs.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, s);
         if (e == cudaSuccess)
@@ -1192,7 +1203,7 @@ extern "C" int canon_enumerate_ksys(canon_ctx *c, uint32_t np, canon_design_cb c
         cudaEventElapsedTime(&gms, g0, g1);
         st.gen_seconds += gms * 1e-3;
         c->launches += 4;
-        const uint64_t n_cand = offs[n_par];
+        const uint64_t n_cand = offs[n_units];
         const size_t bytes = (size_t)m * np;
         e = next.ensure((n_cand ? n_cand : 1) * bytes);
         if (e == cudaSuccess && complete)
@@ -1200,9 +1211,10 @@ extern "C" int canon_enumerate_ksys(canon_ctx *c, uint32_t np, canon_design_cb c
         if (e != cudaSuccess)
             return done(CANON_ENOMEM, "next level", e);
         uint64_t n_next = 0, p0 = 0;
-        while (p0 < n_par) {
+        // slices of walk units whose children fit SLICE_CAP
+        while (p0 < n_units) {
             uint64_t p1 = p0 + 1;
-            while (p1 < n_par && offs[p1 + 1] - offs[p0] <= SLICE_CAP)
+            while (p1 < n_units && offs[p1 + 1] - offs[p0] <= SLICE_CAP)
                 ++p1;
             const uint64_t ns = offs[p1] - offs[p0];
             const size_t cap = ns ? ns : 1;

@@ -5,3 +5,7 @@
 extern "C" uint32_t emu_ksys_children(int np, const uint8_t *parent, int d, uint8_t *dst) {
     return canon::ksys_children(np, parent, d, dst);
 }
+
+extern "C" uint32_t emu_ksys_children_part(int np, const uint8_t *parent, int d, uint8_t *dst, int second) {
+    return canon::ksys_children(np, parent, d, dst, second);
+}

@@ -86,3 +86,26 @@ def test_level_by_level_enumeration_matches_the_oracle_on_k8(gen):
     ref, _ = oracle.ksys_enumerate(8)
     assert len(level) == len(ref) == 6
     assert sorted(M.tobytes() for M in level) == sorted(np.asarray(M, np.uint8).tobytes() for M, _ in ref)
+
+
+def test_children_split_by_the_second_pair_concatenate_to_the_whole(gen):
+    """The device walks a parent in parts, one per partner of the second pair; taken in
+    increasing partner order the parts are the parent's children in their order."""
+    gen.emu_ksys_children_part.restype = ctypes.c_uint32
+    gen.emu_ksys_children_part.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_int]
+    for np_ in (6, 8, 10):
+        found, _ = oracle.ksys_enumerate(np_) if np_ < 10 else (cases.load_k10(), None)
+        mats = [R for R, _ in found]
+        for R in mats[:: max(1, len(mats) // 12)]:
+            for d in range(1, np_ - 1):
+                parent = np.ascontiguousarray(R[:d], np.uint8)
+                whole = children(gen, np_, parent)
+                parts = []
+                for s in range(np_):
+                    cnt = gen.emu_ksys_children_part(np_, parent.ctypes.data, d, None, s)
+                    out = np.zeros((cnt, d + 1, np_), np.uint8)
+                    assert gen.emu_ksys_children_part(np_, parent.ctypes.data, d, out.ctypes.data, s) == cnt
+                    parts.append(out)
+                joined = np.concatenate(parts) if parts else whole[:0]
+                assert np.array_equal(joined, whole), (np_, d)
