@@ -242,6 +242,10 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
                     finish(ST_BADINPUT);
                     continue;
                 }
+                // columns past the matrix's own are empty: they join its last orbit and change
+                // neither a count nor a comparison
+                for (unsigned c2 = b; c2 < (unsigned)BCAP; ++c2)
+                    CM_(c2) = 0;
                 st.w = conv_row_weight(sm, v);
                 eval = true;        // the root: no arrangement step
                 break;
@@ -258,7 +262,9 @@ __global__ void __launch_bounds__(TPB) bibd_conv_kernel(uint32_t n_items, uint32
             continue;
         // the node step: every lane with a node runs the same b-column passes (unrolled
         // when the batch's b is the instance's column capacity)
-        const bool full = b == BCAP;
+        // the unrolled node step over the instance's BCAP columns when the matrix fills at
+        // least three quarters of them (the rest are empty), else a loop over its b columns
+        const bool full = (BCAP - b) * 4 <= (unsigned)BCAP;
         if (ref_lv >= 0) {
             if (full)
                 refine_uniform<BCAP, RDEPTH>(sm, (unsigned)ref_lv, ref_x, b);
@@ -749,14 +755,17 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
         // single pass below rejects most non-canonical matrices in a few trials
         // of the reference order and runs the lex-max search only for the rest.)
         CANON_TRY(cudaMemsetAsync(tk, 0, 2 * sizeof(unsigned), s));
-        // the smallest instance that holds the shape
+        // the smallest instance that holds the shape (the converged pass also has one of 24
+        // columns)
         const int shape = (v <= 15 && b <= 35) ? 0 : (b <= 40 ? 1 : 2);
+        const bool narrow = conv && b <= 24;
         // the staging depth of the arrangement's loads (2 / 4 / 8 columns ahead): the
         // autotuner's variants, instantiated for the 15 x 35 instance
         const unsigned depth = (shape == 0 && variant == VARIANT_CONVERGED_D2)   ? 2u
                                : (shape == 0 && variant == VARIANT_CONVERGED_D8) ? 8u
                                                                                  : 4u;
-        const void *kfn = conv ? (shape == 0   ? (depth == 2   ? (const void *)bibd_conv_kernel<35, 15, 2>
+        const void *kfn = narrow ? (const void *)bibd_conv_kernel<24, 16>
+                          : conv ? (shape == 0   ? (depth == 2   ? (const void *)bibd_conv_kernel<35, 15, 2>
                                                   : depth == 8 ? (const void *)bibd_conv_kernel<35, 15, 8>
                                                                : (const void *)bibd_conv_kernel<35, 15>)
                                   : shape == 1 ? (const void *)bibd_conv_kernel<40, 16>
@@ -774,7 +783,9 @@ cudaError_t launch_bibd_check_uniform(uint32_t n, uint32_t v, uint32_t b, uint32
                                                      tk, d_orders, nullptr, RA)
         if (conv) {
             const uint64_t ra = restart_nodes();
-            if (shape == 0 && depth == 2)
+            if (narrow)
+                CANON_PASS1(bibd_conv_kernel, 24, 16, , ra);
+            else if (shape == 0 && depth == 2)
                 CANON_PASS1D(35, 15, ra, 2);
             else if (shape == 0 && depth == 8)
                 CANON_PASS1D(35, 15, ra, 8);
@@ -829,7 +840,9 @@ cudaError_t launch_bibd_lexmax_nodes(uint32_t n, uint32_t v, uint32_t b, uint32_
         bibd_conv_kernel<BC, VC><<<grid, TPB, 0, s>>>(n, v, b, flags, d_rows, nullptr, nullptr, nullptr, max_nodes, \
                                                       tk, d_orders, d_nodes, ra);                              \
     } while (0)
-    if (v <= 15 && b <= 35)
+    if (b <= 24)
+        CANON_NODES(24, 16);
+    else if (v <= 15 && b <= 35)
         CANON_NODES(35, 15);
     else if (b <= 40)
         CANON_NODES(40, 16);

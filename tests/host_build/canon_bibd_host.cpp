@@ -102,7 +102,7 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
     SmemMax sm{s_rows, s_lvl, nullptr, s_cm, s_vd};
     if (!load_rows(sm, rows, n, b, F_RAW))
         return -1;
-    for (unsigned c = b; c < bt; ++c)
+    for (unsigned c = b; c < 64; ++c)
         CM_(c) = 0;
     // mode: 0 climb, 1 restart after RESTART_AFTER nodes (the kernels' rule), 2 restart
     // whenever the bound is complete and greater than the searched matrix
@@ -114,11 +114,17 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
     st.verdict_only = mode == 3;
     int ref_lv = -1;
     unsigned ref_x = 0;
-    // the kernels' unrolled node step where b is the instance's column capacity
-    const unsigned fb = (b == bt && (b == 35 || b == 40 || b == 64)) ? b : 0;
+    // the kernels' unrolled node step: the smallest instance of 24, 35, 40 or 64 columns
+    // that holds the columns walked, when they fill at least three quarters of it (the
+    // rest are empty columns); else the loop over bt columns
+    unsigned fb = bt <= 24 ? 24 : bt <= 35 ? 35 : bt <= 40 ? 40 : 64;
+    if ((fb - bt) * 4 > fb)
+        fb = 0;
     for (;;) {
         if (ref_lv >= 0) {
-            if (fb == 35)
+            if (fb == 24)
+                refine_uniform<24>(sm, (unsigned)ref_lv, ref_x, bt);
+            else if (fb == 35)
                 refine_uniform<35>(sm, (unsigned)ref_lv, ref_x, bt);
             else if (fb == 40)
                 refine_uniform<40>(sm, (unsigned)ref_lv, ref_x, bt);
@@ -133,7 +139,8 @@ extern "C" int emu_conv_search_bt(const uint64_t *rows, unsigned n, unsigned b, 
         uint64_t arr = 0;
         const bool hb = st.i < st.valid;
         const uint64_t bnd = hb ? R_(st.i) : 0ull;
-        const int state = fb == 35   ? eval_node_planes<35>(sm, st.w, st.i, b, bt, tied, arr, hb, bnd)
+        const int state = fb == 24   ? eval_node_planes<24>(sm, st.w, st.i, b, bt, tied, arr, hb, bnd)
+                          : fb == 35 ? eval_node_planes<35>(sm, st.w, st.i, b, bt, tied, arr, hb, bnd)
                           : fb == 40 ? eval_node_planes<40>(sm, st.w, st.i, b, bt, tied, arr, hb, bnd)
                           : fb == 64 ? eval_node_planes<64>(sm, st.w, st.i, b, bt, tied, arr, hb, bnd)
                                      : eval_node_planes(sm, st.w, st.i, b, bt, tied, arr, hb, bnd);
