@@ -139,7 +139,8 @@ def bibd_canonize(M):
     return M, res.aut_lo | (res.aut_hi << 64), calls
 
 
-def ksys_test(R, full_aut=False, aut_cap=0):
+def ksys_test(R, full_aut=False, aut_cap=0, g=2):
+    """cnvCheckNew() of the rounds R (rows of np players in groups of g)."""
     R = np.ascontiguousarray(R, dtype=np.uint8)
     nr, np_ = R.shape
     res = KsysResult()
@@ -148,7 +149,7 @@ def ksys_test(R, full_aut=False, aut_cap=0):
         arena = np.zeros(aut_cap * np_, np.uint8)
         res.aut_arena = _u8p(arena)
         res.aut_cap = aut_cap
-    rc = lib().or_ksys_test(_u8p(R), nr, np_, 2, int(full_aut), ctypes.byref(res))
+    rc = lib().or_ksys_test(_u8p(R), nr, np_, g, int(full_aut), ctypes.byref(res))
     if rc < 0:
         raise ValueError("oracle rejected input")
     out = dict(canonical=bool(res.canonical), player_index=res.player_index, n_aut=res.n_aut,

@@ -20,9 +20,14 @@ def load_sts15():
     return out
 
 
-def load_k10():
+def load_kts15():
+    """The 7 canonical Kirkman triple systems on 15 points (rounds of 5 groups of 3)."""
+    return load_k10("kts15_canonical.txt")
+
+
+def load_k10(name="k10_canonical.txt"):
     out = []
-    with open(os.path.join(GOLDEN, "k10_canonical.txt")) as f:
+    with open(os.path.join(GOLDEN, name)) as f:
         for line in f:
             if line.startswith("#"):
                 continue
@@ -43,31 +48,31 @@ def bibd_designs(v, b, r, k, lam):
     return found
 
 
-def ksys_sorted_form(R):
-    """Bring rounds (pairs) to the reference's result() form: pairs ascending,
-    ordered by first player, rounds ordered by their second entry."""
+def ksys_sorted_form(R, g=2):
+    """Bring rounds to the reference's result() form: the players of every group
+    ascending, groups ordered by their first player, rounds ordered by their second
+    entry."""
     out = []
     for row in R:
-        pairs = sorted(tuple(sorted((int(row[i]), int(row[i + 1])))) for i in range(0, len(row), 2))
-        out.append([x for p in pairs for x in p])
+        groups = sorted(tuple(sorted(int(row[i + j]) for j in range(g))) for i in range(0, len(row), g))
+        out.append([x for grp in groups for x in grp])
     out.sort(key=lambda r: r[1])
     return np.array(out, np.uint8)
 
 
-def ksys_relabel_random(R, rng):
+def ksys_relabel_random(R, rng, g=2):
     """Random relabeling of a complete/partial k-system that maps a random round onto
-    round 0 = (0 1)(2 3)..., then the sorted form."""
+    round 0 = (0 1 ..)(g ..)..., then the sorted form."""
     nr, n = R.shape
     d = int(rng.integers(nr))
-    pairs = [(int(R[d][i]), int(R[d][i + 1])) for i in range(0, n, 2)]
-    order = rng.permutation(len(pairs))
+    groups = [[int(R[d][i + j]) for j in range(g)] for i in range(0, n, g)]
+    order = rng.permutation(len(groups))
     lab = np.zeros(n, np.int64)
     for new_g, gi in enumerate(order):
-        a, b = pairs[gi]
-        if rng.integers(2):
-            a, b = b, a
-        lab[a], lab[b] = 2 * new_g, 2 * new_g + 1
-    return ksys_sorted_form(lab[R])
+        members = [groups[gi][k] for k in rng.permutation(g)]
+        for k, a in enumerate(members):
+            lab[a] = g * new_g + k
+    return ksys_sorted_form(lab[R], g)
 
 
 def load_result_tables():

@@ -14,6 +14,9 @@ reference tree; the GPU machine never runs this).
                         b <= 63, and for files in the current layout the exact
                         text from the BIBD( line to the "fully constructed" line
   k10_results_table.txt the |Aut(M)| x cycles table of K_Results.txt for K10
+  kts15_canonical.txt   the 7 canonical Kirkman triple systems on 15 points (groups of
+                        3, 7 rounds) with |Aut(M)|, parsed from
+                        k-Factorization/Results/Complete_graphs/15/15x7x3/K_OrderedMatrices.txt
 
 Usage: python tests/golden/make_fixtures.py [REFERENCE_ROOT]
 """
@@ -47,16 +50,17 @@ def parse_bibd_histogram(path):
     return hist
 
 
-def parse_k10(path):
+def parse_k10(path, nrows=9):
+    """(|Aut(M)|, rounds) of every matrix of a K_OrderedMatrices.txt file with nrows rounds."""
     txt = open(path, encoding="latin-1").read().splitlines()
     out = []
     i = 0
     while i < len(txt):
         m = re.match(r"\s*(\d+): \|Aut\(M\)\| =\s*(\d+)", txt[i])
         if m:
-            rows = [txt[i + j].strip().strip('"').split() for j in range(1, 10)]
+            rows = [txt[i + j].strip().strip('"').split() for j in range(1, nrows + 1)]
             out.append((int(m.group(2)), [" ".join(r) for r in rows]))
-            i += 10
+            i += nrows + 1
         else:
             i += 1
     return out
@@ -122,6 +126,15 @@ def main():
     with open(os.path.join(HERE, "k10_canonical.txt"), "w") as f:
         f.write("# 396 canonical 1-factorizations of K10: |Aut| then 9 rounds of 10 players\n")
         for aut, rows in k10:
+            f.write("%d %s\n" % (aut, " | ".join(rows)))
+
+    kts = parse_k10(os.path.join(ref, "k-Factorization", "Results", "Complete_graphs", "15",
+                                 "15x7x3", "K_OrderedMatrices.txt"), nrows=7)
+    assert len(kts) == 7
+    with open(os.path.join(HERE, "kts15_canonical.txt"), "w") as f:
+        f.write("# 7 canonical Kirkman triple systems on 15 points: |Aut| then 7 rounds of 15 players "
+                "(groups of 3)\n")
+        for aut, rows in kts:
             f.write("%d %s\n" % (aut, " | ".join(rows)))
 
     with open(os.path.join(HERE, "bibd_result_tables.json"), "w") as f:

@@ -77,3 +77,26 @@ def test_relabelled_k10_is_rejected_unless_equal():
         X = cases.ksys_relabel_random(R, rng)
         res = oracle.ksys_test(X)
         assert res["canonical"] == (X.tobytes() in canon)
+
+
+def test_kirkman_golden_matrices_are_canonical_with_reference_aut():
+    """The oracle's cnvCheckNew() restatement with groups of 3 (the general path: relabel,
+    sort inside the groups, groups by first player, rounds by second entry) on the 7
+    Kirkman triple systems of k-Factorization/Results/Complete_graphs/15/15x7x3: each is
+    canonical with the reference's |Aut(M)|, after trying all 5! x 3!^5 x 7 - 1
+    relabelings; relabelled copies are rejected."""
+    import concurrent.futures as cf
+    kts = cases.load_kts15()
+    assert sorted(a for _, a in kts) == [12, 12, 21, 24, 24, 168, 168]
+    with cf.ThreadPoolExecutor(max(1, min(7, os.cpu_count() or 1))) as ex:
+        outs = list(ex.map(lambda R: oracle.ksys_test(R, g=3), [R for R, _ in kts]))
+    for (R, aut), o in zip(kts, outs):
+        assert o["canonical"] and o["n_aut"] == aut
+        assert o["candidates"] == 120 * 6 ** 5 * 7 - 1
+    rng = np.random.default_rng(15)
+    rejected = 0
+    for R, _ in kts:
+        X = cases.ksys_relabel_random(R, rng, g=3)
+        if not np.array_equal(X, R):
+            rejected += not oracle.ksys_test(X, g=3)["canonical"]
+    assert rejected >= 5
