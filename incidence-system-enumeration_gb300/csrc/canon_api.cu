@@ -341,6 +341,8 @@ int canon_submit_bibd(canon_ctx *c, const canon_bibd_batch *bt) {
         return fail(c, CANON_EINVAL, "bibd batch: need rows, 1 <= v <= 16, 1 <= b <= 63");
     if (bt->flags & ~0x7Fu)
         return fail(c, CANON_EINVAL, "bibd batch: unknown flags");
+    if (c->q_ks_groups)
+        return fail(c, CANON_EINVAL, "groups of 3 or 4 are queued: canon_sync them before other batches");
     const uint32_t total = c->n_bitems + c->n_kitems;
     if ((uint64_t)total + bt->n > c->cfg.max_items)
         return fail(c, CANON_ENOMEM, "item capacity exceeded (canon_cfg.max_items)");
@@ -399,16 +401,8 @@ int canon_submit_bibd(canon_ctx *c, const canon_bibd_batch *bt) {
     return CANON_OK;
 }
 
-int canon_submit_ksys(canon_ctx *c, const canon_ksys_batch *bt) {
-    if (!c || !bt)
-        return fail(c, CANON_EINVAL, "null argument");
-    if (!bt->n)
-        return CANON_OK;
-    if (!bt->data || bt->np < 4 || bt->np > canon::KS_NPMAX || (bt->np & 1u) || bt->rounds < 1 ||
-        bt->rounds >= bt->np)
-        return fail(c, CANON_EINVAL, "ksys batch: need data, even 4 <= np <= 12, 1 <= rounds < np");
-    if (bt->flags & ~0xFu)
-        return fail(c, CANON_EINVAL, "ksys batch: unknown flags");
+// queues a checked k-system batch with groups of g (Item::pad)
+static int submit_ksys_items(canon_ctx *c, const canon_ksys_batch *bt, uint32_t g) {
     const uint32_t total = c->n_bitems + c->n_kitems;
     const uint64_t bytes = (uint64_t)bt->n * bt->rounds * bt->np;
     if ((uint64_t)total + bt->n > c->cfg.max_items)
@@ -430,6 +424,7 @@ int canon_submit_ksys(canon_ctx *c, const canon_ksys_batch *bt) {
             it.ncols = (uint8_t)bt->np;
             it.flags = (uint8_t)bt->flags;
             it.out_idx = total + (uint32_t)i;
+            it.pad = g;
             c->h_kitems[c->n_kitems + i] = it;
         }
         if (!ok)
@@ -455,10 +450,52 @@ int canon_submit_ksys(canon_ctx *c, const canon_ksys_batch *bt) {
             mr = std::max<uint32_t>(mr, bt->nrows[i]);
     }
     c->q_ks_nr = std::max(c->q_ks_nr, mr);
+    if (g > 2) {
+        c->q_ks_groups = true;
+        c->q_ks_total = std::max(c->q_ks_total, canon::kgen_candidates(bt->np, g, mr));
+    }
     c->n_bytes += (uint32_t)bytes;
     c->n_kitems += bt->n;
     c->item_kind.insert(c->item_kind.end(), bt->n, canon::KIND_KSYS);
     return CANON_OK;
+}
+
+int canon_submit_ksys(canon_ctx *c, const canon_ksys_batch *bt) {
+    if (!c || !bt)
+        return fail(c, CANON_EINVAL, "null argument");
+    if (!bt->n)
+        return CANON_OK;
+    if (!bt->data || bt->np < 4 || bt->np > canon::KS_NPMAX || (bt->np & 1u) || bt->rounds < 1 ||
+        bt->rounds >= bt->np)
+        return fail(c, CANON_EINVAL, "ksys batch: need data, even 4 <= np <= 12, 1 <= rounds < np");
+    if (bt->flags & ~0xFu)
+        return fail(c, CANON_EINVAL, "ksys batch: unknown flags");
+    if (c->q_ks_groups)
+        return fail(c, CANON_EINVAL, "groups of 3 or 4 are queued: canon_sync them before other batches");
+    return submit_ksys_items(c, bt, 2);
+}
+
+int canon_submit_ksys_groups(canon_ctx *c, const canon_ksys_batch *bt, uint32_t group_size) {
+    if (!c || !bt)
+        return fail(c, CANON_EINVAL, "null argument");
+    if (group_size == 2)
+        return canon_submit_ksys(c, bt);
+    if (group_size != 3 && group_size != 4)
+        return fail(c, CANON_EINVAL, "ksys batch: group size 2, 3 or 4");
+    if (!bt->n)
+        return CANON_OK;
+    if (!bt->data || bt->np > 16 || bt->np % group_size || bt->np / group_size < 2 || bt->rounds < 1 ||
+        bt->rounds >= bt->np)
+        return fail(c, CANON_EINVAL,
+                    "ksys batch: need data, np <= 16 a multiple of the group size (2 groups at least), "
+                    "1 <= rounds < np");
+    if (bt->flags & CANON_SAVE_AUTS)
+        return fail(c, CANON_EINVAL, "ksys batch: CANON_SAVE_AUTS is not available for groups of 3 or 4");
+    if (bt->flags & ~0xFu)
+        return fail(c, CANON_EINVAL, "ksys batch: unknown flags");
+    if (c->n_bitems || (c->n_kitems && !c->q_ks_groups))
+        return fail(c, CANON_EINVAL, "groups of 3 or 4 are checked in a queue of their own: canon_sync first");
+    return submit_ksys_items(c, bt, group_size);
 }
 
 int canon_sync(canon_ctx *c, canon_results *r) {
@@ -509,7 +546,9 @@ int canon_sync(canon_ctx *c, canon_results *r) {
             c->launches += two_pass ? 2 : 1;
         } else if (c->n_kitems) {
             const uint32_t seg =
-                c->q_want_auts ? 0u : canon::ksys_segment(c, c->n_kitems, c->q_ks_np, c->q_ks_nr);
+                c->q_ks_groups ? canon::kgen_segment(c, c->n_kitems, c->q_ks_total)
+                : c->q_want_auts ? 0u
+                                 : canon::ksys_segment(c, c->n_kitems, c->q_ks_np, c->q_ks_nr);
             if (seg) {
                 if (c->kseg_cap < (size_t)c->n_kitems + 1) {
                     cudaFree(c->d_kseg);
@@ -520,9 +559,12 @@ int canon_sync(canon_ctx *c, canon_results *r) {
                         return cuda_fail(c, e, "k-system segment state");
                     c->kseg_cap = (size_t)c->n_kitems + 1;
                 }
-                e = canon::launch_ksys_check_split(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, seg,
-                                                   canon::ksys_candidates(c->q_ks_np, c->q_ks_nr), c->d_kseg,
-                                                   c->num_sms, s);
+                e = c->q_ks_groups
+                        ? canon::launch_kgen_check(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, seg,
+                                                   c->q_ks_total, c->d_kseg, c->num_sms, s)
+                        : canon::launch_ksys_check_split(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, seg,
+                                                         canon::ksys_candidates(c->q_ks_np, c->q_ks_nr),
+                                                         c->d_kseg, c->num_sms, s);
                 c->launches += 3;
             } else {
                 e = canon::launch_ksys_check(c->d_kitems, c->n_kitems, c->d_bytes, c->d_out, c->d_ticket + 1,
@@ -589,6 +631,8 @@ int canon_sync(canon_ctx *c, canon_results *r) {
     r->kernel_ms = c->last_ms;
     c->n_bitems = c->n_kitems = c->n_words = c->n_bytes = 0;
     c->q_max_b = c->q_max_v = c->q_ks_np = c->q_ks_nr = 0;
+    c->q_ks_total = 0;
+    c->q_ks_groups = false;
     c->q_two_pass = true;
     c->q_want_auts = c->q_reupload = false;
     c->item_kind.clear();
@@ -1270,6 +1314,17 @@ uint32_t ksys_segment(const canon_ctx *c, uint64_t n, uint32_t np, uint32_t roun
                                      : ksys_auto_segment(n, total, (uint32_t)(c->num_sms > 0 ? c->num_sms : 1) *
                                                                        KSYS_RESIDENT_WARPS_PER_SM);
     return seg >= total ? 0u : (uint32_t)seg;
+}
+
+// Candidates per warp task of the check with groups of 3 or 4 (always segmented: a
+// canonical KTS(15) tries 6,531,840 relabelings); CANON_KSYS_WHOLE = one segment per item.
+uint32_t kgen_segment(const canon_ctx *c, uint64_t n, uint64_t total) {
+    const uint64_t whole = (total + 31) & ~31ull;
+    uint64_t seg = c->ksys_seg == CANON_KSYS_WHOLE ? whole
+                   : c->ksys_seg ? (((uint64_t)c->ksys_seg + 31u) & ~31ull)
+                                 : ksys_auto_segment(n, total, (uint32_t)(c->num_sms > 0 ? c->num_sms : 1) *
+                                                                   KSYS_RESIDENT_WARPS_PER_SM);
+    return (uint32_t)(seg < whole ? seg : whole);
 }
 
 // The largest batch of matrices with `words` 64-bit words (BIBD) or `bytes` bytes

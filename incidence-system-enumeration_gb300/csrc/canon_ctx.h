@@ -29,6 +29,9 @@ struct canon_ctx {
     bool q_reupload = false;
     // k-system items queued: widest players and filled rounds (the segmented check's size)
     uint32_t q_ks_np = 0, q_ks_nr = 0;
+    // queued k-systems with groups of 3 or 4 (a queue of their own), the most relabelings of one
+    bool q_ks_groups = false;
+    uint64_t q_ks_total = 0;
     // candidates per warp task of the k-system check (canon_set_ksys_segment):
     // 0 = chosen per launch, CANON_KSYS_WHOLE = one warp per matrix
     uint32_t ksys_seg = 0;
@@ -69,6 +72,7 @@ namespace canon {
 // candidates per warp task for a k-system check of n items of np players and
 // `rounds` rounds (0 = one warp per matrix)
 uint32_t ksys_segment(const canon_ctx *c, uint64_t n, uint32_t np, uint32_t rounds);
+uint32_t kgen_segment(const canon_ctx *c, uint64_t n, uint64_t total);
 // frees the captured k-system enumeration of a context
 void ksys_graph_release(canon_ctx *c);
 }  // namespace canon

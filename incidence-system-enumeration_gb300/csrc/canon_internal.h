@@ -172,6 +172,23 @@ struct KsysSeg {
 cudaError_t launch_ksys_check_split(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes, Outputs out,
                                    uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
                                    cudaStream_t s, const uint64_t *d_n = nullptr);
+// the check of k-systems with groups of 3 or 4 (np <= 16; Item::pad holds the group
+// size), split into segments of seg_cands relabelings over warps; automorphisms are not
+// stored
+cudaError_t launch_kgen_check(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes, Outputs out,
+                              uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
+                              cudaStream_t s);
+// relabelings of one check with groups of g: (np/g)! * (g!)^(np/g) * rounds
+inline uint64_t kgen_candidates(uint32_t np, uint32_t g, uint32_t rounds) {
+    uint64_t t = 1, gf = 1;
+    for (uint32_t i = 2; i <= g; ++i)
+        gf *= i;
+    for (uint32_t i = 2; i <= np / g; ++i)
+        t *= i;
+    for (uint32_t i = 0; i < np / g; ++i)
+        t *= gf;
+    return t * rounds;
+}
 // warps of the segmented k-system kernel resident on one SM (128-thread blocks)
 constexpr uint32_t KSYS_RESIDENT_WARPS_PER_SM = 64;
 // Candidates per segment for n items of at most `total` candidates each: about 8

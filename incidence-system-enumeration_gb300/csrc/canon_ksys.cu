@@ -13,7 +13,10 @@
 // candidates; a ballot finds the first "smaller" candidate, which ends the check
 // exactly where the reference stops.  Rounds are kept as nibble-packed partner
 // tables, so a round comparison is one XOR and a find-first-set.
+#include <algorithm>
+
 #include "canon_bibd_core.cuh"
+#include "canon_kgen.cuh"
 #include "canon_ksys_core.cuh"
 
 namespace canon {
@@ -155,6 +158,139 @@ __global__ void ksys_seg_finish_kernel(const Item *__restrict__ items, uint32_t 
     }
 }
 
+// ---- k-systems with groups of 3 or 4 ---------------------------------------
+// One relabeling is evaluated by kg_eval (canon_kgen.cuh).  Work split, early stop and
+// outputs are those of the segmented check of group size 2: one (segment, item) unit per
+// warp task, the first rejection kept by an atomic minimum of (candidate << 32 | player
+// index), |Aut| reported for canonical matrices.
+__constant__ uint8_t c_gperm3[6 * 3];  // the 3! in-group orders of cnvInit()
+__constant__ uint8_t c_gperm4[24 * 4];
+
+// Loads one item's rounds into the warp's tables and checks their form (all 32 lanes).
+__device__ bool kg_load(const Item &item, unsigned g, const uint8_t *__restrict__ bytes, KgTables &T,
+                        unsigned lane) {
+    const unsigned np = item.ncols, nr = item.nrows, ng = np / g;
+    bool ok = item.kind == KIND_KSYS && kg_shape_ok(np, g, nr);
+    if (ok && lane < nr) {
+        const uint8_t *row = bytes + item.data_off + lane * np;
+        uint64_t sq = 0, ps = 0;
+        unsigned seen = 0;
+        for (unsigned p = 0; p < np; ++p) {
+            const unsigned x = row[p];
+            if (x >= np || ((seen >> x) & 1u))
+                ok = false;
+            seen |= 1u << (x & 15u);
+            sq = nib_set(sq, p, x);
+            ps = nib_set(ps, x, p);
+            // players ascending inside a group, groups by their first player
+            if (p % g && x <= row[p - 1])
+                ok = false;
+            if (p && p % g == 0 && x <= row[p - g])
+                ok = false;
+            if (lane == 0 && x != p)
+                ok = false;   // round 0 = 0 1 2 .. np-1
+        }
+        T.seq[lane] = sq;
+        T.pos[lane] = ps;
+        for (unsigned k = 0; k < ng; ++k) {
+            uint32_t l[4];
+            for (unsigned e = 0; e < 4; ++e)
+                l[e] = e < g ? row[k * g + e] & 15u : 0u;
+            T.okey[lane][k] = (uint16_t)kg_key(l, g);
+        }
+    }
+    ok = __all_sync(0xFFFFFFFFu, ok);
+    __syncwarp();
+    // no pair of players in two groups
+    if (ok && lane == 0) {
+        uint32_t pairs[16] = {};
+        for (unsigned r = 0; r < nr && ok; ++r) {
+            for (unsigned k = 0; k < ng; ++k)
+                for (unsigned e = 0; e < g; ++e)
+                    for (unsigned f = e + 1; f < g; ++f) {
+                        const unsigned x = nib_get(T.seq[r], k * g + e), y = nib_get(T.seq[r], k * g + f);
+                        if ((pairs[x] >> y) & 1u)
+                            ok = false;
+                        pairs[x] |= 1u << y;
+                        pairs[y] |= 1u << x;
+                    }
+        }
+    }
+    ok = __shfl_sync(0xFFFFFFFFu, ok, 0);
+    return ok;
+}
+
+__global__ void __launch_bounds__(KTPB) kgen_seg_kernel(const Item *__restrict__ items, uint32_t n_items,
+                                                        const uint8_t *__restrict__ bytes, uint32_t seg_cands,
+                                                        uint64_t n_units, KsysSeg *state,
+                                                        unsigned long long *ticket) {
+    __shared__ KgTables s_t[KW];
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0)
+            t = atomicAdd(ticket, 1ull);
+        t = __shfl_sync(0xFFFFFFFFu, t, 0);
+        if (t >= n_units)
+            break;
+        const uint32_t it = (uint32_t)(t % n_items);
+        const uint32_t seg = (uint32_t)(t / n_items);
+        const Item item = items[it];
+        const unsigned g = item.pad, np = item.ncols, nr = item.nrows;
+        KsysSeg &st = state[it];
+        const uint64_t start = (uint64_t)seg * seg_cands;
+        if (seg && kg_shape_ok(np, g, nr) && start >= kg_total(np, g, nr))
+            continue;
+        if ((volatile_key(&st.key) >> 32) < start)
+            continue;
+        const bool ok = kg_load(item, g, bytes, s_t[warp], lane);
+        if (!ok) {
+            if (lane == 0 && seg == 0)
+                st.bad = 1u;
+            continue;
+        }
+        const uint64_t total = kg_total(np, g, nr);
+        const uint64_t end = start + seg_cands < total ? start + seg_cands : total;
+        const int pidx0 = (int)(nr * np) - (int)g - 1;
+        unsigned n_aut = 0;
+        for (uint64_t base = start; base < end; base += 32u) {
+            if ((volatile_key(&st.key) >> 32) < base)
+                break;
+            const unsigned c = (unsigned)base + lane;
+            int res = 1, pi = pidx0;
+            if (c < end)
+                res = kg_eval(c, np, g, np / g, nr, s_t[warp], ksys::c_heap + ksys::c_heap_off[np / g] * 6u,
+                              g == 3 ? c_gperm3 : c_gperm4, pidx0, pi);
+            const unsigned rej = __ballot_sync(0xFFFFFFFFu, c < end && res < 0);
+            const unsigned aut = __ballot_sync(0xFFFFFFFFu, c < end && res == 0);
+            if (rej) {
+                const unsigned fl = __ffs(rej) - 1u;
+                if (lane == fl)
+                    atomicMin(&st.key, ((unsigned long long)c << 32) | (unsigned)pi);
+                break;
+            }
+            n_aut += __popc(aut);
+        }
+        if (lane == 0 && n_aut)
+            atomicAdd(&st.n_aut, n_aut);
+    }
+}
+
+// The outputs of the general check, one thread per item.
+__global__ void kgen_finish_kernel(const Item *__restrict__ items, uint32_t n_items, const KsysSeg *state,
+                                   Outputs out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_items; i += gridDim.x * blockDim.x) {
+        const Item item = items[i];
+        const KsysSeg st = state[i];
+        const unsigned g = item.pad, np = item.ncols, nr = item.nrows;
+        const bool ok = !st.bad && item.kind == KIND_KSYS && kg_shape_ok(np, g, nr);
+        const bool canonical = ok && st.key == ~0ull;
+        const uint64_t cands = !ok ? 0 : canonical ? kg_total(np, g, nr) - 1 : (st.key >> 32);
+        const int pidx = canonical || !ok ? (int)(nr * np) - (int)g - 1 : (int)(uint32_t)st.key;
+        write_item(out, item.out_idx, ok, canonical, false, pidx, st.n_aut, cands, false, np);
+    }
+}
+
 // One persistent kernel over a mixed batch (k-systems and incidence matrices of
 // any shapes): every warp first takes k-system items from the first work counter,
 // one warp per matrix, and then incidence matrices from the second, one thread
@@ -268,7 +404,23 @@ cudaError_t ksys_upload_tables() {
                 p[i] = (uint8_t)i;
         }
     }
-    cudaError_t e = cudaMemcpyToSymbol(ksys::c_heap, heap, sizeof(heap));
+    // the in-group orders of cnvInit() for groups of 3 and 4: permutations in lexicographic order
+    uint8_t g3[6 * 3], g4[24 * 4];
+    for (int gs = 3; gs <= 4; ++gs) {
+        uint8_t *dst = gs == 3 ? g3 : g4;
+        uint8_t cur[4] = {0, 1, 2, 3};
+        int cnt = 0;
+        do {
+            for (int j = 0; j < gs; ++j)
+                dst[cnt * gs + j] = cur[j];
+            ++cnt;
+        } while (std::next_permutation(cur, cur + gs));
+    }
+    cudaError_t e = cudaMemcpyToSymbol(c_gperm3, g3, sizeof(g3));
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbol(c_gperm4, g4, sizeof(g4));
+    if (e == cudaSuccess)
+        e = cudaMemcpyToSymbol(ksys::c_heap, heap, sizeof(heap));
     if (e == cudaSuccess)
         e = cudaMemcpyToSymbol(ksys::c_heap_off, off, sizeof(off));
     if (e == cudaSuccess)
@@ -342,4 +494,44 @@ cudaError_t launch_ksys_check_split(const Item *d_items, uint32_t n_items, const
     ksys_seg_finish_kernel<<<gi, 256, 0, s>>>(d_items, n_items, d_n, d_state, out);
     return cudaGetLastError();
 }
+// the check of k-systems with groups of 3 or 4 (Item::pad = the group size): every item's
+// relabelings in segments of seg_cands over warps; total_max = the most of any item
+cudaError_t launch_kgen_check(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes, Outputs out,
+                              uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
+                              cudaStream_t s) {
+    if (!n_items)
+        return cudaSuccess;
+    if (seg_cands < 32 || (seg_cands & 31u))
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(d_state + n_items, 0, sizeof(KsysSeg), s);
+    if (e != cudaSuccess)
+        return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kgen_seg_kernel, ksys::KTPB, 0);
+    if (e != cudaSuccess)
+        return e;
+    if (per_sm < 1)
+        per_sm = 1;
+    const int sms = num_sms > 0 ? num_sms : 1;
+    const uint64_t units = ((total_max + seg_cands - 1) / seg_cands) * n_items;
+    uint64_t grid = (uint64_t)per_sm * sms;
+    const uint64_t need = (units + ksys::KW - 1) / ksys::KW;
+    if (grid > need)
+        grid = need;
+    int gi = (int)((n_items + 255) / 256);
+    if (gi > 4 * sms)
+        gi = 4 * sms;
+    ksys_seg_init_kernel<<<gi, 256, 0, s>>>(d_state, n_items, nullptr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    unsigned long long *ticket = reinterpret_cast<unsigned long long *>(d_state + n_items);
+    kgen_seg_kernel<<<(int)grid, ksys::KTPB, 0, s>>>(d_items, n_items, d_bytes, seg_cands, units, d_state, ticket);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+        return e;
+    kgen_finish_kernel<<<gi, 256, 0, s>>>(d_items, n_items, d_state, out);
+    return cudaGetLastError();
+}
+
 }  // namespace canon

@@ -14,10 +14,10 @@ namespace canon {
 constexpr uint64_t NIB_ID16 = 0xFEDCBA9876543210ull;   // identity permutation of 0..15
 constexpr uint64_t NIB_ONES = 0x1111111111111111ull;
 
-__device__ __forceinline__ unsigned nib_get(uint64_t p, unsigned i) {
+__host__ __device__ __forceinline__ unsigned nib_get(uint64_t p, unsigned i) {
     return (unsigned)(p >> ((i & 15u) << 2)) & 15u;
 }
-__device__ __forceinline__ uint64_t nib_set(uint64_t p, unsigned i, unsigned x) {
+__host__ __device__ __forceinline__ uint64_t nib_set(uint64_t p, unsigned i, unsigned x) {
     const unsigned sh = (i & 15u) << 2;
     return (p & ~(15ull << sh)) | ((uint64_t)(x & 15u) << sh);
 }

@@ -52,7 +52,7 @@ t_saveRowToChange = 4
 
 HEADER_SYMBOLS = [
     "canon_create", "canon_destroy", "canon_last_error", "canon_submit_bibd", "canon_submit_ksys",
-    "canon_sync", "canon_set_ordering", "canon_canonize_bibd", "canon_check_bibd_device",
+    "canon_submit_ksys_groups", "canon_sync", "canon_set_ordering", "canon_canonize_bibd", "canon_check_bibd_device",
     "canon_generate_sts_device", "canon_device_alloc", "canon_device_free", "canon_memcpy_d2h",
     "canon_memcpy_h2d", "canon_last_kernel_ms", "canon_kernel_launches", "canon_stream_sync",
     "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys", "canon_mlp_features",
@@ -173,6 +173,7 @@ def load_library(path=LIB_PATH):
     L.canon_last_error.restype = ctypes.c_char_p
     L.canon_submit_bibd.argtypes = [vp, ctypes.POINTER(BibdBatch)]
     L.canon_submit_ksys.argtypes = [vp, ctypes.POINTER(KsysBatch)]
+    L.canon_submit_ksys_groups.argtypes = [vp, ctypes.POINTER(KsysBatch), u32]
     L.canon_sync.argtypes = [vp, ctypes.POINTER(Results)]
     L.canon_set_ordering.argtypes = [vp, vp]
     L.canon_canonize_bibd.argtypes = [vp, u32, u32, u32, u64p, u64p]
@@ -377,6 +378,16 @@ class Context:
         bt = KsysBatch(n, np_, rounds, flags, _ptr(data, ctypes.c_uint8),
                        _ptr(nr, ctypes.c_uint8) if nr is not None else None)
         self._check(self.lib.canon_submit_ksys(self.h, ctypes.byref(bt)))
+        return n
+
+    def submit_ksys_groups(self, data, np_, rounds, group_size, flags=0, nrows=None):
+        """canon_submit_ksys_groups: k-systems with groups of 2, 3 or 4 players."""
+        data = np.ascontiguousarray(data, dtype=np.uint8).reshape(-1)
+        n = data.size // (np_ * rounds)
+        nr = None if nrows is None else np.ascontiguousarray(nrows, dtype=np.uint8)
+        bt = KsysBatch(n, np_, rounds, flags, _ptr(data, ctypes.c_uint8),
+                       _ptr(nr, ctypes.c_uint8) if nr is not None else None)
+        self._check(self.lib.canon_submit_ksys_groups(self.h, ctypes.byref(bt), group_size))
         return n
 
     def sync(self, allow_timeout=False, raw=False, copy=True):

@@ -180,6 +180,16 @@ const char *canon_last_error(const canon_ctx *ctx);
 int canon_submit_bibd(canon_ctx *ctx, const canon_bibd_batch *batch);
 /* Queue a batch of k-system matrices: one cnvCheckNew(0, nrows) per matrix. */
 int canon_submit_ksys(canon_ctx *ctx, const canon_ksys_batch *batch);
+/* Queue a batch of k-system matrices with groups of group_size players: one
+ * cnvCheckNew(0, nrows) per matrix on the reference's general path (kmProcessMatrix,
+ * k-Factorization/TripleSys/Source/kmSupport.cpp:220-313), e.g. Kirkman triple systems.
+ * group_size 2 is canon_submit_ksys; 3 and 4 take np <= 16 players (a multiple of the
+ * group size, 2 groups at least), rounds as result() rows (players ascending inside a
+ * group, groups ordered by first player, round 0 = 0 1 .. np-1).  Every relabeling,
+ * (np/g)! * (g!)^(np/g) per round, is tried on the GPU.  Outputs as for group size 2;
+ * CANON_SAVE_AUTS is refused.  Such batches form a queue of their own: no incidence or
+ * group-size-2 batch may be queued with them before canon_sync. */
+int canon_submit_ksys_groups(canon_ctx *ctx, const canon_ksys_batch *batch, uint32_t group_size);
 /* Copy the queued input to the GPU, run the checks, wait, expose the results. */
 int canon_sync(canon_ctx *ctx, canon_results *out);
 /* Work split of the k-system check (cnvCheckNew): the candidates of a matrix

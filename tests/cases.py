@@ -75,6 +75,42 @@ def ksys_relabel_random(R, rng, g=2):
     return ksys_sorted_form(lab[R], g)
 
 
+def ksys_relabel_keep_round0(R, rng, g=2):
+    """Random relabeling that maps round 0 onto itself (groups and the players inside
+    them permuted), then the sorted form: an isomorphic copy, mostly not canonical."""
+    nr, n = R.shape
+    lab = np.zeros(n, np.int64)
+    for new_g, gi in enumerate(rng.permutation(n // g)):
+        for k, pos in enumerate(rng.permutation(g)):
+            lab[gi * g + pos] = g * new_g + k
+    return ksys_sorted_form(lab[R], g)
+
+
+def ksys_random_partial(np_, g, nr, rng, attempts=50, tries=200):
+    """A random partial k-system in sorted form: round 0 = 0 1 .. np-1, every further
+    round a random partition into groups of g that repeats no pair (None if the
+    bounded random search finds none)."""
+    for _ in range(attempts):
+        rows = [list(range(np_))]
+        used = {(a, b) for k in range(0, np_, g) for a in range(k, k + g) for b in range(a + 1, k + g)}
+        ok = True
+        for _r in range(1, nr):
+            for _t in range(tries):
+                perm = [int(x) for x in rng.permutation(np_)]
+                groups = [sorted(perm[i:i + g]) for i in range(0, np_, g)]
+                pairs = {(a, b) for grp in groups for i, a in enumerate(grp) for b in grp[i + 1:]}
+                if not pairs & used:
+                    break
+            else:
+                ok = False
+                break
+            used |= pairs
+            rows.append([x for grp in sorted(groups) for x in grp])
+        if ok:
+            return ksys_sorted_form(np.array(rows, np.uint8), g)
+    return None
+
+
 def load_result_tables():
     import json
     with open(os.path.join(GOLDEN, "bibd_result_tables.json")) as f:

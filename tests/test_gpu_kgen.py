@@ -1,0 +1,139 @@
+"""The GPU check of k-systems with groups of 3 or 4 (canon_submit_ksys_groups) against
+the oracle's cnvCheckNew() restatement and the reference's Kirkman results: the 7
+Kirkman triple systems of 15 players are canonical with the reference's |Aut(M)| after
+all 5! x 3!^5 x 7 - 1 relabelings; prefixes, relabelled copies and random partial
+systems with groups of 3 and 4 give the oracle's verdict, m_playerIndex and relabelings
+tried, under every work split; ill-formed items and refused batches fail as stated."""
+import numpy as np
+import pytest
+
+import cases
+import ise_gb300 as G
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["canonical", "status", "player_index", "trials", "aut"]
+
+
+def expect(R, g):
+    o = oracle.ksys_test(R, g=g)
+    return dict(canonical=o["canonical"], player_index=o["player_index"],
+                aut=o["n_aut"] if o["canonical"] else 0, trials=o["candidates"])
+
+
+def got(r, i):
+    return dict(canonical=bool(r["canonical"][i]), player_index=int(r["player_index"][i]),
+                aut=int(r["aut"][i]), trials=int(r["trials"][i]))
+
+
+def test_kirkman_systems_are_canonical_with_reference_aut(ctx):
+    kts = cases.load_kts15()
+    mats = np.stack([R for R, _ in kts])
+    assert ctx.submit_ksys_groups(mats, 15, 7, 3) == 7
+    r = ctx.sync()
+    for i, (_, aut) in enumerate(kts):
+        assert r["status"][i] == 0
+        assert got(r, i) == dict(canonical=True, player_index=7 * 15 - 4, aut=aut, trials=120 * 6 ** 5 * 7 - 1)
+
+
+def mixed_batch(seed):
+    """(matrices padded to the batch's rounds, filled rounds, group size) per shape."""
+    rng = np.random.default_rng(seed)
+    kts = cases.load_kts15()
+    out = {}
+    mats, nrows = [], []
+    for R, _ in kts:
+        k = int(rng.integers(2, 8))
+        for X in (R[:k] if k < 4 else None, cases.ksys_relabel_random(R, rng, g=3),
+                  cases.ksys_relabel_keep_round0(R[:k], rng, g=3), cases.ksys_relabel_random(R[:k], rng, g=3)):
+            if X is None:
+                continue
+            pad = np.zeros((7, 15), np.uint8)
+            pad[:X.shape[0]] = X
+            mats.append(pad)
+            nrows.append(X.shape[0])
+    n15 = 0
+    while n15 < 40:
+        X = cases.ksys_random_partial(15, 3, 3 + n15 % 2, rng)
+        if X is not None:
+            pad = np.zeros((7, 15), np.uint8)
+            pad[:X.shape[0]] = X
+            mats.append(pad)
+            nrows.append(X.shape[0])
+            n15 += 1
+    bad = mats[1].copy()
+    bad[1, [0, 1]] = bad[1, [1, 0]]       # players out of order inside a group: ill formed
+    mats.append(bad)
+    nrows.append(7)
+    out[(15, 7, 3)] = (np.stack(mats), np.array(nrows, np.uint8))
+    for np_, g, nr in [(9, 3, 4), (12, 3, 4), (16, 4, 3)]:
+        mats, nrows = [], []
+        for t in range(24):
+            X = cases.ksys_random_partial(np_, g, 2 + t % (nr - 1), rng)
+            if X is None:
+                continue
+            if t % 3 == 0:
+                X = cases.ksys_relabel_keep_round0(X, rng, g=g)
+            pad = np.zeros((nr, np_), np.uint8)
+            pad[:X.shape[0]] = X
+            mats.append(pad)
+            nrows.append(X.shape[0])
+        out[(np_, nr, g)] = (np.stack(mats), np.array(nrows, np.uint8))
+    return out
+
+
+def run(ctx, seg, shapes):
+    ctx.set_ksys_segment(seg)
+    for (np_, nr, g), (mats, nrows) in shapes.items():
+        ctx.submit_ksys_groups(mats, np_, nr, g, 0, nrows)
+    return ctx.sync()
+
+
+def test_groups_of_3_and_4_equal_the_oracle_under_every_split(ctx):
+    shapes = mixed_batch(3)
+    try:
+        first = run(ctx, 0, shapes)
+        for seg in [G.KSYS_WHOLE, 32, 4096]:
+            r = run(ctx, seg, shapes)
+            for f in FIELDS:
+                assert np.array_equal(np.asarray(r[f]), np.asarray(first[f])), (seg, f)
+    finally:
+        ctx.set_ksys_segment(0)
+    i = 0
+    n_pi = n_canon = 0
+    for (np_, nr, g), (mats, nrows) in shapes.items():
+        for X, k in zip(mats, nrows):
+            if np_ == 15 and i == len(shapes[(15, 7, 3)][0]) - 1:
+                assert first["status"][i] & G.ST_BADINPUT
+                assert not first["canonical"][i]
+            else:
+                assert first["status"][i] == 0, i
+                w = expect(X[:k], g)
+                assert got(first, i) == w, (i, np_, g, k)
+                n_pi += w["player_index"] != k * np_ - g - 1
+                n_canon += w["canonical"]
+            i += 1
+    assert i == first["n"]
+    assert n_canon >= 3 and n_pi >= 1
+
+
+def test_refused_batches(ctx):
+    kts = cases.load_kts15()
+    R = kts[0][0][None]
+    with pytest.raises(G.CanonError):
+        ctx.submit_ksys_groups(R, 15, 7, 5)
+    with pytest.raises(G.CanonError):
+        ctx.submit_ksys_groups(R, 15, 7, 3, G.SAVE_AUTS)
+    with pytest.raises(G.CanonError):
+        ctx.submit_ksys_groups(np.zeros((1, 3, 14), np.uint8), 14, 3, 3)
+    ctx.submit_ksys_groups(R, 15, 7, 3)
+    k8, _ = oracle.ksys_enumerate(8)
+    with pytest.raises(G.CanonError):
+        ctx.submit_ksys(k8[0][0][None], 8, 7)
+    r = ctx.sync()
+    assert r["n"] == 1 and r["canonical"][0]
+    # the queue takes group-size-2 batches again after the sync
+    ctx.submit_ksys_groups(k8[0][0][None], 8, 7, 2)
+    r = ctx.sync()
+    assert r["n"] == 1 and r["canonical"][0]
