@@ -13,8 +13,6 @@
 // candidates; a ballot finds the first "smaller" candidate, which ends the check
 // exactly where the reference stops.  Rounds are kept as nibble-packed partner
 // tables, so a round comparison is one XOR and a find-first-set.
-#include <algorithm>
-
 #include "canon_bibd_core.cuh"
 #include "canon_kgen.cuh"
 #include "canon_ksys_core.cuh"
@@ -404,17 +402,27 @@ cudaError_t ksys_upload_tables() {
                 p[i] = (uint8_t)i;
         }
     }
-    // the in-group orders of cnvInit() for groups of 3 and 4: permutations in lexicographic order
+    // the in-group orders of cnvInit() for groups of 3 and 4: the g-digit base-g numbers
+    // in increasing order whose digits are all different
     uint8_t g3[6 * 3], g4[24 * 4];
     for (int gs = 3; gs <= 4; ++gs) {
         uint8_t *dst = gs == 3 ? g3 : g4;
-        uint8_t cur[4] = {0, 1, 2, 3};
         int cnt = 0;
-        do {
+        const int lim = gs == 3 ? 27 : 256;
+        for (int x = 0; x < lim; ++x) {
+            int digit[4], y = x;
+            unsigned seen = 0;
+            for (int j = gs - 1; j >= 0; --j) {
+                digit[j] = y % gs;
+                y /= gs;
+                seen |= 1u << digit[j];
+            }
+            if (seen != (1u << gs) - 1u)
+                continue;
             for (int j = 0; j < gs; ++j)
-                dst[cnt * gs + j] = cur[j];
+                dst[cnt * gs + j] = (uint8_t)digit[j];
             ++cnt;
-        } while (std::next_permutation(cur, cur + gs));
+        }
     }
     cudaError_t e = cudaMemcpyToSymbol(c_gperm3, g3, sizeof(g3));
     if (e == cudaSuccess)

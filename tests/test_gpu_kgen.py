@@ -43,25 +43,29 @@ def mixed_batch(seed):
     kts = cases.load_kts15()
     out = {}
     mats, nrows = [], []
-    for R, _ in kts:
+    for i, (R, _) in enumerate(kts):
         k = int(rng.integers(2, 8))
-        for X in (R[:k] if k < 4 else None, cases.ksys_relabel_random(R, rng, g=3),
+        for X in (R[:1 + i % 4], cases.ksys_relabel_random(R, rng, g=3),
                   cases.ksys_relabel_keep_round0(R[:k], rng, g=3), cases.ksys_relabel_random(R[:k], rng, g=3)):
-            if X is None:
-                continue
             pad = np.zeros((7, 15), np.uint8)
             pad[:X.shape[0]] = X
             mats.append(pad)
             nrows.append(X.shape[0])
-    n15 = 0
-    while n15 < 40:
+    # random partial systems of 15 players, until two of them lower m_playerIndex
+    n15 = n_pi = 0
+    while n15 < 40 or (n_pi < 2 and n15 < 800):
         X = cases.ksys_random_partial(15, 3, 3 + n15 % 2, rng)
-        if X is not None:
-            pad = np.zeros((7, 15), np.uint8)
-            pad[:X.shape[0]] = X
-            mats.append(pad)
-            nrows.append(X.shape[0])
-            n15 += 1
+        if X is None:
+            continue
+        n15 += 1
+        lowers = oracle.ksys_test(X, g=3)["player_index"] != X.shape[0] * 15 - 4
+        if n15 > 40 and not lowers:
+            continue
+        n_pi += lowers
+        pad = np.zeros((7, 15), np.uint8)
+        pad[:X.shape[0]] = X
+        mats.append(pad)
+        nrows.append(X.shape[0])
     bad = mats[1].copy()
     bad[1, [0, 1]] = bad[1, [1, 0]]       # players out of order inside a group: ill formed
     mats.append(bad)
