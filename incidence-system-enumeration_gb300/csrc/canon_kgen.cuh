@@ -46,9 +46,15 @@ __host__ __device__ __forceinline__ uint32_t kg_key(const uint32_t *l, unsigned 
     return g == 4 ? (a << 12) | (b << 8) | (c << 4) | d : (a << 12) | (b << 8) | (c << 4);
 }
 
-// player p of a sorted round given as keys
+// player p of a sorted round given as keys (the key picked by compares, so that the
+// keys stay in registers)
 __host__ __device__ __forceinline__ unsigned kg_key_player(const uint32_t *key, unsigned p, unsigned g) {
-    return (key[p / g] >> (4u * (3u - p % g))) & 15u;
+    const unsigned k = p / g;
+    uint32_t v = key[0];
+#pragma unroll
+    for (unsigned j = 1; j < (unsigned)KG_NGMAX; ++j)
+        v = k == j ? key[j] : v;
+    return (v >> (4u * (3u - p % g))) & 15u;
 }
 
 // Relabeling c of the matrix in T (np players in ng groups of g, nr rounds).
@@ -134,12 +140,14 @@ __host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigne
                 }
         int cmp = 0;
         unsigned kd = 0;
-        for (unsigned k = 0; k < ng; ++k) {
-            const uint32_t ok = T.okey[i][k];
-            if (key[k] != ok) {
-                cmp = key[k] < ok ? -1 : 1;
-                kd = k;
-                break;
+#pragma unroll
+        for (unsigned k = 0; k < (unsigned)KG_NGMAX; ++k) {
+            if (!cmp && k < ng) {
+                const uint32_t ok = T.okey[i][k];
+                if (key[k] != ok) {
+                    cmp = key[k] < ok ? -1 : 1;
+                    kd = k;
+                }
             }
         }
         if (!cmp) {
