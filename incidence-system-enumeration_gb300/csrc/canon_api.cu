@@ -1318,12 +1318,19 @@ uint32_t ksys_segment(const canon_ctx *c, uint64_t n, uint32_t np, uint32_t roun
 
 // Candidates per warp task of the check with groups of 3 or 4 (always segmented: a
 // canonical KTS(15) tries 6,531,840 relabelings); CANON_KSYS_WHOLE = one segment per item.
+// The automatic size is capped at KGEN_SEGMENT_MAX: in an enumeration level most matrices
+// are rejected within their first relabelings, so the work is the few canonical ones, and
+// a segment sized as if every matrix tried all its relabelings would leave each of those to
+// a handful of warps (a level of 13,824 matrices of 16 players: 2.8M-relabeling segments).
+constexpr uint64_t KGEN_SEGMENT_MAX = 65536;
 uint32_t kgen_segment(const canon_ctx *c, uint64_t n, uint64_t total) {
     const uint64_t whole = (total + 31) & ~31ull;
     uint64_t seg = c->ksys_seg == CANON_KSYS_WHOLE ? whole
                    : c->ksys_seg ? (((uint64_t)c->ksys_seg + 31u) & ~31ull)
-                                 : ksys_auto_segment(n, total, (uint32_t)(c->num_sms > 0 ? c->num_sms : 1) *
-                                                                   KSYS_RESIDENT_WARPS_PER_SM);
+                                 : std::min<uint64_t>(
+                                       KGEN_SEGMENT_MAX,
+                                       ksys_auto_segment(n, total, (uint32_t)(c->num_sms > 0 ? c->num_sms : 1) *
+                                                                       KSYS_RESIDENT_WARPS_PER_SM));
     return (uint32_t)(seg < whole ? seg : whole);
 }
 

@@ -73,6 +73,9 @@ namespace canon {
 // `rounds` rounds (0 = one warp per matrix)
 uint32_t ksys_segment(const canon_ctx *c, uint64_t n, uint32_t np, uint32_t rounds);
 uint32_t kgen_segment(const canon_ctx *c, uint64_t n, uint64_t total);
+// the largest batch of matrices of `words` 64-bit words (BIBD) or `bytes` bytes
+// (k-systems) each that one canon_submit_* call can queue on an empty context
+uint32_t batch_capacity(const canon_ctx *c, uint32_t words, uint32_t bytes);
 // frees the captured k-system enumeration of a context
 void ksys_graph_release(canon_ctx *c);
 }  // namespace canon

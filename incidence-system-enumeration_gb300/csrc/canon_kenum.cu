@@ -1,0 +1,245 @@
+// canon_kenum.cu -- orderly enumeration of k-systems with groups of 3 or 4 (resolvable
+// designs with blocks of 3 or 4 such as the Kirkman triple systems of 15 players): the
+// next rounds of every canonical parent are built on the host cores, checked in batches
+// by the GPU check of canon_submit_ksys_groups (kgen_seg_kernel), and the canonical
+// ones kept.  The work of alldata::Run() for group size 3 or 4 with the check at every
+// level (k-Factorization/TripleSys/Source/TripleSys.cpp:80-775, rounds built by
+// processOneDay()/getNextPlayer() :487-775, check at checkCurrentResult.cpp:91).
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "../../include/canon_gb300.h"
+#include "canon_ctx.h"
+#include "canon_internal.h"
+
+namespace {
+
+// The pairs not yet used (bit y of free[x]: x and y have not met) must still split into
+// groups: for every player, the players it has not met must fall into groups of g - 1
+// that have not met each other either, or no later rounds complete the matrix.  The links
+// test of the reference (CChecklLink::checkLinksV, k-Factorization/TripleSys/Source/
+// checkLinksV.cpp, applied to every player in checkLinks.cpp:60-110) for groups of 3,
+// generalised to groups of 4.  A necessary condition only: it drops matrices that no
+// complete matrix extends, so the complete matrices found are the same with it.
+bool split_into_groups(unsigned set, const uint32_t *free, int k);
+
+// take `need` more members of a group (pairwise unmet, from cand), then split the rest
+bool pick_members(unsigned set, unsigned cand, const uint32_t *free, int k, int need) {
+    if (!need)
+        return split_into_groups(set, free, k);
+    while (cand) {
+        const int w = __builtin_ctz(cand);
+        cand &= cand - 1u;
+        if (pick_members(set & ~(1u << w), cand & free[w], free, k, need - 1))
+            return true;
+    }
+    return false;
+}
+
+bool split_into_groups(unsigned set, const uint32_t *free, int k) {
+    if (!set)
+        return true;
+    const int v = __builtin_ctz(set);
+    const unsigned rest = set & ~(1u << v);
+    return pick_members(rest, rest & free[v], free, k, k - 1);
+}
+
+bool links_complete(const uint32_t *used, int np, int g) {
+    const unsigned all = (1u << np) - 1u;
+    uint32_t free[16];
+    for (int x = 0; x < np; ++x)
+        free[x] = all & ~used[x] & ~(1u << x);
+    for (int x = 0; x < np; ++x)
+        if (free[x] && !split_into_groups(free[x], free, g - 1))
+            return false;
+    return true;
+}
+
+// The rounds that may follow a parent of d rounds: every partition of the np players
+// into groups of g that repeats no pair of an earlier round, written in result() form
+// (players ascending inside a group, groups ordered by their first player), whose second
+// entry (the first partner of player 0) is above the parent's last one, so that the rounds
+// stay ordered by their second entry, and after which the unmet pairs still split into
+// groups (links_complete).  Appended to out as parent + round.
+struct RoundBuilder {
+    int np, g, d;
+    const uint8_t *parent;
+    uint32_t used[16];
+    uint8_t row[16];
+    std::vector<uint8_t> *out;
+
+    void emit() {
+        uint32_t u[16];
+        std::memcpy(u, used, sizeof(u));
+        for (int q = 0; q < np; q += g)
+            for (int e = 0; e < g; ++e)
+                for (int f = e + 1; f < g; ++f) {
+                    u[row[q + e]] |= 1u << row[q + f];
+                    u[row[q + f]] |= 1u << row[q + e];
+                }
+        if (!links_complete(u, np, g))
+            return;
+        out->insert(out->end(), parent, parent + (size_t)d * np);
+        out->insert(out->end(), row, row + np);
+    }
+    // position pos starts a group: its first player is the lowest one not taken
+    void group(unsigned taken, int pos) {
+        if (pos == np) {
+            emit();
+            return;
+        }
+        const int a = __builtin_ctz(~taken);
+        row[pos] = (uint8_t)a;
+        const int minp = a == 0 ? parent[(size_t)(d - 1) * np + 1] + 1 : a + 1;
+        const unsigned all = (1u << np) - 1u;
+        partner(taken | (1u << a), pos + 1, 1, all & ~(taken | (1u << a)) & ~used[a], minp);
+    }
+    // the k-th member of the group at positions pos-k .. : a player of `allowed` >= minp
+    void partner(unsigned taken, int pos, int k, unsigned allowed, int minp) {
+        if (k == g) {
+            group(taken, pos);
+            return;
+        }
+        unsigned m = allowed & ~((1u << minp) - 1u);
+        while (m) {
+            const int p = __builtin_ctz(m);
+            m &= m - 1u;
+            row[pos] = (uint8_t)p;
+            partner(taken | (1u << p), pos + 1, k + 1, allowed & ~used[p] & ~(1u << p), p + 1);
+        }
+    }
+    void run() {
+        std::memset(used, 0, sizeof(used));
+        for (int r = 0; r < d; ++r)
+            for (int q = 0; q < np; q += g)
+                for (int e = 0; e < g; ++e)
+                    for (int f = e + 1; f < g; ++f) {
+                        const int x = parent[(size_t)r * np + q + e], y = parent[(size_t)r * np + q + f];
+                        used[x] |= 1u << y;
+                        used[y] |= 1u << x;
+                    }
+        group(0u, 0);
+    }
+};
+
+// the children of every parent (in parent order), built on up to 16 host threads
+void build_level(const std::vector<uint8_t> &parents, int d, int np, int g, std::vector<uint8_t> &out) {
+    const size_t pl = (size_t)d * np, n = parents.size() / pl;
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = nt > 16 ? 16 : (nt < 1 ? 1 : nt);
+    if (n < 2 * (size_t)nt)
+        nt = 1;
+    std::vector<std::vector<uint8_t>> part(nt);
+    auto work = [&](unsigned t) {
+        for (size_t i = n * t / nt; i < n * (t + 1) / nt; ++i) {
+            RoundBuilder rb;
+            rb.np = np;
+            rb.g = g;
+            rb.d = d;
+            rb.parent = parents.data() + i * pl;
+            rb.out = &part[t];
+            rb.run();
+        }
+    };
+    if (nt == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nt; ++t)
+            th.emplace_back(work, t);
+        for (auto &x : th)
+            x.join();
+    }
+    out.clear();
+    for (auto &p : part)
+        out.insert(out.end(), p.begin(), p.end());
+}
+
+}  // namespace
+
+extern "C" int canon_enumerate_ksys_groups(canon_ctx *c, uint32_t np, uint32_t g, canon_design_cb cb, void *user,
+                                           canon_enum_stats *stats) {
+    if (!c)
+        return CANON_EINVAL;
+    if (g == 2)
+        return canon_enumerate_ksys(c, np, cb, user, stats);
+    if ((g != 3 && g != 4) || np > 16 || np % g || np / g < 2 || (np - 1) % (g - 1)) {
+        c->err = "enumerate ksys groups: group size 3 or 4, np <= 16 a multiple of it with (np - 1) a "
+                 "multiple of g - 1";
+        return CANON_EINVAL;
+    }
+    if (c->n_bitems || c->n_kitems) {
+        c->err = "enumerate ksys groups: the context's queue must be empty (canon_sync first)";
+        return CANON_EINVAL;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rounds = (int)((np - 1) / (g - 1));
+    canon_enum_stats st{};
+    // the check's |Aut| and relabelings tried are read back: no verdict-only sync here
+    const uint32_t saved_options = c->cfg.options;
+    c->cfg.options &= ~CANON_OPT_VERDICT_SYNC;
+    std::vector<uint8_t> parents(np), children, kept;
+    for (uint32_t p = 0; p < np; ++p)
+        parents[p] = (uint8_t)p;
+    int rc = CANON_OK;
+    for (int d = 1; d < rounds && !parents.empty() && rc == CANON_OK; ++d) {
+        const auto g0 = std::chrono::steady_clock::now();
+        build_level(parents, d, (int)np, (int)g, children);
+        st.gen_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - g0).count();
+        const size_t cl = (size_t)(d + 1) * np, m = children.size() / cl;
+        st.level_checks[d] += m;
+        st.checks += m;
+        kept.clear();
+        const uint32_t cap = canon::batch_capacity(c, 0, (uint32_t)cl);
+        if (!cap) {
+            c->err = "enumerate ksys groups: the context holds no matrix of this size";
+            rc = CANON_ENOMEM;
+            break;
+        }
+        for (size_t lo = 0; lo < m && rc == CANON_OK; lo += cap) {
+            const uint32_t n = (uint32_t)std::min<size_t>(cap, m - lo);
+            canon_ksys_batch bt{};
+            bt.n = n;
+            bt.np = np;
+            bt.rounds = (uint32_t)(d + 1);
+            bt.data = children.data() + lo * cl;
+            rc = canon_submit_ksys_groups(c, &bt, g);
+            canon_results r{};
+            if (rc == CANON_OK)
+                rc = canon_sync(c, &r);
+            if (rc != CANON_OK)
+                break;
+            ++st.batches;
+            st.kernel_ms += r.kernel_ms;
+            st.level_kernel_ms[d] += r.kernel_ms;
+            for (uint32_t i = 0; i < n; ++i) {
+                st.trials += r.trials[i];
+                if (r.status[i]) {
+                    c->err = "enumerate ksys groups: a built round was refused by the check";
+                    rc = CANON_EINVAL;
+                    break;
+                }
+                if (!r.canonical[i])
+                    continue;
+                const uint8_t *child = children.data() + (lo + i) * cl;
+                if (d + 1 == rounds) {
+                    ++st.designs;
+                    if (cb)
+                        cb(user, child, (uint32_t)rounds, np, r.aut[2 * (size_t)i], r.aut[2 * (size_t)i + 1]);
+                } else {
+                    kept.insert(kept.end(), child, child + cl);
+                }
+            }
+        }
+        st.levels = (uint32_t)d;
+        parents.swap(kept);
+    }
+    c->cfg.options = saved_options;
+    st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (stats)
+        *stats = st;
+    return rc;
+}

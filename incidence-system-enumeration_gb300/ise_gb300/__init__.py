@@ -55,7 +55,8 @@ HEADER_SYMBOLS = [
     "canon_submit_ksys_groups", "canon_sync", "canon_set_ordering", "canon_canonize_bibd", "canon_check_bibd_device",
     "canon_generate_sts_device", "canon_device_alloc", "canon_device_free", "canon_memcpy_d2h",
     "canon_memcpy_h2d", "canon_last_kernel_ms", "canon_kernel_launches", "canon_stream_sync",
-    "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys", "canon_mlp_features",
+    "canon_check_bibd_noalloc", "canon_enumerate_bibd", "canon_enumerate_ksys",
+    "canon_enumerate_ksys_groups", "canon_mlp_features",
     "canon_label_first_rows", "canon_mlp_forward", "canon_mlp_grad", "canon_mlp_train",
     "canon_design_properties", "canon_report_bibd", "canon_ksys_cycles", "canon_report_ksys",
     "canon_tune_bibd", "canon_generate_partial_bibd", "canon_generate_partial_ksys", "canon_lexmax_nodes_bibd",
@@ -192,6 +193,7 @@ def load_library(path=LIB_PATH):
     L.canon_check_bibd_noalloc.argtypes = [u32, u32, u32, u32, vp, vp, ctypes.POINTER(DeviceOutputs), u64, vp]
     L.canon_enumerate_bibd.argtypes = [vp, u32, u32, u32, u32, u32, DESIGN_CB, vp, ctypes.POINTER(EnumStats)]
     L.canon_enumerate_ksys.argtypes = [vp, u32, DESIGN_CB, vp, ctypes.POINTER(EnumStats)]
+    L.canon_enumerate_ksys_groups.argtypes = [vp, u32, u32, DESIGN_CB, vp, ctypes.POINTER(EnumStats)]
     fp = ctypes.POINTER(ctypes.c_float)
     L.canon_mlp_features.argtypes = [vp, u32, u32, u32, vp, vp]
     L.canon_label_first_rows.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp, vp]
@@ -534,6 +536,20 @@ class Context:
         c = DESIGN_CB(cb)
         st = EnumStats()
         self._check(self.lib.canon_enumerate_ksys(self.h, np_, c, None, ctypes.byref(st)))
+        return found, st
+
+    def enumerate_ksys_groups(self, np_, g):
+        """All k-systems of np players in groups of g (2, 3 or 4) up to isomorphism:
+        [(rounds x np uint8, |Aut|)], stats."""
+        found = []
+
+        def cb(user, M, rows, cols, lo, hi):
+            found.append((np.ctypeslib.as_array(M, shape=(rows * cols,)).reshape(rows, cols).copy(),
+                          int(lo) | (int(hi) << 64)))
+
+        c = DESIGN_CB(cb)
+        st = EnumStats()
+        self._check(self.lib.canon_enumerate_ksys_groups(self.h, np_, g, c, None, ctypes.byref(st)))
         return found, st
 
     # ---- learned search order ----

@@ -315,6 +315,16 @@ int canon_enumerate_bibd(canon_ctx *ctx, uint32_t v, uint32_t b, uint32_t r, uin
  * alldata::Run() for group size 2 with the check at every level (TripleSys.cpp:80-775,
  * check at checkCurrentResult.cpp:91).  np even, <= 12. */
 int canon_enumerate_ksys(canon_ctx *ctx, uint32_t np, canon_design_cb cb, void *user, canon_enum_stats *stats);
+/* All k-systems of np players in groups of g = 3 or 4 with (np - 1) / (g - 1) rounds
+ * (resolvable designs with blocks of g, e.g. the Kirkman triple systems of 15 players)
+ * up to isomorphism, by orderly generation: the next rounds of every canonical parent are
+ * built on the host cores (every partition into groups that repeats no pair, in result()
+ * form, ordered by second entry), checked in batches on the GPU (canon_submit_ksys_groups)
+ * and the canonical ones kept: alldata::Run() for group size 3 or 4 with the check at
+ * every level (k-Factorization/TripleSys/Source/TripleSys.cpp:80-775).  g = 2 is
+ * canon_enumerate_ksys.  np <= 16; the context's queue must be empty. */
+int canon_enumerate_ksys_groups(canon_ctx *ctx, uint32_t np, uint32_t g, canon_design_cb cb, void *user,
+                                canon_enum_stats *stats);
 
 /* ---- seeded inputs of an uneven batched check ----
  * n partial BIBD(v, b, r, k, lambda) incidence matrices made by random backtracking of

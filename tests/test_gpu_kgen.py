@@ -141,3 +141,51 @@ def test_refused_batches(ctx):
     ctx.submit_ksys_groups(k8[0][0][None], 8, 7, 2)
     r = ctx.sync()
     assert r["n"] == 1 and r["canonical"][0]
+
+
+def test_enumeration_gives_the_reference_kirkman_systems(ctx):
+    """Orderly generation of k-systems with groups of 3 (canon_enumerate_ksys_groups: the
+    next rounds of every canonical parent built on the host, checked on the GPU) gives
+    the 7 Kirkman triple systems of 15 players of the reference's K_OrderedMatrices.txt,
+    matrix for matrix, with its |Aut(M)|."""
+    found, st = ctx.enumerate_ksys_groups(15, 3)
+    kts = cases.load_kts15()
+    assert sorted((R.tobytes(), a) for R, a in found) == sorted((R.tobytes(), a) for R, a in kts)
+    assert st.designs == 7 and st.level_checks[6] == 8
+
+
+def covers_every_pair_once(R, g):
+    n = R.shape[1]
+    seen = np.zeros((n, n), int)
+    for row in R:
+        for q in range(0, n, g):
+            grp = row[q:q + g]
+            for a in grp:
+                for b in grp:
+                    if a != b:
+                        seen[a, b] += 1
+    return bool((seen + np.eye(n, dtype=int) == 1).all())
+
+
+def test_enumeration_of_the_affine_planes_of_order_3_and_4(ctx):
+    """The resolvable designs with blocks of 3 on 9 points and of 4 on 16 are the affine
+    planes AG(2,3) and AG(2,4), each with one resolution: one system each, with |Aut| the
+    order of the affine semilinear group, 9 x 48 = 432 and 16 x 180 x 2 = 5760."""
+    found, _ = ctx.enumerate_ksys_groups(9, 3)
+    assert len(found) == 1 and found[0][1] == 432
+    R = found[0][0]
+    assert covers_every_pair_once(R, 3)
+    o = oracle.ksys_test(R, g=3)
+    assert o["canonical"] and o["n_aut"] == 432
+    found, _ = ctx.enumerate_ksys_groups(16, 4)
+    assert len(found) == 1 and found[0][1] == 5760
+    assert covers_every_pair_once(found[0][0], 4)
+
+
+def test_enumeration_routes_and_refusals(ctx):
+    a, _ = ctx.enumerate_ksys_groups(8, 2)
+    b, _ = ctx.enumerate_ksys(8)
+    assert [(R.tobytes(), x) for R, x in a] == [(R.tobytes(), x) for R, x in b]
+    for np_, g in [(12, 3), (12, 4), (18, 3), (15, 5)]:
+        with pytest.raises(G.CanonError):
+            ctx.enumerate_ksys_groups(np_, g)
