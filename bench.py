@@ -385,8 +385,12 @@ ENUM_WORKLOADS = {
     "enum-12-22": ("bibd", (12, 22, 11, 6, 5), "all BIBD(12,22,11,6,5) (11,603 designs) by orderly generation"),
     "enum-9-36": ("bibd", (9, 36, 12, 3, 3), "all BIBD(9,36,12,3,3) (22,521 designs) by orderly generation"),
     "enum-16-24": ("bibd", (16, 24, 9, 6, 3), "all BIBD(16,24,9,6,3) (18,920 designs) by orderly generation"),
+    # k-systems with groups of 3 and 4 (the reference's 15x7x3 run: 7 matrices, 2.44 s on 10
+    # threads from its 26 start matrices of 4 rounds); the oracle has no enumeration for them
+    "enum-kts15": ("kgroups", (15, 3), "all k-systems of 15 players in groups of 3: the 7 Kirkman triple systems"),
+    "enum-ag24": ("kgroups", (16, 4), "all k-systems of 16 players in groups of 4: the resolution of AG(2,4)"),
 }
-ENUM_NO_CPU = {"enum-12-22", "enum-9-36", "enum-16-24"}
+ENUM_NO_CPU = {"enum-12-22", "enum-9-36", "enum-16-24", "enum-kts15", "enum-ag24"}
 
 
 def run_enum(args):
@@ -401,6 +405,8 @@ def run_enum(args):
             l0 = ctx.kernel_launches()
         if kind == "bibd":
             found, st = ctx.enumerate_bibd(*params)
+        elif kind == "kgroups":
+            found, st = ctx.enumerate_ksys_groups(*params)
         else:
             found, st = ctx.enumerate_ksys(*params)
         runs.append((len(found), st.checks, st.seconds, st.kernel_ms, st.batches,
@@ -435,7 +441,7 @@ def run_enum(args):
             "checks_per_s": checks / secs, "kernel_ms_per_step": sum(r[3] for r in timed) / args.steps,
             "gen_ms_per_step": 1e3 * sum(r[7] for r in timed) / args.steps,
             "cpu_baseline": cpu, "gpu_launches": launches}
-    if kind == "ksys":
+    if kind in ("ksys", "kgroups"):
         # relabelings the checks tried (cnvCheckNew candidates), the k-system check's unit of work
         line["relabelings_tried_per_step"] = timed[0][8]
     print(json.dumps(line), flush=True)
