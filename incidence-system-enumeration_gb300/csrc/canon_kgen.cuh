@@ -48,7 +48,8 @@ __host__ __device__ __forceinline__ uint32_t kg_key(const uint32_t *l, unsigned 
 
 // player p of a sorted round given as keys (the key picked by compares, so that the
 // keys stay in registers)
-__host__ __device__ __forceinline__ unsigned kg_key_player(const uint32_t *key, unsigned p, unsigned g) {
+template <unsigned g>
+__host__ __device__ __forceinline__ unsigned kg_key_player(const uint32_t *key, unsigned p) {
     const unsigned k = p / g;
     uint32_t v = key[0];
 #pragma unroll
@@ -57,38 +58,71 @@ __host__ __device__ __forceinline__ unsigned kg_key_player(const uint32_t *key, 
     return (v >> (4u * (3u - p % g))) & 15u;
 }
 
-// Relabeling c of the matrix in T (np players in ng groups of g, nr rounds).
-// heap = the Heap permutations of ng groups (6 bytes each, group indices), perms = the
-// g! in-group orders (g bytes each).  Returns 0 for an automorphism (the identity, c = 0,
-// without a comparison, cnv.cpp:85-89), > 0 when the relabelled matrix is greater and -1
-// when it is smaller; then pi_out = min(pidx0, the m_playerIndex candidate of
-// setPlayerIndex() / setPlayerIndexByPos(), kmSupport.cpp:314-356).
-__host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigned g, unsigned ng, unsigned nr,
-                                                const KgTables &T, const uint8_t *heap, const uint8_t *perms,
-                                                int pidx0, int &pi_out) {
-    const unsigned gf = g == 3 ? 6u : 24u;
+// In-group order t (0 .. G!-1) of cnvInit(): the G! orders of 0 .. G-1 in lexicographic
+// order, entry j of order t taken from t's factorial digits (the j-th digit picks one of
+// the entries not yet used), so no table is read.  Returned nibble-packed, entry j at 4j.
+template <unsigned G>
+__host__ __device__ __forceinline__ unsigned kg_group_order(unsigned t) {
+    unsigned left = G == 3 ? 0x210u : 0x3210u;   // the entries not yet used, ascending
+    unsigned out = 0, radix = G == 3 ? 2u : 6u;   // (G - 1 - j)!
+#pragma unroll
+    for (unsigned j = 0; j + 1 < G; ++j) {
+        const unsigned k = t / radix;
+        t -= k * radix;
+        const unsigned sh = 4u * k;
+        out |= ((left >> sh) & 15u) << (4u * j);
+        left = (left & ((1u << sh) - 1u)) | ((left >> (sh + 4u)) << sh);
+        radix = j + 2 < G ? radix / (G - 1u - j) : 1u;
+    }
+    out |= (left & 15u) << (4u * (G - 1u));
+    return out;
+}
+
+// Relabeling c of the matrix in T (np players in ng groups of G, nr rounds).
+// heap = the Heap permutations of ng groups (6 bytes each, group indices).  Returns 0 for
+// an automorphism (the identity, c = 0, without a comparison, cnv.cpp:85-89), > 0 when
+// the relabelled matrix is greater and -1 when it is smaller; then pi_out = min(pidx0,
+// the m_playerIndex candidate of setPlayerIndex() / setPlayerIndexByPos(),
+// kmSupport.cpp:314-356).  G is a compile-time constant so that every division by the
+// group size or by G! is a multiplication.
+template <unsigned G>
+__host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigned ng, unsigned nr,
+                                                const KgTables &T, const uint8_t *heap, int pidx0, int &pi_out) {
+    constexpr unsigned g = G, gf = G == 3 ? 6u : 24u;
     unsigned gfn = 1;
     for (unsigned i = 0; i < ng; ++i)
         gfn *= gf;
     const unsigned d = c % nr;
     const unsigned q = c / nr;
-    const unsigned tgi = q % gfn;
+    unsigned tgi = q % gfn;
     const unsigned h = q / gfn;
     const uint8_t *a = heap + h * 6u;
+    // the in-group order of every group, the first group most significant
+    unsigned tg[KG_NGMAX];
+#pragma unroll
+    for (int i = KG_NGMAX - 1; i >= 0; --i) {
+        tg[i] = 0;
+        if ((unsigned)i < ng) {
+            tg[i] = tgi % gf;
+            tgi /= gf;
+        }
+    }
     // the labels of round d's positions (cnvCheckKm, cnv.cpp:168-185): ttr = player ->
     // label, inv = label -> player
     uint64_t ttr = 0, inv = 0;
     const uint64_t sd = T.seq[d];
-    unsigned div = gfn;
-    for (unsigned i = 0; i < ng; ++i) {
-        div /= gf;
-        const unsigned tg = (tgi / div) % gf;
-        const unsigned base = (unsigned)a[i] * g;
-        for (unsigned j = 0; j < g; ++j) {
-            const unsigned lab = base + perms[tg * g + j];
-            const unsigned pl = nib_get(sd, i * g + j);
-            ttr |= (uint64_t)lab << (4u * pl);
-            inv |= (uint64_t)pl << (4u * lab);
+#pragma unroll
+    for (unsigned i = 0; i < (unsigned)KG_NGMAX; ++i) {
+        if (i < ng) {
+            const unsigned ord = kg_group_order<G>(tg[i]);
+            const unsigned base = (unsigned)a[i] * g;
+#pragma unroll
+            for (unsigned j = 0; j < g; ++j) {
+                const unsigned lab = base + ((ord >> (4u * j)) & 15u);
+                const unsigned pl = nib_get(sd, i * g + j);
+                ttr |= (uint64_t)lab << (4u * pl);
+                inv |= (uint64_t)pl << (4u * lab);
+            }
         }
     }
     if (c == 0)
@@ -164,13 +198,13 @@ __host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigne
             const unsigned imax = np - g - 1;
             unsigned ip = imax;
             for (unsigned p = kd * g; p < imax; ++p)
-                if (kg_key_player(key, p, g) < nib_get(T.seq[i], p)) {
+                if (kg_key_player<g>(key, p) < nib_get(T.seq[i], p)) {
                     ip = p;
                     break;
                 }
             unsigned j = 0;
             for (unsigned p = 0; p <= ip; ++p) {
-                const unsigned tp = nib_get(T.pos[r], nib_get(inv, kg_key_player(key, p, g)));
+                const unsigned tp = nib_get(T.pos[r], nib_get(inv, kg_key_player<g>(key, p)));
                 j = tp > j ? tp : j;
             }
             const int cand = (int)(r * np + j);

@@ -161,11 +161,8 @@ __global__ void ksys_seg_finish_kernel(const Item *__restrict__ items, uint32_t 
 // outputs are those of the segmented check of group size 2: one (segment, item) unit per
 // warp task, the first rejection kept by an atomic minimum of (candidate << 32 | player
 // index), |Aut| reported for canonical matrices.
-__constant__ uint8_t c_gperm3[6 * 3];  // the 3! in-group orders of cnvInit()
-__constant__ uint8_t c_gperm4[24 * 4];
-
 // Loads one item's rounds into the warp's tables and checks their form (all 32 lanes).
-__device__ bool kg_load(const Item &item, unsigned g, const uint8_t *__restrict__ bytes, KgTables &T,
+__device__ __noinline__ bool kg_load(const Item &item, unsigned g, const uint8_t *__restrict__ bytes, KgTables &T,
                         unsigned lane) {
     const unsigned np = item.ncols, nr = item.nrows, ng = np / g;
     bool ok = item.kind == KIND_KSYS && kg_shape_ok(np, g, nr);
@@ -250,6 +247,7 @@ __global__ void __launch_bounds__(KTPB) kgen_seg_kernel(const Item *__restrict__
         const uint64_t total = kg_total(np, g, nr);
         const uint64_t end = start + seg_cands < total ? start + seg_cands : total;
         const int pidx0 = (int)(nr * np) - (int)g - 1;
+        const uint8_t *heap = ksys::c_heap + ksys::c_heap_off[np / g] * 6u;
         unsigned n_aut = 0;
         for (uint64_t base = start; base < end; base += 32u) {
             if ((volatile_key(&st.key) >> 32) < base)
@@ -257,8 +255,8 @@ __global__ void __launch_bounds__(KTPB) kgen_seg_kernel(const Item *__restrict__
             const unsigned c = (unsigned)base + lane;
             int res = 1, pi = pidx0;
             if (c < end)
-                res = kg_eval(c, np, g, np / g, nr, s_t[warp], ksys::c_heap + ksys::c_heap_off[np / g] * 6u,
-                              g == 3 ? c_gperm3 : c_gperm4, pidx0, pi);
+                res = g == 3 ? kg_eval<3>(c, np, np / 3u, nr, s_t[warp], heap, pidx0, pi)
+                             : kg_eval<4>(c, np, np / 4u, nr, s_t[warp], heap, pidx0, pi);
             const unsigned rej = __ballot_sync(0xFFFFFFFFu, c < end && res < 0);
             const unsigned aut = __ballot_sync(0xFFFFFFFFu, c < end && res == 0);
             if (rej) {
@@ -402,33 +400,7 @@ cudaError_t ksys_upload_tables() {
                 p[i] = (uint8_t)i;
         }
     }
-    // the in-group orders of cnvInit() for groups of 3 and 4: the g-digit base-g numbers
-    // in increasing order whose digits are all different
-    uint8_t g3[6 * 3], g4[24 * 4];
-    for (int gs = 3; gs <= 4; ++gs) {
-        uint8_t *dst = gs == 3 ? g3 : g4;
-        int cnt = 0;
-        const int lim = gs == 3 ? 27 : 256;
-        for (int x = 0; x < lim; ++x) {
-            int digit[4], y = x;
-            unsigned seen = 0;
-            for (int j = gs - 1; j >= 0; --j) {
-                digit[j] = y % gs;
-                y /= gs;
-                seen |= 1u << digit[j];
-            }
-            if (seen != (1u << gs) - 1u)
-                continue;
-            for (int j = 0; j < gs; ++j)
-                dst[cnt * gs + j] = (uint8_t)digit[j];
-            ++cnt;
-        }
-    }
-    cudaError_t e = cudaMemcpyToSymbol(c_gperm3, g3, sizeof(g3));
-    if (e == cudaSuccess)
-        e = cudaMemcpyToSymbol(c_gperm4, g4, sizeof(g4));
-    if (e == cudaSuccess)
-        e = cudaMemcpyToSymbol(ksys::c_heap, heap, sizeof(heap));
+    cudaError_t e = cudaMemcpyToSymbol(ksys::c_heap, heap, sizeof(heap));
     if (e == cudaSuccess)
         e = cudaMemcpyToSymbol(ksys::c_heap_off, off, sizeof(off));
     if (e == cudaSuccess)

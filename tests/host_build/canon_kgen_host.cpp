@@ -40,12 +40,6 @@ extern "C" int emu_kgen_check(const uint8_t *R, int nr, int np, int g, int *cano
     const int ng = np / g;
     static uint8_t heap[720 * 6];
     heap_rows(ng, heap);
-    uint8_t perms[24 * 4];
-    uint8_t cur[4] = {0, 1, 2, 3};
-    int cnt = 0;
-    do {
-        std::memcpy(perms + g * cnt++, cur, (size_t)g);
-    } while (std::next_permutation(cur, cur + g));
     canon::KgTables T;
     std::memset(&T, 0, sizeof(T));
     for (int r = 0; r < nr; ++r) {
@@ -68,8 +62,10 @@ extern "C" int emu_kgen_check(const uint8_t *R, int nr, int np, int g, int *cano
     *cands = total - 1;
     for (uint64_t c = 0; c < total; ++c) {
         int pi = pidx0;
-        const int res = canon::kg_eval((unsigned)c, (unsigned)np, (unsigned)g, (unsigned)ng, (unsigned)nr, T, heap,
-                                       perms, pidx0, pi);
+        const int res = g == 3 ? canon::kg_eval<3>((unsigned)c, (unsigned)np, (unsigned)ng, (unsigned)nr, T, heap,
+                                                   pidx0, pi)
+                               : canon::kg_eval<4>((unsigned)c, (unsigned)np, (unsigned)ng, (unsigned)nr, T, heap,
+                                                   pidx0, pi);
         if (res == 0)
             ++*n_aut;
         if (res < 0) {
