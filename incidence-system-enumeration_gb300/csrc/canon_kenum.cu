@@ -9,6 +9,7 @@
 #include <chrono>
 #include <cstring>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/canon_gb300.h"
@@ -66,6 +67,8 @@ bool links_complete(const uint32_t *used, int np, int g) {
 // groups (links_complete).  Appended to out as parent + round.
 struct RoundBuilder {
     int np, g, d;
+    int second;            // the first partner of player 0 (the round's second entry)
+    bool links;            // apply links_complete to the children
     const uint8_t *parent;
     uint32_t used[16];
     uint8_t row[16];
@@ -80,7 +83,7 @@ struct RoundBuilder {
                     u[row[q + e]] |= 1u << row[q + f];
                     u[row[q + f]] |= 1u << row[q + e];
                 }
-        if (!links_complete(u, np, g))
+        if (links && !links_complete(u, np, g))
             return;
         out->insert(out->end(), parent, parent + (size_t)d * np);
         out->insert(out->end(), row, row + np);
@@ -104,6 +107,8 @@ struct RoundBuilder {
             return;
         }
         unsigned m = allowed & ~((1u << minp) - 1u);
+        if (pos == 1)
+            m &= 1u << second;
         while (m) {
             const int p = __builtin_ctz(m);
             m &= m - 1u;
@@ -125,21 +130,36 @@ struct RoundBuilder {
     }
 };
 
-// the children of every parent (in parent order), built on up to 16 host threads
+// the children of every parent (in parent order), built on up to 16 host threads; the
+// unit of work is (parent, second entry of the new round), so the single parent of the
+// first level is split too, and units in order give the children in order
 void build_level(const std::vector<uint8_t> &parents, int d, int np, int g, std::vector<uint8_t> &out) {
     const size_t pl = (size_t)d * np, n = parents.size() / pl;
+    std::vector<std::pair<uint32_t, uint8_t>> units;
+    for (size_t i = 0; i < n; ++i)
+        for (int b = parents[i * pl + (size_t)(d - 1) * np + 1] + 1; b < np; ++b)
+            units.emplace_back((uint32_t)i, (uint8_t)b);
+    const size_t nu = units.size();
+    // The links test drops almost nothing while more than half of the rounds are still to
+    // come (the 15-player triples: 20 of 16,450 children with 3 rounds, none with 2) and
+    // costs more than building the rounds, so it runs once at most half remain (69,795 ->
+    // 298 children with 4 rounds).
+    const int total_rounds = (np - 1) / (g - 1), left = total_rounds - (d + 1);
+    const bool links = 2 * left <= total_rounds - 1;
     unsigned nt = std::thread::hardware_concurrency();
     nt = nt > 16 ? 16 : (nt < 1 ? 1 : nt);
-    if (n < 2 * (size_t)nt)
+    if (nu < 2 * (size_t)nt)
         nt = 1;
     std::vector<std::vector<uint8_t>> part(nt);
     auto work = [&](unsigned t) {
-        for (size_t i = n * t / nt; i < n * (t + 1) / nt; ++i) {
+        for (size_t k = nu * t / nt; k < nu * (t + 1) / nt; ++k) {
             RoundBuilder rb;
             rb.np = np;
             rb.g = g;
             rb.d = d;
-            rb.parent = parents.data() + i * pl;
+            rb.second = units[k].second;
+            rb.links = links;
+            rb.parent = parents.data() + (size_t)units[k].first * pl;
             rb.out = &part[t];
             rb.run();
         }
@@ -188,7 +208,9 @@ extern "C" int canon_enumerate_ksys_groups(canon_ctx *c, uint32_t np, uint32_t g
     for (int d = 1; d < rounds && !parents.empty() && rc == CANON_OK; ++d) {
         const auto g0 = std::chrono::steady_clock::now();
         build_level(parents, d, (int)np, (int)g, children);
-        st.gen_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - g0).count();
+        const double gs = std::chrono::duration<double>(std::chrono::steady_clock::now() - g0).count();
+        st.gen_seconds += gs;
+        st.level_gen_ms[d] += 1e3 * gs;
         const size_t cl = (size_t)(d + 1) * np, m = children.size() / cl;
         st.level_checks[d] += m;
         st.checks += m;

@@ -128,11 +128,17 @@ __host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigne
     if (c == 0)
         return 0;
     // the second entry of every relabelled round: the least label among the group-mates
-    // of the player labelled 0; the output rounds in increasing order of it
+    // of the player labelled 0; the output rounds in increasing order of it.  Round d
+    // becomes 0 1 .. np-1 (its groups take the label blocks whole), round 0 of the matrix:
+    // it is the first output round (second entry 1; every other round has a larger one, as
+    // the player labelled 1 meets the player labelled 0 in round d only), and it is equal,
+    // so the comparison starts at output round 1 with day_max = d.
     const unsigned u = nib_get(inv, 0);
     unsigned mask2 = 0;
     uint64_t srcof = 0;
     for (unsigned r = 0; r < nr; ++r) {
+        if (r == d)
+            continue;
         const unsigned gi = nib_get(T.pos[r], u) / g;
         unsigned m = 15;
         for (unsigned e = 0; e < g; ++e) {
@@ -145,8 +151,8 @@ __host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigne
         mask2 |= 1u << m;
         srcof = nib_set(srcof, m, r);
     }
-    unsigned day_max = nib_get(srcof, kg_ctz(mask2));
-    for (unsigned i = 0; mask2; ++i) {
+    unsigned day_max = d;
+    for (unsigned i = 1; mask2; ++i) {
         const unsigned m = kg_ctz(mask2);
         mask2 &= mask2 - 1u;
         const unsigned r = nib_get(srcof, m);

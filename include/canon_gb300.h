@@ -294,7 +294,7 @@ typedef struct {
     double   gen_seconds; /* time spent generating the candidates (host wall time, or
                              device time of the generation kernels) */
     uint64_t trials;      /* k-systems: relabelings tried by all checks (cnvCheckNew candidates) */
-    double   level_gen_ms[16]; /* BIBDs: per level, the wall time of generating its candidates */
+    double   level_gen_ms[16]; /* BIBDs and groups of 3 or 4: per level, the wall time of generating its candidates */
 } canon_enum_stats;
 
 /* Called for every canonical complete matrix: BIBD rows as rows x uint64 (cast to
