@@ -489,8 +489,6 @@ int canon_submit_ksys_groups(canon_ctx *c, const canon_ksys_batch *bt, uint32_t 
         return fail(c, CANON_EINVAL,
                     "ksys batch: need data, np <= 16 a multiple of the group size (2 groups at least), "
                     "1 <= rounds < np");
-    if (bt->flags & CANON_SAVE_AUTS)
-        return fail(c, CANON_EINVAL, "ksys batch: CANON_SAVE_AUTS is not available for groups of 3 or 4");
     if (bt->flags & ~0xFu)
         return fail(c, CANON_EINVAL, "ksys batch: unknown flags");
     if (c->n_bitems || (c->n_kitems && !c->q_ks_groups))

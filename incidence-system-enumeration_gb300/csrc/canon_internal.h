@@ -173,8 +173,8 @@ cudaError_t launch_ksys_check_split(const Item *d_items, uint32_t n_items, const
                                    uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
                                    cudaStream_t s, const uint64_t *d_n = nullptr);
 // the check of k-systems with groups of 3 or 4 (np <= 16; Item::pad holds the group
-// size), split into segments of seg_cands relabelings over warps; automorphisms are not
-// stored
+// size), split into segments of seg_cands relabelings over warps; automorphisms are stored
+// (CANON_SAVE_AUTS) for canonical matrices, unordered (canon_sync sorts them)
 cudaError_t launch_kgen_check(const Item *d_items, uint32_t n_items, const uint8_t *d_bytes, Outputs out,
                               uint32_t seg_cands, uint64_t total_max, KsysSeg *d_state, int num_sms,
                               cudaStream_t s);

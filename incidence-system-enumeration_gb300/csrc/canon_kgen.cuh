@@ -83,11 +83,13 @@ __host__ __device__ __forceinline__ unsigned kg_group_order(unsigned t) {
 // an automorphism (the identity, c = 0, without a comparison, cnv.cpp:85-89), > 0 when
 // the relabelled matrix is greater and -1 when it is smaller; then pi_out = min(pidx0,
 // the m_playerIndex candidate of setPlayerIndex() / setPlayerIndexByPos(),
-// kmSupport.cpp:314-356).  G is a compile-time constant so that every division by the
-// group size or by G! is a multiplication.
+// kmSupport.cpp:314-356).  ttr_out = the relabeling (player -> label, nibble-packed), the
+// permutation an automorphism is stored as.  G is a compile-time constant so that every
+// division by the group size or by G! is a multiplication.
 template <unsigned G>
 __host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigned ng, unsigned nr,
-                                                const KgTables &T, const uint8_t *heap, int pidx0, int &pi_out) {
+                                                const KgTables &T, const uint8_t *heap, int pidx0, int &pi_out,
+                                                uint64_t &ttr_out) {
     constexpr unsigned g = G, gf = G == 3 ? 6u : 24u;
     unsigned gfn = 1;
     for (unsigned i = 0; i < ng; ++i)
@@ -125,6 +127,7 @@ __host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigne
             }
         }
     }
+    ttr_out = ttr;
     if (c == 0)
         return 0;
     // the second entry of every relabelled round: the least label among the group-mates

@@ -215,10 +215,14 @@ __device__ __noinline__ bool kg_load(const Item &item, unsigned g, const uint8_t
     return ok;
 }
 
+// With CANON_SAVE_AUTS an item's automorphisms are counted one by one in KsysSeg::n_aut,
+// whose old value is the arena slot each one is written to (the first aut_cap of them, in
+// the order the warps find them; canon_sync sorts the stored set as CGroupInfo keeps it);
+// they are reported for canonical matrices, whose every relabeling is tried.
 __global__ void __launch_bounds__(KTPB) kgen_seg_kernel(const Item *__restrict__ items, uint32_t n_items,
                                                         const uint8_t *__restrict__ bytes, uint32_t seg_cands,
                                                         uint64_t n_units, KsysSeg *state,
-                                                        unsigned long long *ticket) {
+                                                        unsigned long long *ticket, Outputs out) {
     __shared__ KgTables s_t[KW];
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     for (;;) {
@@ -248,15 +252,18 @@ __global__ void __launch_bounds__(KTPB) kgen_seg_kernel(const Item *__restrict__
         const uint64_t end = start + seg_cands < total ? start + seg_cands : total;
         const int pidx0 = (int)(nr * np) - (int)g - 1;
         const uint8_t *heap = ksys::c_heap + ksys::c_heap_off[np / g] * 6u;
+        const bool save = (item.flags & F_SAVE_AUTS) && out.auts;
+        uint8_t *arena = save ? out.auts + (size_t)item.out_idx * out.aut_cap * 64u : nullptr;
         unsigned n_aut = 0;
         for (uint64_t base = start; base < end; base += 32u) {
             if ((volatile_key(&st.key) >> 32) < base)
                 break;
             const unsigned c = (unsigned)base + lane;
             int res = 1, pi = pidx0;
+            uint64_t ttr = 0;
             if (c < end)
-                res = g == 3 ? kg_eval<3>(c, np, np / 3u, nr, s_t[warp], heap, pidx0, pi)
-                             : kg_eval<4>(c, np, np / 4u, nr, s_t[warp], heap, pidx0, pi);
+                res = g == 3 ? kg_eval<3>(c, np, np / 3u, nr, s_t[warp], heap, pidx0, pi, ttr)
+                             : kg_eval<4>(c, np, np / 4u, nr, s_t[warp], heap, pidx0, pi, ttr);
             const unsigned rej = __ballot_sync(0xFFFFFFFFu, c < end && res < 0);
             const unsigned aut = __ballot_sync(0xFFFFFFFFu, c < end && res == 0);
             if (rej) {
@@ -265,7 +272,16 @@ __global__ void __launch_bounds__(KTPB) kgen_seg_kernel(const Item *__restrict__
                     atomicMin(&st.key, ((unsigned long long)c << 32) | (unsigned)pi);
                 break;
             }
-            n_aut += __popc(aut);
+            if (save) {
+                if ((aut >> lane) & 1u) {
+                    const unsigned slot = atomicAdd(&st.n_aut, 1u);
+                    if (slot < out.aut_cap)
+                        for (unsigned x = 0; x < np; ++x)
+                            arena[(size_t)slot * 64u + x] = (uint8_t)nib_get(ttr, x);
+                }
+            } else {
+                n_aut += __popc(aut);
+            }
         }
         if (lane == 0 && n_aut)
             atomicAdd(&st.n_aut, n_aut);
@@ -283,7 +299,9 @@ __global__ void kgen_finish_kernel(const Item *__restrict__ items, uint32_t n_it
         const bool canonical = ok && st.key == ~0ull;
         const uint64_t cands = !ok ? 0 : canonical ? kg_total(np, g, nr) - 1 : (st.key >> 32);
         const int pidx = canonical || !ok ? (int)(nr * np) - (int)g - 1 : (int)(uint32_t)st.key;
-        write_item(out, item.out_idx, ok, canonical, false, pidx, st.n_aut, cands, false, np);
+        const bool save = canonical && (item.flags & F_SAVE_AUTS) && out.auts;
+        write_item(out, item.out_idx, ok, canonical, save && st.n_aut > out.aut_cap, pidx, st.n_aut, cands, save,
+                   np);
     }
 }
 
@@ -506,7 +524,8 @@ cudaError_t launch_kgen_check(const Item *d_items, uint32_t n_items, const uint8
     if (e != cudaSuccess)
         return e;
     unsigned long long *ticket = reinterpret_cast<unsigned long long *>(d_state + n_items);
-    kgen_seg_kernel<<<(int)grid, ksys::KTPB, 0, s>>>(d_items, n_items, d_bytes, seg_cands, units, d_state, ticket);
+    kgen_seg_kernel<<<(int)grid, ksys::KTPB, 0, s>>>(d_items, n_items, d_bytes, seg_cands, units, d_state, ticket,
+                                                     out);
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return e;

@@ -187,8 +187,10 @@ int canon_submit_ksys(canon_ctx *ctx, const canon_ksys_batch *batch);
  * group size, 2 groups at least), rounds as result() rows (players ascending inside a
  * group, groups ordered by first player, round 0 = 0 1 .. np-1).  Every relabeling,
  * (np/g)! * (g!)^(np/g) per round, is tried on the GPU.  Outputs as for group size 2;
- * CANON_SAVE_AUTS is refused.  Such batches form a queue of their own: no incidence or
- * group-size-2 batch may be queued with them before canon_sync. */
+ * with CANON_SAVE_AUTS the automorphisms of a canonical matrix are stored as a sorted set
+ * (none for a rejected one; beyond aut_cap, CANON_ST_PERM_OVF and aut_cap of them, not
+ * necessarily the first in the reference's order).  Such batches form a queue of their
+ * own: no incidence or group-size-2 batch may be queued with them before canon_sync. */
 int canon_submit_ksys_groups(canon_ctx *ctx, const canon_ksys_batch *batch, uint32_t group_size);
 /* Copy the queued input to the GPU, run the checks, wait, expose the results. */
 int canon_sync(canon_ctx *ctx, canon_results *out);

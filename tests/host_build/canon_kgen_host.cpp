@@ -62,10 +62,11 @@ extern "C" int emu_kgen_check(const uint8_t *R, int nr, int np, int g, int *cano
     *cands = total - 1;
     for (uint64_t c = 0; c < total; ++c) {
         int pi = pidx0;
+        uint64_t ttr = 0;
         const int res = g == 3 ? canon::kg_eval<3>((unsigned)c, (unsigned)np, (unsigned)ng, (unsigned)nr, T, heap,
-                                                   pidx0, pi)
+                                                   pidx0, pi, ttr)
                                : canon::kg_eval<4>((unsigned)c, (unsigned)np, (unsigned)ng, (unsigned)nr, T, heap,
-                                                   pidx0, pi);
+                                                   pidx0, pi, ttr);
         if (res == 0)
             ++*n_aut;
         if (res < 0) {

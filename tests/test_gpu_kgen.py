@@ -128,8 +128,6 @@ def test_refused_batches(ctx):
     with pytest.raises(G.CanonError):
         ctx.submit_ksys_groups(R, 15, 7, 5)
     with pytest.raises(G.CanonError):
-        ctx.submit_ksys_groups(R, 15, 7, 3, G.SAVE_AUTS)
-    with pytest.raises(G.CanonError):
         ctx.submit_ksys_groups(np.zeros((1, 3, 14), np.uint8), 14, 3, 3)
     ctx.submit_ksys_groups(R, 15, 7, 3)
     k8, _ = oracle.ksys_enumerate(8)
@@ -189,3 +187,32 @@ def test_enumeration_routes_and_refusals(ctx):
     for np_, g in [(12, 3), (12, 4), (18, 3), (15, 5)]:
         with pytest.raises(G.CanonError):
             ctx.enumerate_ksys_groups(np_, g)
+
+
+def test_automorphisms_stored_as_the_oracle_stores_them(ctx):
+    """CANON_SAVE_AUTS with groups of 3: the automorphisms of a canonical matrix are the
+    oracle's CGroupInfo set (sorted relabelings, identity first); beyond aut_cap the item
+    reports CANON_ST_PERM_OVF with aut_cap of them stored; a rejected matrix stores none."""
+    kts = cases.load_kts15()
+    big = G.Context(max_items=1024, aut_cap=200)
+    try:
+        picks = [next(R for R, a in kts if a == 12), next(R for R, a in kts if a == 168), kts[0][0][:2],
+                 kts[3][0][:3]]
+        rng = np.random.default_rng(5)
+        rejected = cases.ksys_relabel_random(kts[2][0], rng, g=3)
+        for X in picks + [rejected]:
+            big.submit_ksys_groups(X[None], 15, X.shape[0], 3, G.SAVE_AUTS)
+            r = big.sync()
+            o = oracle.ksys_test(X, g=3, aut_cap=256)
+            assert bool(r["canonical"][0]) == o["canonical"]
+            if not o["canonical"]:
+                assert r["n_auts"][0] == 0 and r["aut"][0] == 0
+                continue
+            n = o["n_aut"]
+            assert r["aut"][0] == n and r["status"][0] == (G.ST_PERM_OVF if n > 200 else 0)
+            if n <= 200:
+                assert r["n_auts"][0] == n
+                got = r["auts_raw"][0][:n, :15]
+                assert np.array_equal(got, o["auts"]), X.shape
+    finally:
+        big.close()
