@@ -19,13 +19,13 @@ namespace {
 
 constexpr int KB_TPB = 64;
 
-// data: n k-systems of `days` rounds x np bytes (result() rows, groups of 2);
-// out: n x np x (days * np / 2) bytes; aut (optional): labelings reaching the form
-__global__ void __launch_bounds__(KB_TPB) kbin_kernel(uint32_t n, uint32_t np, uint32_t days, int free_days,
-                                                      const uint8_t *__restrict__ data, uint8_t *out, uint64_t *aut,
-                                                      uint8_t *status, uint64_t max_nodes) {
+// data: n k-systems of `days` rounds x np bytes (result() rows, groups of k);
+// out: n x np x (days * np / k) bytes; aut (optional): labelings reaching the form
+__global__ void __launch_bounds__(KB_TPB) kbin_kernel(uint32_t n, uint32_t np, uint32_t k, uint32_t days,
+                                                      int free_days, const uint8_t *__restrict__ data, uint8_t *out,
+                                                      uint64_t *aut, uint8_t *status, uint64_t max_nodes) {
     using namespace canon::kbin;
-    const uint32_t g = np / 2, b = days * g;
+    const uint32_t g = np / k, b = days * g;
     for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x) {
         const uint8_t *R = data + (size_t)it * days * np;
         uint64_t rows[KB_VMAX] = {};
@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(KB_TPB) kbin_kernel(uint32_t n, uint32_t np, u
                     break;
                 }
                 seen |= 1u << p;
-                rows[p] |= 1ull << (d * g + q / 2);
+                rows[p] |= 1ull << (d * g + q / k);
             }
         }
         uint8_t *o = out + (size_t)it * np * b;
@@ -80,20 +80,21 @@ int fail(canon_ctx *c, int rc, const char *msg) {
 
 extern "C" {
 
-int canon_canonize_ksys_binary(canon_ctx *c, uint32_t n, uint32_t np, uint32_t days, const uint8_t *data,
-                               uint8_t *out, uint64_t *aut_out) {
+int canon_canonize_ksys_binary_groups(canon_ctx *c, uint32_t n, uint32_t np, uint32_t k, uint32_t days,
+                                      const uint8_t *data, uint8_t *out, uint64_t *aut_out) {
     if (!c || (n && (!data || !out)))
         return fail(c, CANON_EINVAL, "canonize k-system: null argument");
-    const uint32_t num_days = np - 1;
-    if (np < 6 || np > (uint32_t)canon::kbin::KB_VMAX || (np & 1u) || days < 2 || days > num_days ||
-        days * (np / 2) > (uint32_t)canon::kbin::KB_BMAX)
-        return fail(c, CANON_EINVAL, "canonize k-system: need np even in 6..16, 2 <= days <= np-1, "
-                                     "days * np/2 <= 63");
+    if (k < 2 || k > 4 || np % k || (np - 1) % (k - 1) || np < 3 * k || np > (uint32_t)canon::kbin::KB_VMAX)
+        return fail(c, CANON_EINVAL, "canonize k-system: need groups of 2, 3 or 4 and np <= 16 a multiple of "
+                                     "the group size with (np-1) a multiple of k-1");
+    const uint32_t num_days = (np - 1) / (k - 1);
+    if (days < 2 || days > num_days || days * (np / k) > (uint32_t)canon::kbin::KB_BMAX)
+        return fail(c, CANON_EINVAL, "canonize k-system: need 2 <= days <= (np-1)/(k-1), days * np/k <= 63");
     if (!n)
         return CANON_OK;
     cudaSetDevice(c->device);
     cudaStream_t s = c->stream;
-    const uint32_t b = days * (np / 2);
+    const uint32_t b = days * (np / k);
     const size_t in_bytes = (size_t)n * days * np, out_bytes = (size_t)n * np * b;
     uint8_t *d_in = nullptr, *d_out = nullptr, *d_st = nullptr;
     uint64_t *d_aut = nullptr;
@@ -112,7 +113,7 @@ int canon_canonize_ksys_binary(canon_ctx *c, uint32_t n, uint32_t np, uint32_t d
         if (grid > cap)
             grid = cap;
         cudaEventRecord(c->ev0, s);
-        kbin_kernel<<<grid, KB_TPB, 0, s>>>(n, np, days, days == num_days ? 1 : 0, d_in, d_out, d_aut, d_st,
+        kbin_kernel<<<grid, KB_TPB, 0, s>>>(n, np, k, days, days == num_days ? 1 : 0, d_in, d_out, d_aut, d_st,
                                             c->cfg.max_trials);
         e = cudaGetLastError();
         cudaEventRecord(c->ev1, s);
@@ -141,7 +142,7 @@ int canon_canonize_ksys_binary(canon_ctx *c, uint32_t n, uint32_t np, uint32_t d
     int rc = CANON_OK;
     for (uint32_t i = 0; i < n; ++i) {
         if (st[i] & canon::ST_BADINPUT)
-            rc = fail(c, CANON_EINVAL, "canonize k-system: a round is not a perfect matching of the players");
+            rc = fail(c, CANON_EINVAL, "canonize k-system: a round is not a partition of the players");
         else if (st[i] & canon::ST_TIMEOUT && rc == CANON_OK)
             rc = fail(c, CANON_ETIMEOUT, "canonize k-system: the search hit its node budget");
     }
@@ -150,10 +151,18 @@ int canon_canonize_ksys_binary(canon_ctx *c, uint32_t n, uint32_t np, uint32_t d
     return rc;
 }
 
+int canon_canonize_ksys_binary(canon_ctx *c, uint32_t n, uint32_t np, uint32_t days, const uint8_t *data,
+                               uint8_t *out, uint64_t *aut_out) {
+    if (c && (np & 1u))
+        return fail(c, CANON_EINVAL, "canonize k-system: need np even in 6..16, 2 <= days <= np-1, "
+                                     "days * np/2 <= 63");
+    return canon_canonize_ksys_binary_groups(c, n, np, 2, days, data, out, aut_out);
+}
+
 // ---- the reference's plugin ----------------------------------------------------
 // createCanonizer(v, k) prepares the canonizer of k-systems of v players in groups of
 // k (the C_InSys of v+1 rows and numDays*v/k columns, CDTools.cpp:5-14); here, a
-// context on the first GPU and a result buffer.  Group size 2 only.
+// context on the first GPU and a result buffer.  Groups of 2, 3 or 4.
 struct KsysCanonizer {
     canon_ctx *ctx;
     int v, k, num_days;
@@ -161,9 +170,11 @@ struct KsysCanonizer {
 };
 
 void *createCanonizer(int v, int k) {
-    if (k != 2 || v < 6 || v > canon::kbin::KB_VMAX || (v % k))
+    if (k < 2 || k > 4 || v < 3 * k || v > canon::kbin::KB_VMAX || (v % k) || (v - 1) % (k - 1))
         return nullptr;
     const int num_days = (v - 1) / (k - 1);
+    if (num_days * (v / k) > canon::kbin::KB_BMAX)
+        return nullptr;
     canon_cfg cfg{};
     cfg.device = 0;
     cfg.max_items = 16;
@@ -205,8 +216,8 @@ const unsigned char *runCanonizer(void *pCanonizer, const unsigned char *pMatrix
     const int days = iDay <= 0 ? h->num_days : iDay;
     if (days < 2 || days > h->num_days)
         return nullptr;
-    const int rc = canon_canonize_ksys_binary(h->ctx, 1, (uint32_t)h->v, (uint32_t)days, pMatrix, h->result,
-                                              nullptr);
+    const int rc = canon_canonize_ksys_binary_groups(h->ctx, 1, (uint32_t)h->v, (uint32_t)h->k, (uint32_t)days,
+                                                     pMatrix, h->result, nullptr);
     return rc == CANON_OK ? h->result : nullptr;
 }
 

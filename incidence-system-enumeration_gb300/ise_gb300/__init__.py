@@ -60,7 +60,8 @@ HEADER_SYMBOLS = [
     "canon_label_first_rows", "canon_mlp_forward", "canon_mlp_grad", "canon_mlp_train",
     "canon_design_properties", "canon_report_bibd", "canon_ksys_cycles", "canon_report_ksys",
     "canon_tune_bibd", "canon_generate_partial_bibd", "canon_generate_partial_ksys", "canon_lexmax_nodes_bibd",
-    "canon_measure_int_peak", "canon_canonize_ksys_binary", "canon_set_ksys_segment",
+    "canon_measure_int_peak", "canon_canonize_ksys_binary", "canon_canonize_ksys_binary_groups",
+    "canon_set_ksys_segment",
 ]
 # the reference's plugin (k-Factorization/Utils/Include/CDTools.h:9-11)
 PLUGIN_SYMBOLS = ["createCanonizer", "releaseCanonizer", "runCanonizer"]
@@ -218,6 +219,7 @@ def load_library(path=LIB_PATH):
     L.canon_lexmax_nodes_bibd.argtypes = [vp, u32, u32, u32, u32, vp, vp, vp]
     L.canon_measure_int_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.canon_canonize_ksys_binary.argtypes = [vp, u32, u32, u32, u8p, u8p, u64p]
+    L.canon_canonize_ksys_binary_groups.argtypes = [vp, u32, u32, u32, u32, u8p, u8p, u64p]
     L.createCanonizer.argtypes = [ctypes.c_int, ctypes.c_int]
     L.createCanonizer.restype = vp
     L.releaseCanonizer.argtypes = [vp]
@@ -494,16 +496,22 @@ class Context:
         self._check(self.lib.canon_measure_int_peak(self.h, ctypes.byref(x)))
         return x.value
 
-    def canonize_ksys_binary(self, data, np_, days):
-        """Canonical binary matrices (n x np x days*np/2) of n k-systems' first `days`
-        rounds, and the labelings reaching each (canon_canonize_ksys_binary)."""
+    def canonize_ksys_binary(self, data, np_, days, k=2):
+        """Canonical binary matrices (n x np x days*np/k) of n k-systems' first `days`
+        rounds (groups of k), and the labelings reaching each (canon_canonize_ksys_binary,
+        canon_canonize_ksys_binary_groups for k > 2)."""
         X = np.ascontiguousarray(data, np.uint8).reshape(-1, days, np_)
         n = X.shape[0]
-        b = days * np_ // 2
+        b = days * np_ // k
         out = np.zeros((n, np_, b), np.uint8)
         aut = np.zeros(n, np.uint64)
-        self._check(self.lib.canon_canonize_ksys_binary(self.h, n, np_, days, _ptr(X, ctypes.c_uint8),
-                                                        _ptr(out, ctypes.c_uint8), _ptr(aut, ctypes.c_uint64)))
+        if k == 2:
+            rc = self.lib.canon_canonize_ksys_binary(self.h, n, np_, days, _ptr(X, ctypes.c_uint8),
+                                                     _ptr(out, ctypes.c_uint8), _ptr(aut, ctypes.c_uint64))
+        else:
+            rc = self.lib.canon_canonize_ksys_binary_groups(self.h, n, np_, k, days, _ptr(X, ctypes.c_uint8),
+                                                            _ptr(out, ctypes.c_uint8), _ptr(aut, ctypes.c_uint64))
+        self._check(rc)
         return out, aut
 
     def tune_bibd(self, n, v, b, flags, d_rows):

@@ -366,9 +366,10 @@ int canon_generate_partial_ksys(uint32_t np, uint32_t n, uint64_t seed, uint32_t
  * (Source/MatrixCanonChecker.cpp:420-564): the lexicographically greatest matrix over
  * permutations of the players, of the groups inside each day and, when all days are
  * given, of the days.  v rows of iDay*v/k bytes, owned by the canonizer and valid until
- * its next call; NULL on error.  Group size k = 2, v even, 6 <= v <= 16; the
- * canonizer holds a context on GPU 0.  Not thread-safe per canonizer (as the
- * reference's). */
+ * its next call; NULL on error.  Group size k = 2, 3 or 4, v <= 16 a multiple of k with
+ * (v-1) a multiple of k-1 and at least 3 groups a day (k = 2: v even, 6 <= v <= 16;
+ * k = 3: v = 9 or 15; k = 4: v = 16); the canonizer holds a context on GPU 0.  Not
+ * thread-safe per canonizer (as the reference's). */
 void *createCanonizer(int v, int k);
 void releaseCanonizer(void *pCanonizer);
 const unsigned char *runCanonizer(void *pCanonizer, const unsigned char *pMatrix, int k, int iDay);
@@ -378,6 +379,10 @@ const unsigned char *runCanonizer(void *pCanonizer, const unsigned char *pMatrix
  * k-system. */
 int canon_canonize_ksys_binary(canon_ctx *ctx, uint32_t n, uint32_t np, uint32_t days, const uint8_t *data,
                                uint8_t *out, uint64_t *aut_out);
+/* The same with groups of k = 2, 3 or 4 players (out = n x np x (days*np/k) bytes); the
+ * shapes createCanonizer takes. */
+int canon_canonize_ksys_binary_groups(canon_ctx *ctx, uint32_t n, uint32_t np, uint32_t k, uint32_t days,
+                                      const uint8_t *data, uint8_t *out, uint64_t *aut_out);
 
 /* ---- result tables (the reference's text output of a finished run) ----
  * Per complete design: simple[i] = no two equal columns (no replicated blocks) and

@@ -74,3 +74,40 @@ def test_complete_k10_is_invariant_and_separates_the_396(ctx):
             assert np.array_equal(can.run(k10[i][0]), out[i])
     finally:
         can.close()
+
+
+def test_groups_of_3_and_4_match_the_oracle(ctx):
+    """Groups of 3 and 4 (canon_canonize_ksys_binary_groups and the plugin with k = 3, 4):
+    the 7 Kirkman triple systems of 15 players and relabelled copies, all days (|Aut(M)|
+    as the labelings reaching the form) and prefixes through runCanonizer; the resolution
+    of AG(2,4) (groups of 4) from the enumeration."""
+    rng = np.random.default_rng(15)
+    kts = cases.load_kts15()
+    mats = [R for R, _ in kts] + [cases.ksys_relabel_random(R, rng, g=3) for R, _ in kts]
+    out, aut = ctx.canonize_ksys_binary(np.stack(mats), 15, 7, k=3)
+    for i, (R, a) in enumerate(kts):
+        ref, _ = oracle.ksys_binary_canonize(R, 15, 3)
+        assert np.array_equal(out[i], ref) and np.array_equal(out[len(kts) + i], ref)
+        assert aut[i] == a and aut[len(kts) + i] == a
+    can = G.Canonizer(15, 3)
+    try:
+        for R, _ in kts[::3]:
+            for d in (2, 3, 5, 6):
+                ref, _ = oracle.ksys_binary_canonize(R[:d], 15, 3, d)
+                assert np.array_equal(can.run(R, d), ref), d
+            assert np.array_equal(can.run(R), oracle.ksys_binary_canonize(R, 15, 3)[0])
+        assert can.run(kts[0][0], 1) is None and can.run(kts[0][0], 8) is None
+    finally:
+        can.close()
+    found, _ = ctx.enumerate_ksys_groups(16, 4)
+    R = found[0][0]
+    out, aut = ctx.canonize_ksys_binary(R[None], 16, 5, k=4)
+    assert np.array_equal(out[0], oracle.ksys_binary_canonize(R, 16, 4)[0]) and aut[0] == 5760
+    can = G.Canonizer(16, 4)
+    try:
+        assert np.array_equal(can.run(R, 3), oracle.ksys_binary_canonize(R[:3], 16, 4, 3)[0])
+    finally:
+        can.close()
+    for v, k in [(12, 3), (12, 4), (15, 5)]:
+        with pytest.raises(G.CanonError):
+            G.Canonizer(v, k)

@@ -89,3 +89,43 @@ def test_k10_prefixes_match_the_oracle(kb):
             X = relabel(R[:d], rng, 10, False)
             assert np.array_equal(oracle.ksys_binary_canonize(X, 10, 2, d)[0], ref)
             assert np.array_equal(run(kb, X, 10, d, False)[0], ref)
+
+
+def binary_rows_k(R, np_, days, k):
+    """convertToBinaryMatrix with groups of k: column d*g + j = group j of day d"""
+    g = np_ // k
+    rows = np.zeros(np_, np.uint64)
+    for d in range(days):
+        for j in range(g):
+            for p in R[d][k * j: k * j + k]:
+                rows[p] |= np.uint64(1) << np.uint64(d * g + j)
+    return rows
+
+
+def run_k(L, R, np_, days, free, k):
+    g = np_ // k
+    rows = binary_rows_k(R, np_, days, k)
+    out = np.zeros(np_, np.uint64)
+    leaves, nodes = ctypes.c_uint64(), ctypes.c_uint64()
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    assert L.emu_kbin(rows.ctypes.data_as(u64p), np_, days * g, g, days, int(free), out.ctypes.data_as(u64p),
+                      ctypes.byref(leaves), ctypes.byref(nodes)) == 0
+    b = days * g
+    return ((out[:, None] >> np.arange(b, dtype=np.uint64)) & np.uint64(1)).astype(np.uint8), leaves.value
+
+
+def test_kirkman_systems_match_the_oracle_with_groups_of_3(kb):
+    """The same search on the 7 Kirkman triple systems of 15 players (groups of 3, 5
+    columns a day): every prefix of 2..6 days (day order fixed) and the complete systems
+    (days permuted), against the oracle's restatement; the labelings reaching the form
+    of a complete system are its |Aut(M)|, and relabelled copies reach the same form."""
+    rng = np.random.default_rng(3)
+    for R, aut in cases.load_kts15():
+        for d in (2, 4, 6):
+            ref, _ = oracle.ksys_binary_canonize(R[:d], 15, 3, d)
+            assert np.array_equal(run_k(kb, R[:d], 15, d, False, 3)[0], ref), d
+        ref, _ = oracle.ksys_binary_canonize(R, 15, 3)
+        got, leaves = run_k(kb, R, 15, 7, True, 3)
+        assert np.array_equal(got, ref) and leaves == aut
+        X = cases.ksys_relabel_random(R, rng, g=3)
+        assert np.array_equal(run_k(kb, X, 15, 7, True, 3)[0], ref)
