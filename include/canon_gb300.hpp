@@ -63,9 +63,9 @@ public:
     }
     // queue k-system matrices (rounds of pairs in the reference's result() form)
     void submitKSys(const uint8_t *data, uint32_t n, uint32_t np, uint32_t rounds, uint32_t flags,
-                    const uint8_t *nrows = nullptr) {
+                    const uint8_t *nrows = nullptr, uint32_t groupSize = 2) {
         canon_ksys_batch bt{n, np, rounds, flags, data, nrows};
-        check(canon_submit_ksys(ctx_, &bt));
+        check(groupSize == 2 ? canon_submit_ksys(ctx_, &bt) : canon_submit_ksys_groups(ctx_, &bt, groupSize));
     }
     const canon_results &sync() {
         check(canon_sync(ctx_, &res_));
@@ -126,9 +126,11 @@ private:
 
 class GpuKSysChecker {
 public:
-    GpuKSysChecker(Context &ctx, uint32_t numPlayers) : ctx_(ctx), np_(numPlayers) {}
+    // groupSize: m_groupSize of the alldata object (2, 3 or 4)
+    GpuKSysChecker(Context &ctx, uint32_t numPlayers, uint32_t groupSize = 2)
+        : ctx_(ctx), np_(numPlayers), g_(groupSize) {}
     bool cnvCheckNew(uint32_t nrows, const uint8_t *result) {
-        ctx_.submitKSys(result, 1, np_, nrows, CANON_SAVE_AUTS);
+        ctx_.submitKSys(result, 1, np_, nrows, CANON_SAVE_AUTS, nullptr, g_);
         const canon_results &r = ctx_.sync();
         if (r.status[0] & CANON_ST_BADINPUT)
             throw Error(CANON_EINVAL, "rounds are not in the result() form");
@@ -140,7 +142,7 @@ public:
 
 private:
     Context &ctx_;
-    uint32_t np_;
+    uint32_t np_, g_;
 };
 
 // RAII owner of the reference's plugin handle (createCanonizer / runCanonizer /
@@ -149,7 +151,8 @@ class Canonizer {
 public:
     Canonizer(int v, int k) : h_(createCanonizer(v, k)) {
         if (!h_)
-            throw Error(CANON_EINVAL, "createCanonizer failed (k = 2, even v in 6..16, a GPU)");
+            throw Error(CANON_EINVAL, "createCanonizer failed (k = 2 with even v in 6..16, k = 3 with v = 9 or 15, "
+                                      "k = 4 with v = 16; a GPU)");
     }
     ~Canonizer() { releaseCanonizer(h_); }
     Canonizer(const Canonizer &) = delete;
