@@ -1,4 +1,6 @@
-// canon_ksys.cu -- canonicity test of k-systems (rounds of pairs, group size 2) on sm_103a.
+// canon_ksys.cu -- canonicity test of k-systems on sm_103a: rounds of pairs (group size
+// 2, below), and rounds of groups of 3 or 4 (kgen_seg_kernel, with the relabeling step of
+// canon_kgen.cuh).
 //
 // Restates alldata::cnvCheckNew() on its plain path
 // (k-Factorization/TripleSys/Source/cnv.cpp:211-351): every relabeling that maps
