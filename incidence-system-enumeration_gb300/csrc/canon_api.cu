@@ -22,6 +22,7 @@
 #include "../../include/canon_gb300.h"
 #include "canon_internal.h"
 #include "canon_ctx.h"
+#include "canon_hostpool.h"
 
 using canon::Item;
 using canon::Outputs;
@@ -204,78 +205,6 @@ cudaError_t compute_orders(canon_ctx *c, uint32_t n, uint32_t v, uint32_t b, con
 
 namespace {
 
-// Host threads kept for the packing of batches: starting and joining 16 threads costs
-// about 0.35 ms on a Grace host, a quarter of the submit of a 100 MB batch.  run(n, job)
-// calls job(0 .. n-1) on the calling thread and the pool's, and returns when every call has
-// ended and no pool thread still holds the job.  Calls from several host threads are
-// serialised.  The pool lives until the process ends (its threads wait for work).
-class HostPool {
-  public:
-    static HostPool &get() {
-        static HostPool *pool = new HostPool();
-        return *pool;
-    }
-    unsigned threads() const { return (unsigned)workers_.size() + 1u; }
-    void run(unsigned n, const std::function<void(unsigned)> &job) {
-        std::lock_guard<std::mutex> serial(run_mu_);
-        {
-            std::lock_guard<std::mutex> lk(mu_);
-            job_ = &job;
-            n_ = n;
-            done_ = 0;
-            next_.store(0);
-            ++gen_;
-        }
-        cv_work_.notify_all();
-        const unsigned k = take(job, n);
-        std::unique_lock<std::mutex> lk(mu_);
-        done_ += k;
-        cv_done_.wait(lk, [&] { return done_ == n_ && active_ == 0; });
-        job_ = nullptr;
-    }
-
-  private:
-    HostPool() {
-        unsigned nt = std::thread::hardware_concurrency();
-        nt = nt > 16 ? 16 : (nt < 1 ? 1 : nt);
-        for (unsigned t = 1; t < nt; ++t)
-            workers_.emplace_back([this] { loop(); });
-        for (auto &w : workers_)
-            w.detach();
-    }
-    unsigned take(const std::function<void(unsigned)> &job, unsigned n) {
-        unsigned k = 0;
-        for (unsigned t; (t = next_.fetch_add(1)) < n; ++k)
-            job(t);
-        return k;
-    }
-    void loop() {
-        uint64_t seen = 0;
-        for (;;) {
-            std::unique_lock<std::mutex> lk(mu_);
-            cv_work_.wait(lk, [&] { return gen_ != seen && job_ != nullptr; });
-            seen = gen_;
-            const std::function<void(unsigned)> *job = job_;
-            const unsigned n = n_;
-            ++active_;
-            lk.unlock();
-            const unsigned k = take(*job, n);
-            lk.lock();
-            done_ += k;
-            --active_;
-            if (done_ == n_ && active_ == 0)
-                cv_done_.notify_all();
-        }
-    }
-    std::vector<std::thread> workers_;
-    std::mutex run_mu_, mu_;
-    std::condition_variable cv_work_, cv_done_;
-    const std::function<void(unsigned)> *job_ = nullptr;
-    unsigned n_ = 0, done_ = 0, active_ = 0;
-    uint64_t gen_ = 0;
-    std::atomic<unsigned> next_{0};
-};
-
 // The work descriptors of a batch, in order of filled rows (stable), built on the pool.
 // Matrices with the same number of filled rows run the same loops, and the threads of a
 // warp take consecutive descriptors from the work counter, so sorted descriptors keep a
@@ -287,7 +216,7 @@ class HostPool {
 template <typename Copy, typename Make>
 bool pack_items_by_rows(uint64_t n, const uint8_t *nrows, uint32_t maxr, Item *dst, Copy copy, Make make) {
     constexpr unsigned NB = 17;   // row counts 0 .. 16
-    HostPool &pool = HostPool::get();
+    canon::HostPool &pool = canon::HostPool::get();
     const unsigned nt = n < (1u << 16) ? 1u : pool.threads();
     std::vector<uint64_t> at((size_t)nt * NB, 0);
     std::atomic<bool> bad{false};

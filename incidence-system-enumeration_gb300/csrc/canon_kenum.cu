@@ -15,6 +15,7 @@
 #include "../../include/canon_gb300.h"
 #include "canon_ctx.h"
 #include "canon_internal.h"
+#include "canon_hostpool.h"
 #include "canon_kenum_rounds.h"
 
 namespace {
@@ -37,12 +38,10 @@ void build_level(const std::vector<uint8_t> &parents, int d, int np, int g, std:
     // 298 children with 4 rounds).
     const int total_rounds = (np - 1) / (g - 1), left = total_rounds - (d + 1);
     const bool links = 2 * left <= total_rounds - 1;
-    unsigned nt = std::thread::hardware_concurrency();
-    nt = nt > 16 ? 16 : (nt < 1 ? 1 : nt);
-    if (nu < 2 * (size_t)nt)
-        nt = 1;
+    canon::HostPool &pool = canon::HostPool::get();
+    const unsigned nt = nu < 2 ? 1u : (nu < pool.threads() ? (unsigned)nu : pool.threads());
     std::vector<std::vector<uint8_t>> part(nt);
-    auto work = [&](unsigned t) {
+    const std::function<void(unsigned)> work = [&](unsigned t) {
         for (size_t k = nu * t / nt; k < nu * (t + 1) / nt; ++k) {
             RoundBuilder rb;
             rb.np = np;
@@ -55,15 +54,10 @@ void build_level(const std::vector<uint8_t> &parents, int d, int np, int g, std:
             rb.run();
         }
     };
-    if (nt == 1) {
+    if (nt == 1)
         work(0);
-    } else {
-        std::vector<std::thread> th;
-        for (unsigned t = 0; t < nt; ++t)
-            th.emplace_back(work, t);
-        for (auto &x : th)
-            x.join();
-    }
+    else
+        pool.run(nt, work);
     out.clear();
     for (auto &p : part)
         out.insert(out.end(), p.begin(), p.end());

@@ -23,7 +23,6 @@
 // generation makes the result independent of the visiting order: every prefix
 // of a canonical matrix is canonical, so the canonical complete matrices are
 // exactly those the depth-first search finds.
-#include <sched.h>
 
 #include <algorithm>
 #include <chrono>
@@ -34,6 +33,7 @@
 #include "../../include/canon_gb300.h"
 #include "canon_ctx.h"
 #include "canon_internal.h"
+#include "canon_hostpool.h"
 #include "canon_rows.cuh"
 #include "canon_ksys_rounds.cuh"
 
@@ -388,37 +388,15 @@ struct PinBuf {
     ~PinBuf() { cudaFreeHost(p); }
 };
 
-// the host cores this process may run on (its CPU affinity), not every core of
-// the machine: a container or a job slot often holds fewer
-unsigned host_threads() {
-    cpu_set_t set;
-    CPU_ZERO(&set);
-    if (sched_getaffinity(0, sizeof(set), &set) == 0) {
-        const int c = CPU_COUNT(&set);
-        if (c > 0)
-            return (unsigned)c;
-    }
-    const unsigned n = std::thread::hardware_concurrency();
-    return n ? n : 1;
-}
-
-// fn(lo, hi) over [0, n) on all host cores, in contiguous ranges
+// fn(lo, hi) over [0, n) on the host cores (the persistent pool), in contiguous ranges;
+// a level of a few parents stays on the calling thread
 template <typename F>
 void parallel_ranges(uint64_t n, F fn) {
-    unsigned nt = host_threads();
-    if (nt > 64)
-        nt = 64;
-    if (n < 256)
-        nt = 1;
-    if (nt == 1) {
+    if (n < 16) {
         fn((uint64_t)0, n);
         return;
     }
-    std::vector<std::thread> th;
-    for (unsigned t = 0; t < nt; ++t)
-        th.emplace_back(fn, n * t / nt, n * (t + 1) / nt);
-    for (auto &x : th)
-        x.join();
+    canon::HostPool::get().ranges(n, fn);
 }
 
 // ---- k-system rounds on the device ----------------------------------------
