@@ -159,37 +159,51 @@ __host__ __device__ __forceinline__ int kg_eval(unsigned c, unsigned np, unsigne
         const unsigned m = kg_ctz(mask2);
         mask2 &= mask2 - 1u;
         const unsigned r = nib_get(srcof, m);
-        // the relabelled round r as sorted keys
-        uint32_t key[KG_NGMAX];
+        // the relabelled round r as sorted keys.  The group holding label 0 sorts first, and
+        // its key alone usually decides (a relabelled round is mostly greater or smaller from
+        // its second entry on), so it is compared before the other groups are built
+        uint32_t key[KG_NGMAX] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+        const unsigned g0 = nib_get(T.pos[r], u) / g;
+        {
+            uint32_t l[4];
 #pragma unroll
-        for (unsigned k = 0; k < (unsigned)KG_NGMAX; ++k) {
-            key[k] = 0xFFFFFFFFu;
-            if (k < ng) {
-                uint32_t l[4];
-#pragma unroll
-                for (unsigned e = 0; e < 4; ++e)
-                    l[e] = e < g ? (uint32_t)nib_get(ttr, nib_get(T.seq[r], k * g + e)) : 0u;
-                key[k] = kg_key(l, g);
-            }
+            for (unsigned e = 0; e < 4; ++e)
+                l[e] = e < g ? (uint32_t)nib_get(ttr, nib_get(T.seq[r], g0 * g + e)) : 0u;
+            key[0] = kg_key(l, g);
         }
-#pragma unroll
-        for (unsigned x = 1; x < (unsigned)KG_NGMAX; ++x)
-#pragma unroll
-            for (unsigned y = x; y > 0; --y)
-                if (key[y] < key[y - 1]) {
-                    const uint32_t t = key[y];
-                    key[y] = key[y - 1];
-                    key[y - 1] = t;
-                }
         int cmp = 0;
         unsigned kd = 0;
+        if (key[0] != T.okey[i][0]) {
+            cmp = key[0] < T.okey[i][0] ? -1 : 1;
+        } else {
 #pragma unroll
-        for (unsigned k = 0; k < (unsigned)KG_NGMAX; ++k) {
-            if (!cmp && k < ng) {
-                const uint32_t ok = T.okey[i][k];
-                if (key[k] != ok) {
-                    cmp = key[k] < ok ? -1 : 1;
-                    kd = k;
+            for (unsigned k = 1; k < (unsigned)KG_NGMAX; ++k) {
+                if (k < ng) {
+                    const unsigned grp = k - 1u + (k - 1u >= g0 ? 1u : 0u);   // the groups other than g0
+                    uint32_t l[4];
+#pragma unroll
+                    for (unsigned e = 0; e < 4; ++e)
+                        l[e] = e < g ? (uint32_t)nib_get(ttr, nib_get(T.seq[r], grp * g + e)) : 0u;
+                    key[k] = kg_key(l, g);
+                }
+            }
+#pragma unroll
+            for (unsigned x = 2; x < (unsigned)KG_NGMAX; ++x)
+#pragma unroll
+                for (unsigned y = x; y > 1; --y)
+                    if (key[y] < key[y - 1]) {
+                        const uint32_t t = key[y];
+                        key[y] = key[y - 1];
+                        key[y - 1] = t;
+                    }
+#pragma unroll
+            for (unsigned k = 1; k < (unsigned)KG_NGMAX; ++k) {
+                if (!cmp && k < ng) {
+                    const uint32_t ok = T.okey[i][k];
+                    if (key[k] != ok) {
+                        cmp = key[k] < ok ? -1 : 1;
+                        kd = k;
+                    }
                 }
             }
         }
