@@ -153,3 +153,29 @@ def test_links_test_against_completability(lib):
             assert ok == 1
         checked += 1
     assert checked > 0
+
+
+def test_orderly_enumeration_of_nine_players_in_triples(lib):
+    """The whole orderly generation with groups of 3 on 9 players, on the CPU: the host
+    round builder with its links test, the oracle's cnvCheckNew() as the check.  One
+    system results, AG(2,3) with its 4 parallel classes, |Aut| = 9 x 48 = 432 -- the result
+    the GPU enumeration gives (tests/test_gpu_kgen.py)."""
+    import oracle
+    level = [np.arange(9, dtype=np.uint8)[None, :]]
+    found = []
+    for d in range(1, 4):
+        nxt = []
+        for P in level:
+            for C in children(lib, P, 3, 2 * (4 - (d + 1)) <= 3):
+                o = oracle.ksys_test(C, g=3)
+                if not o["canonical"]:
+                    continue
+                if d + 1 == 4:
+                    found.append((C, o["n_aut"]))
+                else:
+                    nxt.append(C)
+        level = nxt
+    assert len(found) == 1 and found[0][1] == 432
+    R = found[0][0]
+    pairs = used_pairs(R, 3)
+    assert len(pairs) == 9 * 8      # every pair of players meets exactly once
