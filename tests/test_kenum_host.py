@@ -179,3 +179,25 @@ def test_orderly_enumeration_of_nine_players_in_triples(lib):
     R = found[0][0]
     pairs = used_pairs(R, 3)
     assert len(pairs) == 9 * 8      # every pair of players meets exactly once
+
+
+def test_orderly_enumeration_of_sixteen_players_in_fours(lib):
+    """The same on 16 players in groups of 4 (about 50 s on 8 host threads): one system,
+    the resolution of AG(2,4), with |Aut| = 16 x 180 x 2 = 5760 (the affine semilinear
+    group) -- a known answer that pins the oracle's check with groups of 4, and the result
+    of the GPU enumeration."""
+    import concurrent.futures as cf
+    import oracle
+    level = [np.arange(16, dtype=np.uint8)[None, :]]
+    found = []
+    with cf.ThreadPoolExecutor(max(1, min(8, os.cpu_count() or 1))) as ex:
+        for d in range(1, 5):
+            cands = [C for P in level for C in children(lib, P, 4, 2 * (5 - (d + 1)) <= 4)]
+            res = list(ex.map(lambda C: oracle.ksys_test(C, g=4), cands))
+            nxt = []
+            for C, o in zip(cands, res):
+                if o["canonical"]:
+                    (found.append((C, o["n_aut"])) if d + 1 == 5 else nxt.append(C))
+            level = nxt
+    assert len(found) == 1 and found[0][1] == 5760
+    assert len(used_pairs(found[0][0], 4)) == 16 * 15
